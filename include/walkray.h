@@ -1,0 +1,206 @@
+/*
+ * walkray.h — C ABI of the GB300 path-tracing library (libwalkray_gpu.so).
+ *
+ * This is the only boundary between host code and the sm_103a kernels.  It
+ * replaces, for WalkRay's unidirectional path tracer, the in-process calls
+ * that the reference makes between its renderer plugin and its scene:
+ *
+ *   reference interface (WalkRay)                    entry point here
+ *   ----------------------------------------------   ------------------------
+ *   Config::load builds objects + Scene::buildKDTree  wr_scene_upload
+ *     (config.cpp:432-519, scene.cpp:20-44)
+ *   KDTree::intersect / Scene::intersect             wr_trace_closest
+ *     (kdtree.cpp:349-353, scene.cpp:102-113,
+ *      NoSelfCondition::legal noself.cpp:13-20)
+ *   MCRenderer::renderPixels (mcRenderer.h:27),      wr_render
+ *     PathTracer::renderPixels (pathTracer.cpp:7-76)
+ *   RenderEngine::renderFilm (renderEngine.cpp:27-30) wr_submit/wr_poll/wr_fetch
+ *     called once per request                          (serving loop)
+ *
+ * Conventions: every function returns an int status (WR_OK or WR_ERR_*); no
+ * C++ exception crosses this boundary; wr_last_error() gives a message for
+ * the last failure on a context.  Host buffers belong to the caller; device
+ * memory belongs to the library.  A context is not thread-safe: use one per
+ * host thread, or serialise calls.
+ */
+#ifndef WALKRAY_H
+#define WALKRAY_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WR_ABI_VERSION 1u
+
+/* status codes */
+#define WR_OK 0
+#define WR_ERR_INVALID_ARGUMENT 1
+#define WR_ERR_OUT_OF_MEMORY 2
+#define WR_ERR_CUDA 3
+#define WR_ERR_NOT_FOUND 4
+#define WR_ERR_TIMEOUT 5
+#define WR_ERR_BUSY 6
+#define WR_ERR_CANCELLED 7
+#define WR_ERR_UNSUPPORTED 8
+#define WR_ERR_INTERNAL 9
+
+#define WR_NO_HIT 0xffffffffu
+#define WR_NO_OBJECT (-1)
+
+/* material / object kinds (one per reference scene-object class) */
+#define WR_MAT_DIFFUSE 0       /* DiffuseObject            diffuseObj.h */
+#define WR_MAT_GLOSSY 1        /* GlossyObject (iso Phong)  glossyObj.h */
+#define WR_MAT_ANISO 2         /* AnisotropicGlossyObject   anisotropicGlossyObj.h */
+#define WR_MAT_REFRACTIVE 3    /* RefractiveObject          refractiveObj.h */
+#define WR_MAT_EMISSIVE 4      /* EmissiveObject            emissiveObj.h */
+#define WR_MAT_HOMOGENEOUS 5   /* HomogeneousVolume         homogeneousVolume.h */
+#define WR_MAT_HETEROGENEOUS 6 /* HeterogeneousVolume       HeterogeneousVolume.h */
+
+/* One scene object: a triangle mesh with world-space vertices (the
+ * reference's Mesh with an identity transform) and its material.  Fields a
+ * material does not use are ignored.  136 bytes, all 4-byte fields. */
+typedef struct wr_object_desc {
+    uint32_t type;           /* WR_MAT_* */
+    uint32_t vert_begin;     /* first vertex of this object in wr_scene_desc.vertices */
+    uint32_t vert_count;
+    uint32_t tri_begin;      /* first triangle of this object in wr_scene_desc.triangles */
+    uint32_t tri_count;
+    uint32_t grid_index;     /* heterogeneous media: index into wr_scene_desc.grids */
+    float albedo[3];         /* diffuse / glossy reflectanceAlbedo */
+    float emission[3];       /* emissive color */
+    float power;             /* isotropic Phong exponent */
+    float ior;               /* refractive object / medium index of refraction */
+    float decay[3];          /* refractive decayColor (per unit distance) */
+    float rs[3];             /* anisotropic Phong Rs */
+    float rd[3];             /* anisotropic Phong Rd */
+    float nu, nv;            /* anisotropic Phong exponents */
+    float sigma_s[3];        /* media scattering coefficient */
+    float sigma_a[3];        /* media absorption coefficient */
+    float g;                 /* Henyey-Greenstein asymmetry */
+    float density_scale;     /* heterogeneous: density multiplier (reference default 100) */
+    float step_size;         /* heterogeneous: ray-marching step (reference default 0.002) */
+} wr_object_desc;
+
+/* Pinhole camera (Camera::setup, camera.h:28-48); image_plane_dist is the
+ * reference's mImagePlaneDist in pixels.  lens_radius > 0 enables the
+ * thin-lens path (camera.cpp:30-47). */
+typedef struct wr_camera_desc {
+    float position[3];
+    float focus[3];
+    float up[3];
+    uint32_t width;
+    uint32_t height;
+    float image_plane_dist;
+    float lens_radius;
+    float focal_dist;
+} wr_camera_desc;
+
+/* Density grid of a heterogeneous medium, z-major (index z*nx*ny + y*nx + x,
+ * HeterogeneousVolume.h:31-36), spanning the box [p0, p1]. */
+typedef struct wr_grid_desc {
+    uint32_t nx, ny, nz;
+    uint32_t pad;
+    const float* density;
+    float p0[3];
+    float p1[3];
+} wr_grid_desc;
+
+typedef struct wr_scene_desc {
+    uint32_t num_objects;
+    uint32_t num_vertices;
+    uint32_t num_triangles;
+    uint32_t num_grids;
+    const wr_object_desc* objects;
+    const float* vertices;     /* num_vertices x 3, world space, object by object */
+    const uint32_t* triangles; /* num_triangles x 3, vertex indices LOCAL to the object */
+    const wr_grid_desc* grids;
+    wr_camera_desc camera;
+} wr_scene_desc;
+
+/* Closest hit: tri is the global triangle index (scene order, object by
+ * object) or WR_NO_HIT; t the reference's hit distance; b1, b2 the
+ * barycentric coordinates of the hit point (mesh.h:67-73 formula). */
+typedef struct wr_hit {
+    uint32_t tri;
+    float t;
+    float b1;
+    float b2;
+} wr_hit;
+
+typedef struct wr_ctx wr_ctx;
+typedef uint32_t wr_scene_id;
+
+typedef struct wr_ctx_desc {
+    int device;                      /* CUDA device ordinal */
+    uint64_t device_memory_budget;   /* bytes the serving loop may use; 0 = 90% of free */
+    uint32_t flags;
+    uint32_t pad;
+} wr_ctx_desc;
+
+/* ---- context ------------------------------------------------------------ */
+int wr_get_abi_version(uint32_t* version);
+int wr_ctx_create(const wr_ctx_desc* desc, wr_ctx** out);
+int wr_ctx_destroy(wr_ctx* ctx);
+const char* wr_last_error(const wr_ctx* ctx);
+
+/* ---- scenes ------------------------------------------------------------- */
+/* Flattens the scene (Scene::buildKDTree, scene.cpp:20-44), builds the
+ * reference's median-split tree over all triangles (KDTree::build with
+ * splitBest, kdtree.cpp:141-258) and makes it resident on the device. */
+int wr_scene_upload(wr_ctx* ctx, const wr_scene_desc* desc, wr_scene_id* out);
+int wr_scene_release(wr_ctx* ctx, wr_scene_id scene);
+
+typedef struct wr_scene_info {
+    uint32_t num_triangles;
+    uint32_t num_nodes;        /* reference tree nodes (root + children) */
+    uint32_t num_leaves;
+    uint32_t max_depth;
+    uint64_t device_bytes;     /* resident bytes of this scene */
+    double build_seconds;      /* host tree build time */
+} wr_scene_info;
+int wr_scene_get_info(wr_ctx* ctx, wr_scene_id scene, wr_scene_info* out);
+
+/* ---- traversal ---------------------------------------------------------- */
+/* Per-ray self-intersection filter (NoSelfCondition, noself.cpp:13-20):
+ * inside_obj / contact_obj are object indices or WR_NO_OBJECT.  Pass NULL
+ * for the unfiltered query (KDTree::intersect with condition == NULL). */
+typedef struct wr_trace_filter {
+    const int32_t* inside_obj;
+    const int32_t* contact_obj;
+} wr_trace_filter;
+
+/* Closest hit of n rays (origin xyz, direction xyz; n x 6 floats).  Host
+ * buffers: the call copies rays to the device and hits back.
+ * Replaces KDTree::intersect (kdtree.cpp:349-353) and Scene::intersect
+ * (scene.cpp:102-113). */
+int wr_trace_closest(wr_ctx* ctx, wr_scene_id scene, const float* rays, uint64_t n,
+                     const wr_trace_filter* filter, wr_hit* hits);
+
+/* Same on device buffers already resident in HBM, enqueued on `stream`
+ * (a cudaStream_t; NULL = the legacy default stream). */
+int wr_trace_closest_device(wr_ctx* ctx, wr_scene_id scene, const float* d_rays, uint64_t n,
+                            const int32_t* d_inside_obj, const int32_t* d_contact_obj,
+                            wr_hit* d_hits, void* stream);
+
+/* ---- host-side tree (no GPU needed) ------------------------------------- */
+/* Builds the reference tree on the host only and returns its flattened
+ * form, so that host logic can be checked without a device.
+ * nodes: per node {first, count_or_child} as described in kdtree_host.h;
+ * boxes: per node min xyz, max xyz; leaf_tris: global triangle ids in
+ * leaf order. */
+typedef struct wr_kdtree_host wr_kdtree_host;
+int wr_kdtree_build_host(const float* vertices, uint32_t num_vertices, const uint32_t* triangles,
+                         uint32_t num_triangles, int num_threads, wr_kdtree_host** out);
+int wr_kdtree_host_sizes(const wr_kdtree_host* t, uint32_t* num_nodes, uint32_t* num_leaf_tris,
+                         uint32_t* max_depth);
+int wr_kdtree_host_export(const wr_kdtree_host* t, int32_t* left, int32_t* right, float* boxes,
+                          uint32_t* leaf_first, uint32_t* leaf_count, uint32_t* leaf_tris);
+int wr_kdtree_host_free(wr_kdtree_host* t);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WALKRAY_H */

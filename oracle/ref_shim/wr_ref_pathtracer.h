@@ -1,0 +1,12 @@
+/* Extra forced include for pathTracer.cpp only.  Line 23 of that file passes
+ * the temporary returned by Camera::generateRay to MCRenderer::samplePath,
+ * which takes Ray& — MSVC binds it, g++ does not.  The macro routes that one
+ * call through an identity function that yields an lvalue; the reference
+ * source file itself is compiled as it lies. */
+#pragma once
+#include "wr_ref_prelude.h"
+#include "mcRenderer.h"
+namespace wr_shim {
+template <class T> T& as_lvalue(T&& t) { return t; }
+}
+#define samplePath(path, ray) samplePath(path, ::wr_shim::as_lvalue(ray))
