@@ -185,6 +185,32 @@ int wr_trace_closest_device(wr_ctx* ctx, wr_scene_id scene, const float* d_rays,
                             const int32_t* d_inside_obj, const int32_t* d_contact_obj,
                             wr_hit* d_hits, void* stream);
 
+/* ---- rendering ---------------------------------------------------------- */
+#define WR_MODE_MEGAKERNEL 0u /* one thread per pixel runs whole paths */
+#define WR_MODE_WAVEFRONT 1u  /* generate / extend / shade queues, persistent kernels, graph bounce loop */
+
+#define WR_RENDER_NEE 1u      /* PathTracer's next-event-estimation branch (pathTracer.cpp:39-66) */
+
+typedef struct wr_render_desc {
+    uint32_t spp;          /* samples per pixel (PathTracer spp) */
+    uint32_t max_path_len; /* MCRenderer maxPathLen */
+    uint64_t seed;         /* key of the per-path counter-based random stream */
+    uint32_t mode;         /* WR_MODE_* */
+    uint32_t flags;        /* WR_RENDER_* */
+    uint32_t spp_offset;   /* index of the first sample (progressive rendering / resume) */
+    uint32_t pad;
+} wr_render_desc;
+
+/* PathTracer::renderPixels (pathTracer.cpp:7-76) on the GPU: rgb_out gets
+ * the W*H*3 mean image (p = y*W + x, row 0 at the top), host buffer. */
+int wr_render(wr_ctx* ctx, wr_scene_id scene, const wr_render_desc* desc, float* rgb_out);
+
+/* Adds the desc->spp samples starting at desc->spp_offset to a device film:
+ * d_sum[3p+c] += colour, d_sumsq (may be NULL) += colour^2.  Enqueued on
+ * `stream` (cudaStream_t; NULL = the context's stream), asynchronous. */
+int wr_render_device(wr_ctx* ctx, wr_scene_id scene, const wr_render_desc* desc, float* d_sum, float* d_sumsq,
+                     void* stream);
+
 /* ---- host-side tree (no GPU needed) ------------------------------------- */
 /* Builds the reference tree on the host only and returns its flattened
  * form, so that host logic can be checked without a device.

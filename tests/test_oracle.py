@@ -1,0 +1,84 @@
+"""The oracle (C restatement) against the reference's own answers: golden
+fixtures made by tests/golden/make_golden.py from WalkRay's code, and the
+published Philox4x32-10 known-answer vectors."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+import make_golden
+import wr_oracle
+from walkray_gb300 import scenes as S
+
+
+def test_philox_known_answers(built):
+    # Random123 known-answer vectors for Philox4x32-10: (counter, key) -> output
+    kat = [
+        ([0, 0, 0, 0], [0, 0], [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]),
+        ([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2, [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]),
+        ([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0],
+         [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]),
+    ]
+    for ctr, key, out in kat:
+        assert list(wr_oracle.philox(ctr, key)) == out
+
+
+def test_draw_stream_layout(built):
+    # draw d of (pixel, sample) is word d%4 of philox({d/4, sample, pixel, 0}, seed) >> 8 * 2^-24
+    seed = 0x123456789ABCDEF
+    for pixel, sample, dim in [(0, 0, 0), (5, 3, 7), (65535, 255, 41), (2**31, 17, 3)]:
+        w = wr_oracle.philox([dim >> 2, sample, pixel, 0], [seed & 0xFFFFFFFF, seed >> 32])[dim & 3]
+        assert wr_oracle.draw(seed, pixel, sample, dim) == np.float32((int(w) >> 8) / 16777216.0)
+
+
+@pytest.mark.parametrize("name", ["cornell", "ico4", "mixed_l2", "media_small"])
+def test_oracle_tree_equals_reference(built, name):
+    s = make_golden.golden_scenes()[name]
+    _, v, _, _ = s.flatten()
+    tree = wr_oracle.Tree(v, s.global_triangles())
+    want = json.load(open(os.path.join(GOLDEN, "trees.json")))[name]
+    assert hashlib.sha256(tree.dump()).hexdigest() == want
+
+
+def test_oracle_hits_equal_reference(built):
+    s = make_golden.golden_scenes()["ico4"]
+    _, v, _, _ = s.flatten()
+    g = np.load(os.path.join(GOLDEN, "trace_ico4.npz"))
+    rays = S.kd_rays(s, 32768, seed=2)
+    tri, t, nb, nt = wr_oracle.Tree(v, s.global_triangles()).trace(rays)
+    assert np.array_equal(tri, g["tri"])
+    hit = tri != 0xFFFFFFFF
+    assert np.array_equal(t[hit].view(np.uint32), g["t"][hit].view(np.uint32))
+    assert 0.05 < hit.mean() < 0.5
+
+
+def test_oracle_filtered_hits_equal_reference(built):
+    s = make_golden.golden_scenes()["mixed_l2"]
+    _, v, _, _ = s.flatten()
+    g = np.load(os.path.join(GOLDEN, "trace_filtered.npz"))
+    rays, ids = make_golden.filtered_rays(s, 32768, seed=5)
+    tree = wr_oracle.Tree(v, s.global_triangles(), s.tri_object_ids())
+    tri, t, _, _ = tree.trace(rays, ids[:, 0], ids[:, 1])
+    assert np.array_equal(tri, g["tri"])
+
+
+def test_oracle_render_matches_reference_statistically(built):
+    """Cornell 32x32: the restated PathTracer vs 8 reference renders of 256 spp.
+    Per-pixel z on 4x4 blocks; |z| > 4 on no block, mean within 1.5 %."""
+    g = np.load(os.path.join(GOLDEN, "render_cornell.npz"))
+    ref = g["images"].astype(np.float64)  # (8, 32, 32, 3)
+    s = make_golden.golden_scenes()["cornell"]
+    orc = wr_oracle.SceneOracle(s)
+    imgs = []
+    for seed in range(8):
+        sm, _, _ = orc.render(256, 8, seed=1000 + seed)
+        imgs.append((sm / 256).reshape(32, 32, 3))
+    port = np.stack(imgs)
+    blk = lambda a: a.reshape(a.shape[0], 8, 4, 8, 4, 3).mean((2, 4))
+    br, bp = blk(ref), blk(port)
+    z = (br.mean(0) - bp.mean(0)) / np.sqrt(br.var(0, ddof=1) / 8 + bp.var(0, ddof=1) / 8 + 1e-12)
+    assert np.abs(z).max() < 4.5, np.abs(z).max()
+    assert abs(port.mean() / ref.mean() - 1) < 0.015

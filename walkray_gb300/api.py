@@ -1,0 +1,165 @@
+"""Python front end of the C ABI: a thin object layer over libwalkray_gpu.so.
+
+    ctx = Context()                      # wr_ctx_create
+    sid = ctx.upload(scene)              # wr_scene_upload (tree build + residency)
+    hits = ctx.trace_closest(sid, rays)  # wr_trace_closest (host buffers)
+    img = ctx.render(sid, spp=64, max_path_len=8)   # wr_render
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from .scenes import Scene
+
+
+def scene_desc(scene: Scene):
+    """wr_scene_desc for a scenes.Scene plus the arrays that back it (keep both alive)."""
+    objs, verts, tris, grids = scene.flatten()
+    keep = [objs, verts, tris]
+    gd = (L.wr_grid_desc * max(1, len(grids)))()
+    for i, g in enumerate(grids):
+        dens = np.ascontiguousarray(g.density, np.float32)
+        keep.append(dens)
+        nz, ny, nx = dens.shape
+        gd[i].nx, gd[i].ny, gd[i].nz = nx, ny, nz
+        gd[i].density = dens.ctypes.data_as(C.POINTER(C.c_float))
+        gd[i].p0[:] = list(g.p0)
+        gd[i].p1[:] = list(g.p1)
+    keep.append(gd)
+    d = L.wr_scene_desc()
+    d.num_objects, d.num_vertices, d.num_triangles, d.num_grids = len(objs), len(verts), len(tris), len(grids)
+    d.objects = objs.ctypes.data
+    d.vertices = verts.ctypes.data
+    d.triangles = tris.ctypes.data
+    d.grids = C.addressof(gd)
+    c = scene.camera
+    if c is not None:
+        d.camera.position[:] = list(c.position)
+        d.camera.focus[:] = list(c.focus)
+        d.camera.up[:] = list(c.up)
+        d.camera.width, d.camera.height = c.width, c.height
+        d.camera.image_plane_dist = c.image_plane_dist
+        d.camera.lens_radius = c.lens_radius
+        d.camera.focal_dist = c.focal_dist
+    return d, keep
+
+
+class Context:
+    def __init__(self, device: int = 0, memory_budget: int = 0):
+        self.lib = L.load()
+        desc = L.wr_ctx_desc(device, memory_budget, 0, 0)
+        h = C.c_void_p()
+        rc = self.lib.wr_ctx_create(C.byref(desc), C.byref(h))
+        if rc != L.WR_OK:
+            raise L.WRError(rc, "wr_ctx_create failed (no usable CUDA device?)")
+        self.h = h
+
+    def _check(self, rc):
+        L.check(rc, self.h)
+
+    def close(self):
+        if self.h:
+            self.lib.wr_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- scenes -------------------------------------------------------
+    def upload(self, scene: Scene) -> int:
+        d, keep = scene_desc(scene)
+        sid = C.c_uint32()
+        self._check(self.lib.wr_scene_upload(self.h, C.byref(d), C.byref(sid)))
+        del keep
+        return sid.value
+
+    def release(self, sid: int) -> None:
+        self._check(self.lib.wr_scene_release(self.h, sid))
+
+    def info(self, sid: int) -> dict:
+        inf = L.wr_scene_info()
+        self._check(self.lib.wr_scene_get_info(self.h, sid, C.byref(inf)))
+        return {k: getattr(inf, k) for k, _ in L.wr_scene_info._fields_}
+
+    # ---- traversal ----------------------------------------------------
+    def trace_closest(self, sid: int, rays: np.ndarray, inside=None, contact=None, out=None) -> np.ndarray:
+        """Closest hits of host rays (n x 6 float32).  `out` may be a
+        preallocated (e.g. pinned) buffer of n x 16 bytes."""
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        n = len(rays)
+        if out is not None:
+            assert out.flags.c_contiguous and out.nbytes == 16 * n
+            hits = out
+        else:
+            hits = np.empty(n, L.HIT_DTYPE)
+        filt = None
+        if inside is not None:
+            ins = np.ascontiguousarray(inside, np.int32)
+            con = np.ascontiguousarray(contact, np.int32)
+            filt = L.wr_trace_filter(ins.ctypes.data, con.ctypes.data)
+        self._check(self.lib.wr_trace_closest(self.h, sid, L.ptr(rays), n, C.byref(filt) if filt else None,
+                                              L.ptr(hits)))
+        return hits
+
+    def trace_closest_device(self, sid: int, d_rays: int, n: int, d_hits: int, stream: int = 0,
+                             d_inside: int = 0, d_contact: int = 0) -> None:
+        self._check(self.lib.wr_trace_closest_device(self.h, sid, C.c_void_p(d_rays), n,
+                                                     C.c_void_p(d_inside or None), C.c_void_p(d_contact or None),
+                                                     C.c_void_p(d_hits), C.c_void_p(stream or None)))
+
+
+def build_tree_host(verts: np.ndarray, tris: np.ndarray, threads: int = 0) -> dict:
+    """The reference tree built by the library on the host only (no GPU)."""
+    lib = L.load()
+    verts = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
+    tris = np.ascontiguousarray(tris, np.uint32).reshape(-1, 3)
+    h = C.c_void_p()
+    rc = lib.wr_kdtree_build_host(L.ptr(verts), len(verts), L.ptr(tris), len(tris), threads, C.byref(h))
+    if rc != L.WR_OK:
+        raise L.WRError(rc, "wr_kdtree_build_host failed")
+    try:
+        nn, nlt, md = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        lib.wr_kdtree_host_sizes(h, C.byref(nn), C.byref(nlt), C.byref(md))
+        N = nn.value
+        out = {
+            "left": np.empty(N, np.int32), "right": np.empty(N, np.int32), "box": np.empty((N, 6), np.float32),
+            "leaf_first": np.empty(N, np.uint32), "leaf_count": np.empty(N, np.uint32),
+            "leaf_tris": np.empty(nlt.value, np.uint32), "max_depth": md.value,
+        }
+        lib.wr_kdtree_host_export(h, *(L.ptr(out[k]) for k in ("left", "right", "box", "leaf_first", "leaf_count",
+                                                               "leaf_tris")))
+        return out
+    finally:
+        lib.wr_kdtree_host_free(h)
+
+
+def tree_dump_bytes(t: dict) -> bytes:
+    """The tree in the pre-order dump format of the oracle programs."""
+    parts = []
+    stack = [0]
+    while stack:
+        n = stack.pop()
+        leaf = t["left"][n] < 0
+        cnt = int(t["leaf_count"][n]) if leaf else 0
+        parts.append(np.array([1 if leaf else 0], np.uint32).tobytes())
+        parts.append(t["box"][n].astype(np.float32).tobytes())
+        parts.append(np.array([cnt], np.uint32).tobytes())
+        if leaf:
+            f = int(t["leaf_first"][n])
+            parts.append(t["leaf_tris"][f:f + cnt].astype(np.uint32).tobytes())
+        else:
+            stack.append(int(t["right"][n]))
+            stack.append(int(t["left"][n]))
+    return b"".join(parts)

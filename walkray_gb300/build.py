@@ -1,0 +1,95 @@
+"""Build recipe for the in-tree CUDA library (libwalkray_gpu.so, sm_103a) and
+the oracle programs.
+
+    python -m walkray_gb300.build            # library + oracle
+    python -m walkray_gb300.build --lib      # library only
+
+Every translation unit is compiled by nvcc in parallel; kernels use
+``-fmad=false`` (no contraction) with IEEE division and square root, host code
+``-ffp-contract=off``, so that traversal arithmetic is bit-identical to the
+reference's FP32 code on both x86-64 and aarch64 hosts.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OBJ = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libwalkray_gpu.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _sources():
+    return sorted(f for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
+
+
+def _compile(src: str, nvcc: str) -> str:
+    out = os.path.join(OBJ, src.rsplit(".", 1)[0] + ".o")
+    path = os.path.join(CSRC, src)
+    deps = [path] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
+    deps.append(os.path.join(ROOT, "include", "walkray.h"))
+    if os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(d) for d in deps):
+        return out
+    host = "-Xcompiler=-fPIC,-fopenmp,-ffp-contract=off,-O3"
+    if src.endswith(".cu"):
+        cmd = [nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
+               host, "-c", path, "-o", out]
+    else:
+        cmd = [nvcc, "-std=c++17", "-O3", host, "-c", path, "-o", out]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+    return out
+
+
+def build_lib(verbose: bool = False) -> str:
+    nvcc = _nvcc()
+    os.makedirs(OBJ, exist_ok=True)
+    srcs = _sources()
+    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+        objs = list(ex.map(lambda s: _compile(s, nvcc), srcs))
+    if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
+        tmp = LIB + ".tmp"
+        cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-Xcompiler=-fopenmp", "-lgomp"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, LIB)
+    if verbose:
+        print("built", LIB)
+    return LIB
+
+
+def build_oracle(verbose: bool = False) -> None:
+    """The C restatement always; the reference harness when the reference
+    tree is present on this machine."""
+    odir = os.path.join(ROOT, "oracle")
+    r = subprocess.run(["make", "-s", "-C", odir, "port"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
+    ref = os.environ.get("WR_REFERENCE_DIR", "/root/reference")
+    if os.path.isfile(os.path.join(ref, "kdtree.cpp")):
+        r = subprocess.run(["make", "-s", "-j8", "-C", odir, "ref", f"REF={ref}"], capture_output=True, text=True)
+        if r.returncode != 0 and verbose:
+            print("reference harness not built:", r.stderr[-2000:])
+    if verbose:
+        print("built oracle")
+
+
+if __name__ == "__main__":
+    build_lib(verbose=True)
+    if "--lib" not in sys.argv:
+        build_oracle(verbose=True)

@@ -1,0 +1,23 @@
+// render_launch.h — host-side launchers of the rendering kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "wr_shade.cuh"
+
+namespace wr {
+
+struct RenderParams {
+    uint64_t seed;
+    uint32_t s0, s1;          // sample range [s0, s1)
+    uint32_t max_path_len;    // MCRenderer maxPathLen
+    uint32_t flags;
+    int stack_cap;            // traversal stack entries per thread (tree depth + 3)
+};
+
+// plain megakernel: film[3*p+c] += sum over samples of the pixel colour
+// (film2 != NULL: also the sum of squares)
+cudaError_t launch_megakernel(const RenderScene& S, const RenderParams& P, float* film, float* film2,
+                              unsigned int* err, cudaStream_t stream);
+
+}  // namespace wr

@@ -1,0 +1,86 @@
+// render_mega.cu — k_megakernel: the plain form of the renderer.  One thread
+// per pixel runs whole paths (PathTracer::renderPixels inner loop,
+// pathTracer.cpp:21-70: camera ray, samplePath bounce loop, throughput,
+// isLegalColor, fixVignetting) for a range of samples and adds the results
+// to an FP32 film (sum and optional sum of squares per channel).
+#include "render_launch.h"
+#include "wr_shade.cuh"
+
+namespace wr {
+
+template <bool STATS>
+__global__ void __launch_bounds__(128) k_megakernel(RenderScene S, RenderParams P, float* __restrict__ film,
+                                                      float* __restrict__ film2, unsigned int* __restrict__ err) {
+    extern __shared__ uint32_t s_stack[];
+    uint32_t* stack = s_stack + threadIdx.x;
+    const int stride = blockDim.x;
+    const uint32_t npix = S.width * S.height;
+    const uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pixel >= npix) return;
+    f3 acc = mk(0, 0, 0), acc2 = mk(0, 0, 0);
+    for (uint32_t s = P.s0; s < P.s1; s++) {
+        PathRng g;
+        g.init(P.seed, pixel, s);
+        PRay cur = camera_ray(S, pixel, g);
+        {
+            const RayQ q = make_rayq(cur.o, cur.d, S.tree.scene_mag);
+            set_hit(S, cur, trace_closest<false, false>(S.tree, q, -1, -1, stack, stride, P.stack_cap, err));
+        }
+        InsideStack st;
+        st.reset(cur.inside);
+        f3 color = mk(1, 1, 1), result = mk(0, 0, 0);
+        for (uint32_t depth = 0;; depth++) {
+            const int self = cur.inside >= 0 ? cur.inside : cur.iobj;
+            if (self < 0) break;  // escaped: terminateRay carries zero radiance
+            PRay next = scatter(S, self, cur, g, st);
+            if (length(next.d) < 0.5f) {
+                color = color * cos_term(S, cur);
+                color = vmul(color, radiance_decay(S, cur, length(next.o - cur.o)));
+                color = vmul(color, weight(cur));
+                result = vmul(color, weight(next));
+                break;
+            }
+            if (depth + 1 > P.max_path_len) break;
+            st.set_top(next.inside);
+            const RayQ q = make_rayq(next.o, next.d, S.tree.scene_mag);
+            const Hit h = trace_closest<true, false>(S.tree, q, next.inside, next.contact, stack, stride, P.stack_cap, err);
+            if (h.slot < 0) break;
+            set_hit(S, next, h);
+            color = color * cos_term(S, cur);
+            color = vmul(color, radiance_decay(S, cur, length(next.o - cur.o)));
+            color = vmul(color, weight(cur));
+            cur = next;
+        }
+        if (!legal(result)) result = mk(0, 0, 0);
+        const f3 c = fix_vignetting(S, result, pixel);
+        acc = acc + c;
+        if (STATS) acc2 = acc2 + vmul(c, c);
+    }
+    float* f = film + 3 * (size_t)pixel;
+    f[0] += acc.x;
+    f[1] += acc.y;
+    f[2] += acc.z;
+    if (STATS) {
+        float* f2 = film2 + 3 * (size_t)pixel;
+        f2[0] += acc2.x;
+        f2[1] += acc2.y;
+        f2[2] += acc2.z;
+    }
+}
+
+cudaError_t launch_megakernel(const RenderScene& S, const RenderParams& P, float* film, float* film2,
+                              unsigned int* err, cudaStream_t stream) {
+    const int block = 128;
+    const size_t smem = (size_t)P.stack_cap * block * sizeof(uint32_t);
+    const uint32_t npix = S.width * S.height;
+    const int grid = (int)((npix + block - 1) / block);
+    auto kern = film2 ? k_megakernel<true> : k_megakernel<false>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    kern<<<grid, block, smem, stream>>>(S, P, film, film2, err);
+    return cudaGetLastError();
+}
+
+}  // namespace wr

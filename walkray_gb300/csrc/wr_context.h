@@ -1,0 +1,91 @@
+// wr_context.h — the library's internal state behind the opaque wr_ctx.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/walkray.h"
+#include "kdtree_build.h"
+#include "wr_device.cuh"
+
+namespace wr {
+
+struct DeviceBuffer {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DeviceBuffer() = default;
+    DeviceBuffer(const DeviceBuffer&) = delete;
+    DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+    ~DeviceBuffer() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    // grows (never shrinks) to at least n bytes; contents are not kept
+    cudaError_t reserve(size_t n) {
+        if (n <= bytes) return cudaSuccess;
+        release();
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e == cudaSuccess) bytes = n;
+        else p = nullptr;
+        return e;
+    }
+    template <class T>
+    T* as() const {
+        return static_cast<T*>(p);
+    }
+};
+
+// one resident scene
+struct SceneGPU {
+    uint32_t id = 0;
+    DevTree tree{};
+    DeviceBuffer pairs, tris;
+    wr_scene_info info{};
+    // scene description kept on the host for rendering set-up
+    std::vector<wr_object_desc> objects;
+    std::vector<float> vertices;
+    std::vector<uint32_t> triangles;  // object-local
+    std::vector<int32_t> tri_obj;
+    std::vector<uint32_t> tri_local;
+    wr_camera_desc camera{};
+    std::vector<wr_grid_desc> grids;
+    std::vector<std::vector<float>> grid_data;
+    // rendering tables (materials, lights, grids) on the device, filled lazily
+    std::shared_ptr<void> render_data;
+};
+
+}  // namespace wr
+
+struct wr_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    uint64_t memory_budget = 0;
+    std::map<uint32_t, std::unique_ptr<wr::SceneGPU>> scenes;
+    uint32_t next_scene = 1;
+    wr::DeviceBuffer rays, hits, inside, contact;
+    wr::DeviceBuffer scratch_words;  // counters / error flags
+    bool trace_prune = false;
+    int last_trace_blocks = 0;
+    std::shared_ptr<void> serving;  // serving loop state (serve.cpp)
+};
+
+namespace wr {
+int set_error(wr_ctx* ctx, int code, const std::string& msg);
+int cuda_error(wr_ctx* ctx, cudaError_t e, const char* what);
+SceneGPU* find_scene(wr_ctx* ctx, wr_scene_id id);
+}  // namespace wr
+
+#define WR_CUDA(ctx, call)                                        \
+    do {                                                          \
+        cudaError_t e_ = (call);                                  \
+        if (e_ != cudaSuccess) return wr::cuda_error(ctx, e_, #call); \
+    } while (0)

@@ -1,0 +1,768 @@
+// wr_shade.cuh — per-path shading on sm_103a: camera rays, the material
+// scatter() functions, media, and the reference's throughput product.
+//
+// Semantics follow WalkRay's PathTracer (pathTracer.cpp:21-68) and
+// MCRenderer::samplePath (mcRenderer.cpp:16-57): the same path-vertex records,
+// the same draw order per material (so draw d of a path is the same Philox
+// number on the GPU and in the oracle), and the throughput factors applied in
+// the reference's order:  for every vertex i but the last
+//     color *= cos_i;  color *= decay_i(|o_{i+1} - o_i|);  color *= rad_i / oP_i / dP_i
+// and for the last one only the last factor.  Differences from the reference,
+// all statistical (no change of expectation):
+//  * shading arithmetic is FP32 with CUDA's math library where the reference
+//    mixes in double temporaries and glibc;
+//  * findInsideObject on a refraction/medium exit is replaced by a per-path
+//    stack of enclosing objects (equal for closed, properly nested meshes);
+//  * heterogeneous media use delta tracking on the same trilinear density
+//    instead of Simpson quadrature + Newton inversion (the reference's
+//    estimator has quadrature bias; delta tracking has none).
+#pragma once
+
+#include "../../include/walkray.h"
+#include "wr_traverse.cuh"
+
+namespace wr {
+
+constexpr int CAMERA_OBJ = -2;
+constexpr int INSIDE_STACK = 4;
+constexpr float PI_F = 3.14159265358979323846f;
+constexpr float INV_PI_F = 0.31830988618379067154f;
+constexpr float EPS_F = 1e-5f;
+
+struct GridDev {
+    uint32_t nx, ny, nz;
+    float p0[3], p1[3];
+    float majorant;  // max of the raw density (times density_scale and sigma_t in use)
+    const float* data;
+};
+
+struct RenderScene {
+    DevTree tree;
+    const wr_object_desc* objs;
+    uint32_t num_objs;
+    const uint32_t* tri_slot;  // global triangle id -> slot
+    // camera (Camera::setup / generateRay, camera.cpp:6-60)
+    f3 cam_pos, cam_focus, front, right, top;
+    uint32_t width, height;
+    float ipd, lens_radius, focal_dist;
+    int camera_inside;
+    // lights (SurfaceSampler, surfaceSampler.cpp:7-23)
+    uint32_t nlights;
+    const int* light_obj;
+    const float* light_thresh;
+    float light_area;
+    const float* obj_area;
+    const float* pick_prob;
+    const float* tri_thresh;  // cumulative triangle areas, indexed by global triangle id
+    const GridDev* grids;
+};
+
+// ---------------------------------------------------------------------------
+// scene access
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t obj_type(const RenderScene& S, int o) { return __ldg(&S.objs[o].type); }
+__device__ __forceinline__ bool is_volume(const RenderScene& S, int o) {
+    uint32_t t = obj_type(S, o);
+    return t == WR_MAT_HOMOGENEOUS || t == WR_MAT_HETEROGENEOUS;
+}
+__device__ __forceinline__ float obj_ior(const RenderScene& S, int o) {
+    uint32_t t = obj_type(S, o);
+    return (t == WR_MAT_REFRACTIVE || t == WR_MAT_HOMOGENEOUS || t == WR_MAT_HETEROGENEOUS) ? __ldg(&S.objs[o].ior)
+                                                                                            : 1.0f;
+}
+__device__ __forceinline__ f3 ld3(const float* p) { return mk(__ldg(p), __ldg(p + 1), __ldg(p + 2)); }
+
+// face normal of object o's local triangle t (Mesh::getWorldNormal, mesh.h:47-56)
+__device__ __forceinline__ f3 obj_normal(const RenderScene& S, int o, uint32_t t) {
+    uint32_t tb = __ldg(&S.objs[o].tri_begin), tc = __ldg(&S.objs[o].tri_count);
+    if (t >= tc) t = tc ? tc - 1 : 0;  // the reference indexes out of range here; clamp
+    const TriRec* r = S.tree.tris + __ldg(&S.tri_slot[tb + t]);
+    return face_normal(xyz(__ldg(&r->v0)), xyz(__ldg(&r->v1)), xyz(__ldg(&r->v2)));
+}
+
+// ---------------------------------------------------------------------------
+// path vertex (the reference Ray, ray.h:10-31)
+// ---------------------------------------------------------------------------
+struct PRay {
+    f3 o, d, rad;
+    float oP, dP;
+    int iobj;       // hit object or -1
+    float idist;
+    uint32_t itri;  // hit triangle, object-local
+    f3 inorm;       // face normal of the hit triangle
+    int inside;
+    int contact;    // object, CAMERA_OBJ or -1
+    f3 cnorm;       // contact normal (valid when contact != -1)
+};
+
+__device__ __forceinline__ PRay ray_default() {
+    PRay r;
+    r.o = mk(0, 0, 0);
+    r.d = mk(0, 0, 0);
+    r.rad = mk(1, 1, 1);
+    r.oP = r.dP = 1.f;
+    r.iobj = -1;
+    r.idist = 0.f;
+    r.itri = 0;
+    r.inorm = mk(0, 0, 0);
+    r.inside = -1;
+    r.contact = -1;
+    r.cnorm = mk(0, 0, 0);
+    return r;
+}
+
+// per-path stack of enclosing objects; top == current inside object
+struct InsideStack {
+    int v[INSIDE_STACK];
+    int n;
+    __device__ __forceinline__ void reset(int top) {
+        n = 0;
+        if (top >= 0) v[n++] = top;
+    }
+    __device__ __forceinline__ int top() const { return n > 0 ? v[n - 1] : -1; }
+    // object enclosing the exit point of `self` (what findInsideObject(outRay, self) finds for nested meshes)
+    __device__ __forceinline__ int below(int self) const {
+        for (int k = n - 1; k >= 0; k--)
+            if (v[k] == self) return k > 0 ? v[k - 1] : -1;
+        return n > 0 && v[n - 1] != self ? v[n - 1] : -1;
+    }
+    __device__ __forceinline__ void set_top(int obj) {
+        // a ray's inside object changed: entering pushes, leaving pops
+        if (obj == top()) return;
+        for (int k = n - 1; k >= 0; k--)
+            if (v[k] == obj) {
+                n = k + 1;
+                return;
+            }
+        if (obj < 0) {
+            n = 0;
+            return;
+        }
+        if (n < INSIDE_STACK) v[n++] = obj;
+        else v[n - 1] = obj;
+    }
+};
+
+// Ray::cosineTerm (ray.cpp:52-58)
+__device__ __forceinline__ float cos_term(const RenderScene& S, const PRay& r) {
+    float c = 1.f;
+    bool has_cos = r.contact == CAMERA_OBJ || (r.contact >= 0 && !is_volume(S, r.contact));
+    if (r.contact != -1 && has_cos && length(r.d) > 0.5f) c = fabsf(dot(r.cnorm, r.d));
+    return c > EPS_F ? c : EPS_F;
+}
+
+// ---------------------------------------------------------------------------
+// samplers
+// ---------------------------------------------------------------------------
+// Frame::setFromN (frame.h:30-49)
+__device__ __forceinline__ void frame_from_n(f3 w, f3& X, f3& Y, f3& Z) {
+    Y = w;
+    if (fabsf(w.x) > EPS_F) {
+        X = normalize(cross(mk(0, 1, 0), w));
+        Z = cross(X, Y);
+    } else {
+        Z = normalize(cross(mk(1, 0, 0), w));
+        X = cross(Y, Z);
+    }
+}
+__device__ __forceinline__ f3 to_world(f3 X, f3 Y, f3 Z, f3 l) { return (X * l.x + Y * l.y) + Z * l.z; }
+__device__ __forceinline__ f3 mirror_dir(f3 N, f3 d) { return normalize((N * (-dot(N, d))) * 2.f + d); }
+
+// RotateMatrix(axis, angle) * vec4(v, 0) (util.h:40-54)
+__device__ __forceinline__ f3 rotate_about(f3 a, float angle, f3 v) {
+    float s, c;
+    sincosf(angle, &s, &c);
+    const float _c = 1.f - c;
+    const float m00 = c + _c * a.x * a.x, m01 = _c * a.x * a.y - s * a.z, m02 = _c * a.x * a.z + s * a.y;
+    const float m10 = _c * a.x * a.y + s * a.z, m11 = c + _c * a.y * a.y, m12 = _c * a.y * a.z - s * a.x;
+    const float m20 = _c * a.x * a.z - s * a.y, m21 = _c * a.y * a.z + s * a.x, m22 = c + _c * a.z * a.z;
+    return mk((v.x * m00 + v.y * m01) + v.z * m02, (v.x * m10 + v.y * m11) + v.z * m12,
+              (v.x * m20 + v.y * m21) + v.z * m22);
+}
+
+// DiffuseBSDF::sampleBSDF (diffuseBsdf.h:21-30) + CosHemiSphereSampler
+__device__ __forceinline__ f3 diffuse_sample(f3 albedo, f3 N, PathRng& g, f3& out, float& pdf) {
+    f3 X, Y, Z;
+    frame_from_n(N, X, Y, Z);
+    const float a = g.next(), b = g.next();
+    const float t2 = sqrtf(1.f - b);
+    float s, c;
+    sincosf(2.f * PI_F * a, &s, &c);
+    out = to_world(X, Y, Z, mk(s * t2, sqrtf(b), c * t2));
+    const float dn = dot(N, out);
+    pdf = dn > 0.f ? dn * INV_PI_F : 0.f;
+    return albedo * INV_PI_F;
+}
+
+// IsotropicPhong::sampleBSDF (isotropicPhong.h:20-38) + PowerCosHemiSphereSampler
+__device__ __forceinline__ f3 phong_sample(f3 albedo, float power, f3 in, f3 N, PathRng& g, f3& out, float& pdf) {
+    f3 X, Y, Z;
+    frame_from_n(N, X, Y, Z);
+    const float a = g.next(), b = g.next();
+    const float t2 = powf(b, 1.f / (power + 1.f));
+    const float t3 = sqrtf(fmaxf(0.f, 1.f - t2 * t2));
+    float s, c;
+    sincosf(2.f * PI_F * a, &s, &c);
+    out = to_world(X, Y, Z, mk(s * t3, t2, c * t3));
+    const float dn = dot(N, out);
+    pdf = dn > 0.f ? (power + 1.f) * powf(dn, power) * (INV_PI_F * 0.5f) : 0.f;
+    const f3 R = mirror_dir(N, in);
+    const f3 rho = albedo * ((power + 2.f) * 0.5f * INV_PI_F);
+    const float dRW = dot(R, out);
+    if (dot(out, N) < 0.f) {
+        out = mk(0, 0, 0);
+        return mk(EPS_F, EPS_F, EPS_F);
+    }
+    return rho * powf(dRW > 0.f ? dRW : 0.f, power);
+}
+
+// AnisotropicPhong::evalBSDF (anisotropicPhong.h:62-101), including the
+// reference's unparenthesised MAX in the specular denominator
+__device__ __forceinline__ f3 aniso_eval(const wr_object_desc* m, f3 in, f3 out, f3 N) {
+    if (!(dot(in, N) <= 0.f && dot(out, N) >= 0.f)) return mk(0, 0, 0);
+    const f3 Rs = ld3(m->rs), Rd = ld3(m->rd);
+    const float nu = __ldg(&m->nu), nv = __ldg(&m->nv);
+    const f3 h = normalize(out - in);
+    f3 X, Y, Z;
+    frame_from_n(N, X, Y, Z);
+    const float ndh = dot(N, h), kdh = fabsf(dot(in, h));
+    const f3 F = Rs + (mk(1, 1, 1) - Rs) * powf(1.f - kdh, 5.f);
+    const float hu = dot(h, Z), hv = dot(h, X);
+    const float expo = fabsf(ndh) < EPS_F ? 1.f : (nu * hu * hu + nv * hv * hv) / (1.f - ndh * ndh);
+    const float a = fabsf(dot(N, in)), b = fabsf(dot(N, out));
+    const float den = (kdh * a > b) ? a : b;
+    const float k = sqrtf((nu + 1.f) * (nv + 1.f)) / (8.f * PI_F);
+    const f3 spec = divs((F * k) * powf(ndh, expo), den);
+    const float t1 = 1.f - (-dot(in, N) / 2.f), t2 = 1.f - dot(out, N) / 2.f;
+    const f3 diff = vmul(Rd * (28.f / (23.f * PI_F)), mk(1, 1, 1) - Rs) * (1.f - powf(t1, 5.f)) * (1.f - powf(t2, 5.f));
+    return spec + diff;
+}
+
+// half-vector sampler pdf (anisotropicPhongHalfVecSampler.h:39-56)
+__device__ __forceinline__ float aniso_half_pdf(float nu, float nv, f3 N, f3 h) {
+    f3 X, Y, Z;
+    frame_from_n(N, X, Y, Z);
+    const float ct = dot(h, Y), st = sqrtf(fmaxf(0.f, 1.f - ct * ct));
+    if (st < EPS_F) return 0.f;
+    const float cp = dot(h, Z) / st, sp = dot(h, X) / st;
+    return sqrtf((nu + 1.f) * (nv + 1.f)) / (2.f * PI_F) * powf(dot(N, h), nu * cp * cp + nv * sp * sp);
+}
+
+// AnisotropicPhong::sampleBSDF (anisotropicPhong.h:42-59), 3 draws
+__device__ __forceinline__ f3 aniso_sample(const wr_object_desc* m, f3 in, f3 N, PathRng& g, f3& out, float& pdf) {
+    const float nu = __ldg(&m->nu), nv = __ldg(&m->nv);
+    f3 X, Y, Z;
+    frame_from_n(N, X, Y, Z);
+    const float sx = g.next(), sy = g.next();
+    float phi = atanf(sqrtf((nu + 1.f) / (nv + 1.f)) * tanf(PI_F / 2.f * sx));
+    const float choose = g.next();
+    if (choose < 0.25f) {
+    } else if (choose < 0.5f) phi = PI_F - phi;
+    else if (choose < 0.75f) phi += PI_F;
+    else phi = 2.f * PI_F - phi;
+    float sp, cp;
+    sincosf(phi, &sp, &cp);
+    const float cosT = powf(1.f - sy, 1.f / (1.f + nu * cp * cp + nv * sp * sp));
+    const float sinT = sqrtf(fmaxf(0.f, 1.f - cosT * cosT));
+    const f3 h = to_world(X, Y, Z, mk(sinT * sp, cosT, sinT * cp));
+    out = in + (h * 2.f) * (-dot(in, h));
+    pdf = dot(N, out) > 0.f ? aniso_half_pdf(nu, nv, N, h) : 0.f;
+    pdf /= 4.f * fabsf(dot(in, h));
+    if (dot(out, N) < 0.f) {
+        out = mk(0, 0, 0);
+        return mk(0, 0, 0);
+    }
+    return aniso_eval(m, in, out, N);
+}
+
+// HGPhaseSampler (hgPhaseSampler.h:9-59): value/pdf and sampling, 2 draws
+__device__ __forceinline__ float hg_value(float g, f3 a, f3 b) {
+    const float ct = dot(a, b);
+    const float temp = 1.f + g * g - 2.f * g * ct;
+    return (1.f / (4.f * PI_F)) * (1.f - g * g) / (temp * sqrtf(temp));
+}
+__device__ __forceinline__ void ortho_basis(f3 w, f3& u, f3& v) {
+    f3 co;
+    if (fabsf(w.x) <= fabsf(w.y)) co = fabsf(w.x) <= fabsf(w.z) ? mk(0, -w.z, w.y) : mk(-w.y, w.x, 0);
+    else co = fabsf(w.y) <= fabsf(w.z) ? mk(-w.z, 0, w.x) : mk(-w.y, w.x, 0);
+    co = normalize(co);
+    u = cross(w, co);
+    v = cross(w, u);
+}
+__device__ __forceinline__ f3 hg_sample(float g, f3 in, PathRng& gen, f3& out, float& pdf) {
+    const f3 rd = normalize(in);
+    const float e1 = gen.next(), e2 = gen.next();
+    float ct;
+    if (fabsf(g) < EPS_F) ct = 1.f - 2.f * e1;
+    else {
+        const float sq = (1.f - g * g) / (1.f - g + 2.f * g * e1);
+        ct = (1.f + g * g - sq * sq) / (2.f * g);
+    }
+    const float st = sqrtf(fmaxf(0.f, 1.f - ct * ct));
+    float sp, cp;
+    sincosf(2.f * PI_F * e2, &sp, &cp);
+    f3 u, v;
+    ortho_basis(rd, u, v);
+    out = (u * (st * cp) + v * (st * sp)) + rd * ct;
+    pdf = hg_value(g, rd, out);
+    const float val = hg_value(g, in, out);
+    return mk(val, val, val);
+}
+
+// trilinear density (HeterogeneousVolume.cpp:71-116), identity transform;
+// the inside-mesh test is implied by the path's inside object
+__device__ __forceinline__ float grid_D(const GridDev& G, int x, int y, int z) {
+    x = min(max(x, 0), (int)G.nx - 1);
+    y = min(max(y, 0), (int)G.ny - 1);
+    z = min(max(z, 0), (int)G.nz - 1);
+    return __ldg(&G.data[((size_t)z * G.ny + y) * G.nx + x]);
+}
+__device__ __forceinline__ float lerpf(float t, float a, float b) { return (1.f - t) * a + t * b; }
+__device__ __forceinline__ float grid_density(const GridDev& G, f3 p, float scale) {
+    if (p.x > G.p1[0] || p.x < G.p0[0] || p.y > G.p1[1] || p.y < G.p0[1] || p.z > G.p1[2] || p.z < G.p0[2])
+        return 0.f;
+    const float fx = (float)G.nx * (p.x - G.p0[0]) / (G.p1[0] - G.p0[0]);
+    const float fy = (float)G.ny * (p.y - G.p0[1]) / (G.p1[1] - G.p0[1]);
+    const float fz = (float)G.nz * (p.z - G.p0[2]) / (G.p1[2] - G.p0[2]);
+    const int ix = (int)floorf(fx), iy = (int)floorf(fy), iz = (int)floorf(fz);
+    if (ix < 0 || ix >= (int)G.nx || iy < 0 || iy >= (int)G.ny || iz < 0 || iz >= (int)G.nz) return 0.f;
+    const float dx = fx - ix, dy = fy - iy, dz = fz - iz;
+    const float s00 = lerpf(dx, grid_D(G, ix, iy, iz), grid_D(G, ix + 1, iy, iz));
+    const float s10 = lerpf(dx, grid_D(G, ix, iy + 1, iz), grid_D(G, ix + 1, iy + 1, iz));
+    const float s01 = lerpf(dx, grid_D(G, ix, iy, iz + 1), grid_D(G, ix + 1, iy, iz + 1));
+    const float s11 = lerpf(dx, grid_D(G, ix, iy + 1, iz + 1), grid_D(G, ix + 1, iy + 1, iz + 1));
+    return lerpf(dz, lerpf(dy, s00, s10), lerpf(dy, s01, s11)) * scale;
+}
+
+__device__ __forceinline__ float luminance(f3 c) { return 0.212671f * c.x + 0.715160f * c.y + 0.072169f * c.z; }
+
+// ---------------------------------------------------------------------------
+// scatter (the material's Ray scatter(Ray&)); `st` tracks enclosing objects
+// ---------------------------------------------------------------------------
+struct Fresnel {
+    bool tir;
+    f3 refl, refr;
+    float er;
+};
+// shared dielectric boundary step (refractiveObj.h:37-82)
+__device__ __forceinline__ Fresnel fresnel_split(f3 N, f3 d, float cn, float nn) {
+    Fresnel f;
+    f.refl = mirror_dir(N, d);
+    f.refr = mk(0, 0, 0);
+    f.er = 0.f;
+    const float theta = acosf(fminf(1.f, fmaxf(-1.f, dot(d, N))));
+    const float sin_phi = cn / nn * sinf(theta);
+    f.tir = sin_phi > 1.f;
+    if (f.tir) return f;
+    float phi = asinf(sin_phi);
+    if (theta > PI_F / 2.f) phi = PI_F - phi;
+    const f3 axis = normalize(cross(N, d));
+    f.refr = normalize(rotate_about(axis, phi, N));
+    const float ct = fabsf(cosf(theta)), cp = fabsf(cosf(phi));
+    const float a1 = fabsf(cn * ct - nn * cp) / (cn * ct + nn * cp);
+    const float a2 = fabsf(nn * ct - cn * cp) / (nn * ct + cn * cp);
+    f.er = (a1 * a1 + a2 * a2) / 2.f;
+    return f;
+}
+
+__device__ __forceinline__ void set_contact(const RenderScene& S, PRay& out, int obj, uint32_t tri, f3 n) {
+    out.contact = obj;
+    out.cnorm = n;
+    (void)S;
+    (void)tri;
+}
+
+__device__ PRay scatter(const RenderScene& S, int self, const PRay& in, PathRng& g, InsideStack& st);
+
+// Diffuse / Glossy / AnisotropicGlossy (diffuseObj.h:34-57, glossyObj.h:39-62, anisotropicGlossyObj.h:54-68)
+__device__ __forceinline__ PRay scatter_surface(const RenderScene& S, int self, const PRay& in, PathRng& g) {
+    const wr_object_desc* m = &S.objs[self];
+    PRay out = ray_default();
+    out.o = in.o + in.d * in.idist;
+    const f3 N = in.inorm;
+    out.inside = in.inside;
+    // contactTriangleID = inRay.intersectTriangleID, normal looked up on `self`
+    out.contact = self;
+    out.cnorm = self == in.iobj ? N : obj_normal(S, self, in.itri);
+    const uint32_t type = __ldg(&m->type);
+    if (type == WR_MAT_ANISO) {
+        out.rad = aniso_sample(m, in.d, N, g, out.d, out.dP);
+        return out;
+    }
+    const f3 albedo = ld3(m->albedo);
+    float p = albedo.x;
+    if (albedo.y > p) p = albedo.y;
+    if (albedo.z > p) p = albedo.z;
+    if (g.next() < p) {
+        if (type == WR_MAT_DIFFUSE) out.rad = diffuse_sample(albedo, N, g, out.d, out.dP);
+        else out.rad = phong_sample(albedo, __ldg(&m->power), in.d, N, g, out.d, out.dP);
+        out.dP *= p;
+    } else {
+        out.d = mk(0, 0, 0);
+        out.rad = mk(0, 0, 0);
+        out.dP = 1.f - p;
+    }
+    return out;
+}
+
+// EmissiveObject::scatter (emissiveObj.h:15-28)
+__device__ __forceinline__ PRay scatter_emissive(const RenderScene& S, int self, const PRay& in) {
+    PRay out = ray_default();
+    out.o = in.o + in.d * in.idist;
+    out.d = mk(0, 0, 0);
+    out.inside = -1;
+    out.contact = self;
+    out.cnorm = self == in.iobj ? in.inorm : obj_normal(S, self, in.itri);
+    out.rad = dot(in.d, in.inorm) <= 0.f ? ld3(S.objs[self].emission) : mk(0, 0, 0);
+    return out;
+}
+
+// RefractiveObject::scatter (refractiveObj.h:27-88)
+__device__ __forceinline__ PRay scatter_refractive(const RenderScene& S, int self, const PRay& in, PathRng& g,
+                                                   InsideStack& st, bool* delegate) {
+    *delegate = in.iobj != self && in.inside == self;
+    PRay out = ray_default();
+    if (*delegate) return out;
+    const f3 N = in.inorm;
+    out.o = in.o + in.d * in.idist;
+    out.d = in.d;
+    const int curIn = in.inside;
+    const int curOut = in.inside == self ? st.below(self) : self;
+    const float cn = curIn >= 0 ? obj_ior(S, curIn) : 1.f, nn = curOut >= 0 ? obj_ior(S, curOut) : 1.f;
+    out.contact = self;
+    out.cnorm = self == in.iobj ? N : obj_normal(S, self, in.itri);
+    const Fresnel f = fresnel_split(N, in.d, cn, nn);
+    if (f.tir) {
+        out.d = f.refl;
+        out.inside = in.inside;
+    } else {
+        out.d = f.refr;
+        if (g.next() < f.er) {
+            out.d = f.refl;
+            out.rad = out.rad * (f.er / cos_term(S, out));
+            out.dP = f.er;
+            out.inside = in.inside;
+        } else {
+            out.rad = out.rad * ((1.f - f.er) / cos_term(S, out));
+            out.dP = 1.f - f.er;
+            out.inside = curOut;
+        }
+    }
+    out.d = normalize(out.d);
+    return out;
+}
+
+// entering a medium (homogeneousVolume.cpp:16-67 / HeterogeneousVolume.cpp:456-507)
+__device__ __forceinline__ PRay medium_enter(const RenderScene& S, int self, const PRay& in, PathRng& g) {
+    PRay out = ray_default();
+    const f3 N = in.inorm;
+    out.o = in.o + in.d * in.idist;
+    out.d = in.d;
+    const float cn = in.inside >= 0 ? obj_ior(S, in.inside) : 1.f, nn = obj_ior(S, self);
+    out.contact = self;
+    out.cnorm = N;
+    const Fresnel f = fresnel_split(N, in.d, cn, nn);
+    if (f.tir) {
+        out.d = f.refl;
+        out.inside = in.inside;
+        return out;
+    }
+    out.d = f.refr;
+    if (g.next() < f.er) {
+        out.d = f.refl;
+        out.rad = out.rad * (f.er / cos_term(S, out));
+        out.dP = f.er;
+        out.inside = in.inside;
+    } else {
+        out.rad = out.rad * ((1.f - f.er) / cos_term(S, out));
+        out.dP = 1.f - f.er;
+        out.inside = self;
+    }
+    out.d = normalize(out.d);
+    return out;
+}
+
+// leaving a medium at its own boundary (Fresnel) or handing over to the surface hit inside it
+// (homogeneousVolume.cpp:101-180 / HeterogeneousVolume.cpp:561-637); `delegate` asks the caller
+// to run the hit object's scatter on the returned record and multiply its oP by P_surface
+__device__ __forceinline__ PRay medium_exit(const RenderScene& S, int self, const PRay& in, float P_surface,
+                                            PathRng& g, InsideStack& st, bool* delegate) {
+    PRay out = in;
+    out.o = in.o + in.d * in.idist;
+    out.contact = in.iobj;
+    out.cnorm = in.inorm;
+    out.inside = self;
+    out.dP = 1.f;
+    out.rad = mk(1, 1, 1);
+    *delegate = in.iobj != self;
+    if (*delegate) {
+        out.contact = -1;
+        out.idist = 0.f;
+        return out;
+    }
+    const f3 N = in.inorm;
+    const int curOut = st.below(self);
+    const float cn = obj_ior(S, self), nn = curOut >= 0 ? obj_ior(S, curOut) : 1.f;
+    out.iobj = -1;
+    const Fresnel f = fresnel_split(N, in.d, cn, nn);
+    if (f.tir) {
+        out.d = f.refl;
+        out.inside = in.inside;
+        out.contact = self;
+        out.oP = P_surface;
+        return out;
+    }
+    out.d = f.refr;
+    if (g.next() < f.er) {
+        out.d = f.refl;
+        out.rad = out.rad * (f.er / cos_term(S, out));
+        out.dP = f.er;
+        out.oP = P_surface;
+        out.inside = in.inside;
+    } else {
+        out.rad = out.rad * ((1.f - f.er) / cos_term(S, out));
+        out.dP = 1.f - f.er;
+        out.oP = P_surface;
+        out.inside = curOut;
+    }
+    out.d = normalize(out.d);
+    return out;
+}
+
+// HomogeneousVolume::scatter (homogeneousVolume.cpp:7-199): analytic free flight on Luminance(sigma_t)
+__device__ __forceinline__ PRay scatter_homogeneous(const RenderScene& S, int self, const PRay& in, PathRng& g,
+                                                    InsideStack& st, bool* delegate, float* psurf) {
+    const wr_object_desc* m = &S.objs[self];
+    const f3 ss = ld3(m->sigma_s), st_ = ss + ld3(m->sigma_a);
+    const float lt = luminance(st_);
+    const float sampDist = -logf(1.f - g.next()) / lt;
+    *delegate = false;
+    const bool go_in = in.iobj == self && in.inside != self;
+    const bool be_in = in.inside == self;
+    if (go_in) return medium_enter(S, self, in, g);
+    if (be_in && sampDist < in.idist) {
+        PRay out = ray_default();
+        out.o = in.o + in.d * sampDist;
+        out.rad = hg_sample(__ldg(&m->g), in.d, g, out.d, out.dP);
+        out.inside = self;
+        const float albedo = luminance(ss) / lt;
+        const f3 pm = mk(st_.x * expf(-st_.x * sampDist), st_.y * expf(-st_.y * sampDist), st_.z * expf(-st_.z * sampDist));
+        if (g.next() < albedo) {
+            out.contact = -1;
+            out.dP *= albedo;
+            out.oP = luminance(pm);
+            out.rad = vmul(out.rad, ss);
+        } else {
+            out.d = mk(0, 0, 0);
+            out.rad = mk(0, 0, 0);
+            out.dP = 1.f;
+            out.oP = luminance(pm);
+            out.inside = -1;
+            out.contact = -1;
+        }
+        return out;
+    }
+    if (be_in) {
+        const float d = in.idist;
+        *psurf = luminance(mk(expf(-st_.x * d), expf(-st_.y * d), expf(-st_.z * d)));
+        return medium_exit(S, self, in, *psurf, g, st, delegate);
+    }
+    return ray_default();
+}
+
+// HeterogeneousVolume::scatter (HeterogeneousVolume.cpp:449-641) with delta
+// tracking (Woodcock) against the grid's majorant in place of Simpson +
+// Newton inversion.  For a grey sigma_t the reference's throughput weights
+// reduce to 1 per free flight; this keeps the same product with
+// oP = sigma_t * density at a collision and 1 on passing.
+__device__ __forceinline__ PRay scatter_heterogeneous(const RenderScene& S, int self, const PRay& in, PathRng& g,
+                                                      InsideStack& st, bool* delegate, float* psurf) {
+    const wr_object_desc* m = &S.objs[self];
+    *delegate = false;
+    const bool go_in = in.iobj == self && in.inside != self;
+    const bool be_in = in.inside == self;
+    if (go_in) return medium_enter(S, self, in, g);
+    const f3 ss = ld3(m->sigma_s), st_ = ss + ld3(m->sigma_a);
+    const float sgt = st_.x;  // grey extinction (checked at upload)
+    const GridDev G = S.grids[__ldg(&m->grid_index)];
+    const float scale = __ldg(&m->density_scale);
+    const float mu = G.majorant * scale * sgt;
+    float t = 0.f;
+    bool collided = false;
+    float dens = 0.f;
+    if (mu > 0.f) {
+        for (int it = 0; it < 1 << 16; it++) {  // bounded: the expected count is mu * distance
+            t += -logf(1.f - g.next()) / mu;
+            if (t >= in.idist) break;
+            dens = grid_density(G, in.o + in.d * t, scale);
+            if (g.next() * mu < sgt * dens) {
+                collided = true;
+                break;
+            }
+        }
+    }
+    if (be_in && collided) {
+        PRay out = ray_default();
+        out.o = in.o + in.d * t;
+        out.rad = hg_sample(__ldg(&m->g), in.d, g, out.d, out.dP);
+        out.inside = self;
+        const float albedo = luminance(ss) / luminance(st_);
+        if (g.next() < albedo) {
+            out.contact = -1;
+            out.dP *= albedo;
+            out.oP = sgt * dens;
+            out.rad = vmul(out.rad, ss * dens);
+        } else {
+            out.d = mk(0, 0, 0);
+            out.rad = mk(0, 0, 0);
+            out.dP = 1.f;
+            out.oP = sgt * dens;
+            out.inside = -1;
+            out.contact = -1;
+        }
+        return out;
+    }
+    if (be_in) {
+        *psurf = 1.f;
+        return medium_exit(S, self, in, 1.f, g, st, delegate);
+    }
+    return ray_default();
+}
+
+// one scatter() call, following delegations (RefractiveObject handing a hit
+// inside it to the hit object; media handing over to the surface hit)
+__device__ __noinline__ PRay scatter(const RenderScene& S, int self, const PRay& in, PathRng& g, InsideStack& st) {
+    PRay cur = in;
+    float oP_scale = 1.f;
+    for (int hop = 0; hop < 4; hop++) {
+        const uint32_t type = obj_type(S, self);
+        bool del = false;
+        float ps = 1.f;
+        PRay out;
+        switch (type) {
+            case WR_MAT_DIFFUSE:
+            case WR_MAT_GLOSSY:
+            case WR_MAT_ANISO: out = scatter_surface(S, self, cur, g); break;
+            case WR_MAT_EMISSIVE: out = scatter_emissive(S, self, cur); break;
+            case WR_MAT_REFRACTIVE:
+                out = scatter_refractive(S, self, cur, g, st, &del);
+                if (del) {  // `return inRay.intersectObj->scatter(inRay)`
+                    self = cur.iobj;
+                    continue;
+                }
+                break;
+            case WR_MAT_HOMOGENEOUS: out = scatter_homogeneous(S, self, cur, g, st, &del, &ps); break;
+            default: out = scatter_heterogeneous(S, self, cur, g, st, &del, &ps); break;
+        }
+        if (del) {  // medium hands over to the surface it hit: scatter there, oP *= P_surface
+            oP_scale *= ps;
+            self = cur.iobj;
+            cur = out;
+            continue;
+        }
+        out.oP *= oP_scale;
+        return out;
+    }
+    PRay dead = ray_default();
+    dead.rad = mk(0, 0, 0);
+    return dead;
+}
+
+// Ray::radianceDecay (ray.cpp:46-50): refractive decay^dist, homogeneous
+// exp(-sigma_t dist); heterogeneous media are already weighted by tracking
+__device__ __forceinline__ f3 radiance_decay(const RenderScene& S, const PRay& r, float dist) {
+    if (r.inside < 0) return mk(1, 1, 1);
+    const wr_object_desc* m = &S.objs[r.inside];
+    const uint32_t t = __ldg(&m->type);
+    if (t == WR_MAT_REFRACTIVE) {
+        const f3 dc = ld3(m->decay);
+        return mk(powf(dc.x, dist), powf(dc.y, dist), powf(dc.z, dist));
+    }
+    if (t == WR_MAT_HOMOGENEOUS) {
+        const f3 s = ld3(m->sigma_s) + ld3(m->sigma_a);
+        return mk(expf(-s.x * dist), expf(-s.y * dist), expf(-s.z * dist));
+    }
+    return mk(1, 1, 1);
+}
+
+// color *= rad / oP / dP with vec3/scalar's zero rule
+__device__ __forceinline__ f3 weight(const PRay& r) { return divs(divs(r.rad, r.oP), r.dP); }
+
+// Camera::generateRay (camera.cpp:6-60), draws 0 and 1 (+2, 3 for the lens)
+__device__ __forceinline__ PRay camera_ray(const RenderScene& S, uint32_t pixel, PathRng& g) {
+    PRay r = ray_default();
+    const uint32_t x = pixel % S.width, y = pixel / S.width;
+    const float u = g.next(), v = g.next();
+    r.d = normalize((S.front * S.ipd + S.right * (((float)x + u) - ((float)S.width / 2.f))) +
+                    S.top * ((((float)S.height / 2.f) - (float)y) - v));
+    r.o = S.cam_pos;
+    if (S.lens_radius > 0.f) {  // thin lens (camera.cpp:30-47, concentricSampleDisk :207-249)
+        const float a = g.next(), b = g.next();
+        const float sx = 2.f * a - 1.f, sy = 2.f * b - 1.f;
+        float lu = 0.f, lv = 0.f;
+        if (!(sx == 0.f && sy == 0.f)) {
+            float rr, th;
+            if (sx >= -sy) {
+                if (sx > sy) {
+                    rr = sx;
+                    th = sy > 0.f ? sy / rr : 8.f + sy / rr;
+                } else {
+                    rr = sy;
+                    th = 2.f - sx / rr;
+                }
+            } else {
+                if (sx <= sy) {
+                    rr = -sx;
+                    th = 4.f - sy / rr;
+                } else {
+                    rr = -sy;
+                    th = 6.f + sx / rr;
+                }
+            }
+            th *= PI_F / 4.f;
+            lu = rr * cosf(th);
+            lv = rr * sinf(th);
+        }
+        lu *= S.lens_radius;
+        lv *= S.lens_radius;
+        const float ft = S.focal_dist / fabsf(dot(S.front, r.d));
+        const f3 pf = r.o + r.d * ft;
+        r.o = (S.cam_pos + S.right * lu) + S.top * lv;
+        r.d = normalize(pf - r.o);
+    }
+    r.contact = CAMERA_OBJ;
+    r.cnorm = normalize(S.cam_focus - r.o);
+    r.inside = S.camera_inside;
+    return r;
+}
+
+// Camera::fixVignetting (camera.cpp:90-123) + isLegalColor (util.h:8-18)
+__device__ __forceinline__ bool legal(f3 c) {
+    return isfinite(c.x) && isfinite(c.y) && isfinite(c.z) && c.x >= 0.f && c.y >= 0.f && c.z >= 0.f;
+}
+__device__ __forceinline__ f3 fix_vignetting(const RenderScene& S, f3 color, uint32_t pixel) {
+    const uint32_t x = pixel % S.width, y = pixel / S.width;
+    const f3 dir = normalize((S.front * S.ipd + S.right * ((float)x + 0.5f - S.width / 2.f)) +
+                             S.top * (S.height / 2.f - 0.5f - (float)y));
+    const float c = dot(dir, S.front);
+    if (c == 0.f) return mk(0, 0, 0);
+    const f3 r = divs(color, fabsf(c));
+    return legal(r) ? r : mk(0, 0, 0);
+}
+
+// fill the hit fields of `r` from a closest-hit result
+__device__ __forceinline__ void set_hit(const RenderScene& S, PRay& r, const Hit& h) {
+    if (h.slot < 0) {
+        r.iobj = -1;
+        r.idist = -1.f;
+        return;
+    }
+    const TriRec* tr = S.tree.tris + h.slot;
+    const float4 a = __ldg(&tr->v0), b = __ldg(&tr->v1), c = __ldg(&tr->v2);
+    r.iobj = (int)__float_as_uint(b.w);
+    r.itri = __float_as_uint(c.w);
+    r.idist = h.t;
+    r.inorm = face_normal(xyz(a), xyz(b), xyz(c));
+}
+
+}  // namespace wr

@@ -1,0 +1,255 @@
+// wr_traverse.cuh — closest-hit traversal of the reference tree on sm_103a.
+//
+// Result contract: identical triangle id (and t) to KDTree::intersect
+// (kdtree.cpp:308-353) with NoSelfCondition (noself.cpp:13-20) when filtered.
+//
+// How the reference's semantics are kept while the GPU is free to reorder:
+//  * The reference descends every child whose box passes its predicate
+//    (BoundingBox::intersect, kdtree.cpp:46-64), so its candidate set is "all
+//    triangles under passing boxes".  The same predicate decides here, so the
+//    candidate set is the same whatever the visiting order.
+//  * Its winner is the smallest t, ties to the right child / first in a leaf;
+//    with the slot layout of wr_device.cuh that is "smallest t, then largest
+//    slot", an order-free rule.
+//  * The predicate itself is evaluated cheaply: a slab test on the box grown
+//    by a margin M that covers the predicate's rounding proves most misses
+//    (a box missed by the grown box fails all six reference face tests); for
+//    the rest the reference face test is run on the most likely face first
+//    (entry face, or exit face when the origin is inside) and on all six only
+//    if that one fails.  Every "pass" is decided by the reference's own
+//    arithmetic, every "fail" either by it or by the proof above.
+//  * Optional pruning (PRUNE): a child whose grown-box entry distance exceeds
+//    the best hit by a relative margin is skipped.  Not covered by the proof
+//    for grazing triangles; off in the parity path.
+#pragma once
+
+#include "wr_device.cuh"
+
+namespace wr {
+
+struct RayQ {
+    f3 o, d, inv;
+    float M;  // grown-box margin for this ray
+};
+
+__device__ __forceinline__ RayQ make_rayq(f3 o, f3 d, float scene_mag) {
+    RayQ q;
+    q.o = o;
+    q.d = d;
+    q.inv = mk(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+    float om = fmaxf(fabsf(o.x), fmaxf(fabsf(o.y), fabsf(o.z)));
+    // reference predicate rounding <= ~4.1 eps (B + |o|), slab test rounding
+    // <= ~3 eps (B + |o|) (eps = 2^-24); 2e-6 is ~33 eps
+    q.M = 2e-6f * (scene_mag + om) + 1e-30f;
+    return q;
+}
+
+struct Box {
+    float lx, ly, lz, hx, hy, hz;
+};
+template <int K>
+__device__ __forceinline__ float lo_(const Box& b) { return K == 0 ? b.lx : (K == 1 ? b.ly : b.lz); }
+template <int K>
+__device__ __forceinline__ float hi_(const Box& b) { return K == 0 ? b.hx : (K == 1 ? b.hy : b.hz); }
+template <int K>
+__device__ __forceinline__ float c_(f3 v) { return K == 0 ? v.x : (K == 1 ? v.y : v.z); }
+
+// One reference face test (kdtree.cpp:50-63), face I in 0..5 of the box.
+template <int I>
+__device__ __forceinline__ bool face_pass(const Box& bx, const RayQ& q) {
+    constexpr int A = I % 3, B = (I + 1) % 3, C = (I + 2) % 3;
+    const float dA = c_<A>(q.d);
+    if (dA == 0.f) return false;
+    const float plane = I < 3 ? lo_<A>(bx) : hi_<A>(bx);
+    const float dist = (plane - c_<A>(q.o)) / dA;
+    const float pb = c_<B>(q.o) + dist * c_<B>(q.d);
+    const float pc = c_<C>(q.o) + dist * c_<C>(q.d);
+    return dist >= 0.f && lo_<B>(bx) <= pb && hi_<B>(bx) >= pb && lo_<C>(bx) <= pc && hi_<C>(bx) >= pc;
+}
+
+__device__ __forceinline__ bool face_pass_dyn(int i, const Box& bx, const RayQ& q) {
+    switch (i) {
+        case 0: return face_pass<0>(bx, q);
+        case 1: return face_pass<1>(bx, q);
+        case 2: return face_pass<2>(bx, q);
+        case 3: return face_pass<3>(bx, q);
+        case 4: return face_pass<4>(bx, q);
+        default: return face_pass<5>(bx, q);
+    }
+}
+
+__device__ __forceinline__ bool all_faces(const Box& bx, const RayQ& q) {
+    return face_pass<0>(bx, q) || face_pass<1>(bx, q) || face_pass<2>(bx, q) || face_pass<3>(bx, q) ||
+           face_pass<4>(bx, q) || face_pass<5>(bx, q);
+}
+
+// The reference box predicate; *tnear gets the grown-box entry distance.
+__device__ __forceinline__ bool box_pred(const Box& bx, const RayQ& q, float* tnear) {
+    const float M = q.M;
+    float ax = (bx.lx - M - q.o.x) * q.inv.x, bxx = (bx.hx + M - q.o.x) * q.inv.x;
+    float ay = (bx.ly - M - q.o.y) * q.inv.y, by = (bx.hy + M - q.o.y) * q.inv.y;
+    float az = (bx.lz - M - q.o.z) * q.inv.z, bz = (bx.hz + M - q.o.z) * q.inv.z;
+    // fminf/fmaxf drop NaN (0 * inf on a zero direction component): no constraint
+    float nx = fminf(ax, bxx), fx = fmaxf(ax, bxx);
+    float ny = fminf(ay, by), fy = fmaxf(ay, by);
+    float nz = fminf(az, bz), fz = fmaxf(az, bz);
+    float tn = fmaxf(nx, fmaxf(ny, nz));
+    float tf = fminf(fx, fminf(fy, fz));
+    *tnear = tn;
+    if (!(tn <= tf) || tf < 0.f) {
+        // grown box missed: every reference face test fails.  A NaN interval
+        // (not expected) is decided by the reference test itself.
+        if (tn == tn && tf == tf) return false;
+        return all_faces(bx, q);
+    }
+    int face;
+    if (tn >= 0.f) {  // entry face: axis of the largest near distance
+        int ax_i = (nx >= ny && nx >= nz) ? 0 : (ny >= nz ? 1 : 2);
+        float da = ax_i == 0 ? q.d.x : (ax_i == 1 ? q.d.y : q.d.z);
+        face = ax_i + (da > 0.f ? 0 : 3);
+    } else {  // origin inside: exit face
+        int ax_i = (fx <= fy && fx <= fz) ? 0 : (fy <= fz ? 1 : 2);
+        float da = ax_i == 0 ? q.d.x : (ax_i == 1 ? q.d.y : q.d.z);
+        face = ax_i + (da > 0.f ? 3 : 0);
+    }
+    if (face_pass_dyn(face, bx, q)) return true;
+    return all_faces(bx, q);
+}
+
+// KDTree::intersect(ray, tri) geometric part (kdtree.cpp:279-301); returns
+// the distance or -1.  The edge-mask rejection is taken before the plane
+// distance (same result, less work).
+__device__ __forceinline__ float tri_test(f3 v0, f3 v1, f3 v2, const RayQ& q) {
+    const f3 l0 = v1 - v0, l1 = v2 - v1, l2 = v0 - v2;
+    const f3 r0 = v0 - q.o, r1 = v1 - q.o, r2 = v2 - q.o;
+    const float s0 = dot(q.d, cross(l0, r0));
+    const float s1 = dot(q.d, cross(l1, r1));
+    const float s2 = dot(q.d, cross(l2, r2));
+    const bool pos = s0 >= 0.f && s1 >= 0.f && s2 >= 0.f;
+    const bool neg = s0 <= 0.f && s1 <= 0.f && s2 <= 0.f;
+    if (!pos && !neg) return -1.f;
+    const f3 n = normalize(cross(l0, l1));
+    const float od = dot(n, r2);
+    const float dd = dot(n, q.d);
+    if (dd == 0.f) return -1.f;
+    const float t = od / dd;
+    if (t < 0.f) return -1.f;
+    return t;
+}
+
+// Mesh::getWorldNormal without vertex normals (mesh.h:47-56)
+__device__ __forceinline__ f3 face_normal(f3 v0, f3 v1, f3 v2) { return normalize(cross(v1 - v0, v2 - v0)); }
+
+// NoSelfCondition::legal (noself.cpp:13-20); object ids, -1 = none
+__device__ __forceinline__ bool noself_legal(int inside, int contact, int hit_obj, f3 dir, f3 fn) {
+    const float d = dot(dir, fn);
+    const bool in = d <= 0.f, out = d >= 0.f;
+    if (inside == contact) return !(in && contact == hit_obj);
+    return !(out && inside != hit_obj);
+}
+
+__device__ __forceinline__ Box root_box(const DevTree& T) {
+    return Box{T.root_lo[0], T.root_lo[1], T.root_lo[2], T.root_hi[0], T.root_hi[1], T.root_hi[2]};
+}
+
+struct Hit {
+    float t;    // +inf when no hit
+    int slot;   // -1 when no hit
+};
+
+__device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
+__device__ __forceinline__ uint4 ldg4u(const uint4* p) { return __ldg(p); }
+
+template <bool FILTERED>
+__device__ __forceinline__ void leaf_test(const DevTree& T, uint32_t first, uint32_t count, const RayQ& q, int inside,
+                                          int contact, Hit& h) {
+    for (uint32_t k = 0; k < count; k++) {
+        const int slot = (int)(first + k);
+        const TriRec* tr = T.tris + slot;
+        const float4 a = ldg4(&tr->v0), b = ldg4(&tr->v1), c = ldg4(&tr->v2);
+        const f3 v0 = xyz(a), v1 = xyz(b), v2 = xyz(c);
+        const float t = tri_test(v0, v1, v2, q);
+        if (t >= 0.f && (t < h.t || (t == h.t && slot > h.slot))) {
+            if (FILTERED) {
+                if (!noself_legal(inside, contact, (int)__float_as_uint(b.w), q.d, face_normal(v0, v1, v2))) continue;
+            }
+            h.t = t;
+            h.slot = slot;
+        }
+    }
+}
+
+// Closest hit.  `stack` is this thread's stack: entries at stack[k * stride],
+// at most `cap` of them (cap >= tree depth + 2 always suffices; a traversal
+// that would exceed it stops and sets bit 0 of *err instead of writing past).
+template <bool FILTERED, bool PRUNE>
+__device__ __forceinline__ Hit trace_closest(const DevTree& T, const RayQ& q, int inside, int contact, uint32_t* stack,
+                                             int stride, int cap, unsigned int* err) {
+    Hit h;
+    h.t = __int_as_float(0x7f800000);
+    h.slot = -1;
+    float tn;
+    if (!box_pred(root_box(T), q, &tn)) return h;
+    if (T.root_w1 & LEAF_FLAG) {
+        leaf_test<FILTERED>(T, T.root_w0, T.root_w1 & ~LEAF_FLAG, q, inside, contact, h);
+        return h;
+    }
+    int sp = 0;
+    stack[0] = T.root_w0;
+    sp = 1;
+    while (sp > 0) {
+        const uint32_t pi = stack[(--sp) * stride];
+        const NodePair* P = T.pairs + pi;
+        const float4 A = ldg4(&P->a), B = ldg4(&P->b), C = ldg4(&P->c);
+        const uint4 W = ldg4u(&P->t);
+        float tl, tr;
+        bool hl = box_pred(Box{A.x, A.y, A.z, A.w, B.x, B.y}, q, &tl);
+        bool hr = box_pred(Box{B.z, B.w, C.x, C.y, C.z, C.w}, q, &tr);
+        if (PRUNE) {
+            const float lim = h.t * 1.001f + q.M;
+            hl = hl && !(tl > lim);
+            hr = hr && !(tr > lim);
+        }
+        // leaves first (they can tighten the bound), then push internal
+        // children far-first so the near one is popped next
+        if (hl && (W.y & LEAF_FLAG)) {
+            leaf_test<FILTERED>(T, W.x, W.y & ~LEAF_FLAG, q, inside, contact, h);
+            hl = false;
+        }
+        if (hr && (W.w & LEAF_FLAG)) {
+            leaf_test<FILTERED>(T, W.z, W.w & ~LEAF_FLAG, q, inside, contact, h);
+            hr = false;
+        }
+        if (sp + 2 > cap) {
+            atomicOr(err, 1u);
+            break;
+        }
+        if (hl && hr) {
+            const bool lnear = tl <= tr;
+            stack[(sp++) * stride] = lnear ? W.z : W.x;
+            stack[(sp++) * stride] = lnear ? W.x : W.z;
+        } else if (hl) {
+            stack[(sp++) * stride] = W.x;
+        } else if (hr) {
+            stack[(sp++) * stride] = W.z;
+        }
+    }
+    return h;
+}
+
+// barycentric weights of v1, v2 at the hit point (mesh.h:67-73)
+__device__ __forceinline__ void hit_barycentrics(const DevTree& T, int slot, const RayQ& q, float t, float* u1,
+                                                 float* u2, uint32_t* gid) {
+    const TriRec* tr = T.tris + slot;
+    const float4 a = ldg4(&tr->v0), b = ldg4(&tr->v1), c = ldg4(&tr->v2);
+    const f3 v0 = xyz(a), b1 = xyz(b) - v0, b2 = xyz(c) - v0;
+    const f3 v = (q.o + q.d * t) - v0;
+    const float d12 = dot(b1, b2), l1 = length(b1), l2 = length(b2);
+    const float vb1 = dot(v, b1), vb2 = dot(v, b2);
+    const float w2 = (vb1 * d12 - vb2 * l1 * l1) / (d12 * d12 - l1 * l1 * l2 * l2);
+    *u1 = (vb1 - w2 * d12) / (l1 * l1);
+    *u2 = w2;
+    *gid = __float_as_uint(a.w);
+}
+
+}  // namespace wr
