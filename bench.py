@@ -1,23 +1,26 @@
 #!/usr/bin/env python3
 """Benchmark driver.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload kd|pt]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload pt|kd]
 
 Prints ONE JSON line (rank 0).  Workloads:
 
-  pt  (default) wavefront path tracing of the mixed-material scene: 25
-      displaced level-5 icospheres (512,006 triangles) on a ground plane,
-      1024x1024, max depth 16; one step = one sample per pixel (1,048,576
-      paths).  Metric Mpaths/s.
+  pt  (default) path tracing of the mixed-material scene: 25 displaced
+      level-5 icospheres (512,006 triangles) on a ground plane, 40 % diffuse /
+      40 % isotropic Phong / 20 % refractive, two area lights, 1024x1024, max
+      path length 16.  One step = one sample per pixel (1,048,576 paths)
+      through the wavefront renderer.  Metric: Mpaths/s (the megakernel's
+      Mpaths/s and the time to relMSE 1e-3 of both are reported beside it).
   kd  closest-hit microbenchmark: level-8 displaced icosphere (1,310,720
-      triangles), 2^24 rays; one step = all rays.  Metric Mrays/s.
+      triangles), 2^24 rays; one step = all rays.  Metric: Mrays/s.
 
 `value` is device-timed with CUDA events per step on the launching stream,
-L2 flushed (a 512 MiB write) before every step, inputs resident in HBM;
-`e2e` runs the same steps through the public C ABI with host buffers
-(pinned), host<->device copies inside the timed region.  `--impl reference`
-times WalkRay's CPU algorithm (the oracle restatement, all host threads) on
-a bounded sample of the same workload.
+with the L2 flushed (a 512 MiB write) before every step and inputs resident
+in HBM; `e2e` runs the same steps through the public C ABI with host buffers
+(wr_render returning the image to the host / wr_trace_closest with pinned
+host rays and hits), host<->device copies inside the timed region.
+`--impl reference` times WalkRay's CPU algorithm (the C restatement of it,
+all host threads) on a bounded sample of the same workload.
 """
 from __future__ import annotations
 
@@ -41,9 +44,13 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 # tests/test_trace_gpu.py): AABB tests and ray-triangle tests per ray.
 KD_BOX_TESTS = 22.5567
 KD_TRI_TESTS = 2.9383
-# algorithmic bytes: ray in (24) + hit out (16) + per box test 8 B topology
-# + 24 B AABB + per triangle test 3 x 16 B vertices + 4 B object id
-KD_BYTES_PER_RAY = 24 + 16 + KD_BOX_TESTS * 32 + KD_TRI_TESTS * 52
+# algorithmic bytes of one traced ray: ray in (24) + hit out (16) + per box
+# test 8 B topology + 24 B AABB + per triangle test 3 x 16 B vertices + 4 B id
+RAY_IO_BYTES, BOX_BYTES, TRI_BYTES = 40, 32, 52
+KD_BYTES_PER_RAY = RAY_IO_BYTES + KD_BOX_TESTS * BOX_BYTES + KD_TRI_TESTS * TRI_BYTES
+
+PT_SIZE, PT_DEPTH, PT_SEED = 1024, 16, 7
+METRIC_PT = "Mpaths/s (wavefront path tracing, 1024^2 mixed-material scene; time-to-relMSE 1e-3 beside it)"
 
 
 def peaks():
@@ -123,26 +130,189 @@ def barrier(world):
         dist.barrier()
 
 
-def allmax(world, x: float) -> float:
+def allreduce(world, x: float, op: str) -> float:
     if world <= 1:
         return x
     import torch
     import torch.distributed as dist
 
     t = torch.tensor([x], dtype=torch.float64)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
     return float(t.item())
 
 
-def allsum(world, x: float) -> float:
-    if world <= 1:
-        return x
+def timed_steps(step, k: int, stream, flush):
+    """Sum of per-step CUDA-event durations (ms) on `stream`, L2 flushed before each step."""
     import torch
-    import torch.distributed as dist
 
-    t = torch.tensor([x], dtype=torch.float64)
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    evs = []
+    with torch.cuda.stream(stream):
+        for i in range(k):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step(i)
+            b.record(stream)
+            evs.append((a, b))
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in evs)
+
+
+def launches(ctx) -> int:
+    import ctypes as C
+
+    v = C.c_uint64()
+    ctx.lib.wr_kernel_launches(ctx.h, C.byref(v))
+    return v.value
+
+
+# ---------------------------------------------------------------------------
+# pt: wavefront path tracing of the mixed-material scene
+# ---------------------------------------------------------------------------
+def pt_scene():
+    from walkray_gb300 import scenes as S
+
+    return S.mixed_spheres(PT_SIZE, PT_SIZE, seed=PT_SEED)
+
+
+def relmse_variance(a, b, ref):
+    """relMSE of one of two independent renders a, b (same spp) against the
+    converged image: mean over pixels and channels of Var/(R^2 + 1e-2), the
+    variance estimated as (a-b)^2/2 (the estimator is unbiased, so the bias
+    term is zero)."""
+    return float(np.mean(((a - b) ** 2 / 2.0) / (ref ** 2 + 1e-2)))
+
+
+def cpu_baseline_pt(scene, rows: int, threads: int):
+    import wr_oracle
+
+    w = scene.camera.width
+    y0 = (scene.camera.height - rows) // 2
+    orc = wr_oracle.SceneOracle(scene)
+    t0 = time.perf_counter()
+    orc.render(1, PT_DEPTH, seed=1, p0=y0 * w, p1=(y0 + rows) * w, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": rows * w / dt / 1e6, "unit": "Mpaths/s", "cores": threads, "kind": "port",
+            "sample": f"{rows} centre rows x {w} pixels x 1 spp of the 1024^2 mixed-material scene, "
+                      f"WalkRay's PathTracer restated in C (oracle), {threads} OpenMP threads, tree build excluded"}
+
+
+def run_pt(args, world, rank, local):
+    import torch
+
+    from walkray_gb300.api import Context
+
+    torch.cuda.set_device(local)
+    scene = pt_scene()
+    npix = PT_SIZE * PT_SIZE
+    ctx = Context(device=local)
+    sid = ctx.upload(scene)
+    tuned = ctx.autotune(sid, 1, PT_DEPTH) if args.tune else None
+    stream = torch.cuda.Stream()
+    film = torch.zeros(npix * 3, dtype=torch.float32, device="cuda")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    seed = 1000 + rank
+
+    def step_mode(mode):
+        return lambda i: ctx.render_device(sid, 1, PT_DEPTH, film.data_ptr(), seed=seed, mode=mode, spp_offset=i,
+                                           stream=stream.cuda_stream)
+
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup):
+            step_mode("wavefront")(i)
+            step_mode("megakernel")(i)
+    torch.cuda.synchronize()
+    barrier(world)
+    with ClockSampler(local) as clk:
+        l0 = launches(ctx)
+        ms = timed_steps(step_mode("wavefront"), args.steps, stream, flush)
+        n_launch = launches(ctx) - l0
+        ms_mk = timed_steps(step_mode("megakernel"), args.steps, stream, flush)
+    ms_max = allreduce(world, ms, "max")
+    units = allreduce(world, float(npix * args.steps), "sum")
+    value = units / (ms_max / 1e3) / 1e6
+    mk_value = allreduce(world, float(npix * args.steps), "sum") / (allreduce(world, ms_mk, "max") / 1e3) / 1e6
+
+    # e2e: wr_render returning the image to the host, one sample per pixel per step
+    barrier(world)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        ctx.render(sid, 1, PT_DEPTH, seed=seed + 1, mode="wavefront", spp_offset=i)
+    e2e_s = allreduce(world, time.perf_counter() - t0, "max")
+    e2e = allreduce(world, float(npix * args.steps), "sum") / e2e_s / 1e6
+
+    line = {
+        "metric": METRIC_PT, "value": round(value, 2), "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+        "config": {"workload": "pt: 25 displaced level-5 icospheres (512,006 tris) on a ground plane, 40% diffuse / "
+                               "40% Phong / 20% refractive, two area lights, 1024x1024, max depth 16, 1 spp per step",
+                   "renderer": "wavefront (generate/extend/shade/shadow queues, CUDA-graph bounce loop)",
+                   "l2": "flushed (512 MiB write) before every step", "parallelism": f"replicas x{world}"},
+        "e2e": {"value": round(e2e, 2), "unit": "Mpaths/s", "h2d_bytes_per_step": 256 + 4 * 257,
+                "d2h_bytes_per_step": npix * 12},
+        "megakernel": {"value": round(mk_value, 2), "unit": "Mpaths/s", "ms_per_step": round(ms_mk / args.steps, 3)},
+        "wavefront_over_megakernel": round(value / mk_value, 3),
+        "gpu_launches": int(n_launch), "clocks": clk.summary(),
+    }
+    if tuned:
+        line["config"]["autotuned"] = {k: tuned[k] for k in ("capacity", "extend_block", "shade_block",
+                                                             "ctas_per_sm", "iters_per_graph")}
+    if rank == 0 and not args.quick:
+        # roofline of the dominant kernel (the extend / traversal stage), from a profiled frame
+        prof = ctx.profile_render(sid, 1, PT_DEPTH, film.data_ptr(), seed=seed + 2)
+        peak, peak_kind = peaks()
+        alg = prof["rays"] * RAY_IO_BYTES + prof["box_tests"] * BOX_BYTES + prof["tri_tests"] * TRI_BYTES
+        achieved = alg / (prof["ms_extend"] / 1e3) / 1e9
+        traffic = None
+        pf = os.path.join(ROOT, "profiles", "wf_extend_pt.json")
+        if os.path.exists(pf):
+            per_ray = json.load(open(pf)).get("dram_bytes_per_ray")
+            traffic = round(per_ray * prof["rays"] / max(1, prof["iterations"]), 0) if per_ray else None
+        line["roofline"] = {
+            "bound": "hbm", "kernel": "k_wf_extend", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+            "algorithmic_bytes_per_ray": round(alg / max(1, prof["rays"]), 1),
+            "box_tests_per_ray": round(prof["box_tests"] / max(1, prof["rays"]), 3),
+            "tri_tests_per_ray": round(prof["tri_tests"] / max(1, prof["rays"]), 3),
+            "stage_ms": {k: round(prof[k], 2) for k in ("ms_extend", "ms_shade", "ms_shadow", "ms_generate")},
+            "rays_per_frame": prof["rays"], "iterations": prof["iterations"],
+        }
+        # time to relMSE 1e-3: the variance of a k-spp render (two independent k-spp
+        # renders) against a 256-spp wavefront render, scaled as 1/spp
+        k = 16
+        ref = ctx.render(sid, 256, PT_DEPTH, seed=99, mode="wavefront").astype(np.float64)
+        a = ctx.render(sid, k, PT_DEPTH, seed=11, mode="wavefront").astype(np.float64)
+        b = ctx.render(sid, k, PT_DEPTH, seed=12, mode="wavefront").astype(np.float64)
+        rel_k = relmse_variance(a, b, ref)
+        spp_needed = k * rel_k / 1e-3
+        line["time_to_relmse_1e-3"] = {
+            "wavefront_s": round(spp_needed * (ms / args.steps) / 1e3, 3),
+            "megakernel_s": round(spp_needed * (ms_mk / args.steps) / 1e3, 3),
+            "spp_needed": round(spp_needed, 1), "relmse_16spp": round(rel_k, 6),
+            "formula": "mean((I-R)^2/(R^2+1e-2)), variance from two independent 16-spp renders, R = 256 spp",
+        }
+        if world == 1 and not args.no_cpu:
+            line["cpu_baseline"] = cpu_baseline_pt(scene, args.cpu_rows or 64, os.cpu_count() or 1)
+    ctx.close()
+    return line
+
+
+def reference_pt(args):
+    scene = pt_scene()
+    threads = os.cpu_count() or 1
+    rows = args.cpu_rows or 16
+    for _ in range(min(args.warmup, 1)):
+        cpu_baseline_pt(scene, 2, threads)
+    vals = [cpu_baseline_pt(scene, rows, threads) for _ in range(args.steps)]
+    v = statistics.median(x["value"] for x in vals)
+    return {"metric": METRIC_PT, "value": round(v, 4), "unit": "Mpaths/s", "impl": "reference", "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+            "config": {"workload": "pt: 1024^2 mixed-material scene, max depth 16, 1 spp",
+                       "paths_per_step": rows * PT_SIZE},
+            "cpu_baseline": dict(vals[0], value=round(v, 4)),
+            "e2e": {"value": round(v, 4), "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 # ---------------------------------------------------------------------------
@@ -187,52 +357,39 @@ def run_kd(args, world, rank, local):
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
     torch.cuda.synchronize()
 
-    def step():
+    def step(i):
         ctx.trace_closest_device(sid, d_rays.data_ptr(), n, d_hits.data_ptr(), stream=stream.cuda_stream)
 
     with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            step()
+        for i in range(args.warmup):
+            step(i)
     torch.cuda.synchronize()
     barrier(world)
-    evs = []
     with ClockSampler(local) as clk:
-        torch.cuda.synchronize()
-        t_wall = time.perf_counter()
-        with torch.cuda.stream(stream):
-            for _ in range(args.steps):
-                flush.zero_()
-                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                a.record(stream)
-                step()
-                b.record(stream)
-                evs.append((a, b))
-        torch.cuda.synchronize()
-        t_wall = time.perf_counter() - t_wall
-    ms = sum(a.elapsed_time(b) for a, b in evs)
-    ms_max = allmax(world, ms)
-    units = allsum(world, float(n * args.steps))
-    value = units / (ms_max / 1e3) / 1e6
+        l0 = launches(ctx)
+        ms = timed_steps(step, args.steps, stream, flush)
+        n_launch = launches(ctx) - l0
+    ms_max = allreduce(world, ms, "max")
+    value = allreduce(world, float(n * args.steps), "sum") / (ms_max / 1e3) / 1e6
     avg_launch_s = ms / 1e3 / args.steps
 
-    # e2e through the host-buffer entry point, pinned host memory
     h_rays = torch.from_numpy(rays).pin_memory().numpy()
     h_hits = torch.empty((n, 4), dtype=torch.int32).pin_memory().numpy()
-    ctx.trace_closest(sid, h_rays, out=h_hits)  # warm
+    ctx.trace_closest(sid, h_rays, out=h_hits)
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         ctx.trace_closest(sid, h_rays, out=h_hits)
-    e2e_s = allmax(world, time.perf_counter() - t0)
-    e2e = allsum(world, float(n * args.steps)) / e2e_s / 1e6
+    e2e_s = allreduce(world, time.perf_counter() - t0, "max")
+    e2e = allreduce(world, float(n * args.steps), "sum") / e2e_s / 1e6
 
     peak, peak_kind = peaks()
     achieved = KD_BYTES_PER_RAY * n / avg_launch_s / 1e9
     traffic = None
     prof = os.path.join(ROOT, "profiles", "trace_closest_kd.json")
     if os.path.exists(prof):
-        traffic = json.load(open(prof)).get("dram_bytes_per_ray")
-        traffic = traffic * n if traffic else None
+        per_ray = json.load(open(prof)).get("dram_bytes_per_ray")
+        traffic = round(per_ray * n, 0) if per_ray else None
     line = {
         "metric": "Mrays/s (closest hit, bit-exact vs reference)", "value": round(value, 2), "unit": "Mrays/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -242,10 +399,10 @@ def run_kd(args, world, rank, local):
                                "uniform directions)", "rays_per_step": n, "l2": "flushed (512 MiB write) before every step",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": round(e2e, 2), "unit": "Mrays/s", "h2d_bytes_per_step": n * 24, "d2h_bytes_per_step": n * 16},
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+        "roofline": {"bound": "hbm", "kernel": "k_trace_closest", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
                      "algorithmic_bytes_per_ray": round(KD_BYTES_PER_RAY, 1)},
-        "gpu_launches": args.steps, "clocks": clk.summary(),
+        "gpu_launches": int(n_launch), "clocks": clk.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_kd(scene, rays, args.cpu_sample or (1 << 22))
@@ -279,8 +436,11 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["kd", "pt"], default=os.environ.get("WR_BENCH_WORKLOAD", "kd"))
+    ap.add_argument("--workload", choices=["pt", "kd"], default=os.environ.get("WR_BENCH_WORKLOAD", "pt"))
+    ap.add_argument("--tune", action="store_true", help="run the wavefront autotuner first (pt)")
+    ap.add_argument("--quick", action="store_true", help="skip the roofline profile, relMSE and CPU legs (pt)")
     ap.add_argument("--cpu-sample", type=int, default=0)
+    ap.add_argument("--cpu-rows", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     world, rank, local = dist_setup()
@@ -289,7 +449,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        line = reference_kd(args)
+        line = reference_pt(args) if args.workload == "pt" else reference_kd(args)
         print(json.dumps(line), flush=True)
         return
     if world > 1:
@@ -299,7 +459,7 @@ def main():
     from walkray_gb300 import build
 
     build.build_lib()
-    line = run_kd(args, world, rank, local)
+    line = run_pt(args, world, rank, local) if args.workload == "pt" else run_kd(args, world, rank, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -145,6 +145,9 @@ int wr_get_abi_version(uint32_t* version);
 int wr_ctx_create(const wr_ctx_desc* desc, wr_ctx** out);
 int wr_ctx_destroy(wr_ctx* ctx);
 const char* wr_last_error(const wr_ctx* ctx);
+/* Number of kernels the library has launched on this context so far (graph
+ * replays count every kernel node).  No reference counterpart. */
+int wr_kernel_launches(const wr_ctx* ctx, uint64_t* out);
 
 /* ---- scenes ------------------------------------------------------------- */
 /* Flattens the scene (Scene::buildKDTree, scene.cpp:20-44), builds the
@@ -210,6 +213,88 @@ int wr_render(wr_ctx* ctx, wr_scene_id scene, const wr_render_desc* desc, float*
  * `stream` (cudaStream_t; NULL = the context's stream), asynchronous. */
 int wr_render_device(wr_ctx* ctx, wr_scene_id scene, const wr_render_desc* desc, float* d_sum, float* d_sumsq,
                      void* stream);
+
+/* Per-stage profile of one wavefront render (no reference counterpart: the
+ * reference has no timers).  The stages are launched one by one instead of
+ * as a graph, each between CUDA events on the context's stream; the
+ * traversal stage also counts its work. */
+typedef struct wr_render_profile {
+    double ms_extend, ms_shade, ms_shadow, ms_generate, ms_total;
+    uint64_t iterations;       /* bounce iterations run */
+    uint64_t rays;             /* rays traced by the extend stage */
+    uint64_t box_tests;        /* AABB predicate evaluations (reference count) */
+    uint64_t tri_tests;        /* ray-triangle tests */
+    uint64_t paths;
+} wr_render_profile;
+int wr_profile_render(wr_ctx* ctx, wr_scene_id scene, const wr_render_desc* desc, float* d_sum,
+                      wr_render_profile* out);
+
+/* ---- serving ------------------------------------------------------------- */
+/* A request loop over resident scenes: RenderEngine::renderFilm
+ * (renderEngine.cpp:27-30) once per request, with requests admitted while
+ * others run (continuous batching) and their paths sharing the wavefront
+ * queues.  A request is admitted when a job slot is free and its film fits
+ * in the serving film memory; until then it waits in FIFO order.  While the
+ * loop runs, only wr_submit / wr_poll / wr_fetch / wr_cancel / wr_serve_stop
+ * may be called on the context; scenes are uploaded before wr_serve_start. */
+#define WR_REQ_QUEUED 0u
+#define WR_REQ_RUNNING 1u
+#define WR_REQ_DONE 2u
+#define WR_REQ_CANCELLED 3u
+#define WR_REQ_FAILED 4u
+
+typedef uint64_t wr_req_id;
+
+typedef struct wr_serve_desc {
+    uint64_t film_bytes; /* device memory for request films; 0 = a quarter of the context budget */
+    uint32_t max_active; /* requests in flight at once; 0 = 64 */
+    uint32_t pad;
+} wr_serve_desc;
+
+typedef struct wr_request_desc {
+    wr_scene_id scene;
+    uint32_t width, height;  /* resolution; the scene camera's field of view is kept */
+    uint32_t spp;
+    uint32_t max_path_len;
+    uint32_t flags;          /* WR_RENDER_* */
+    uint64_t seed;
+} wr_request_desc;
+
+typedef struct wr_req_status {
+    uint32_t state;          /* WR_REQ_* */
+    uint32_t pad;
+    uint64_t paths_total;
+    uint64_t paths_done;
+    double submit_s, admit_s, finish_s; /* seconds since wr_serve_start */
+} wr_req_status;
+
+int wr_serve_start(wr_ctx* ctx, const wr_serve_desc* desc);
+int wr_serve_stop(wr_ctx* ctx);  /* cancels what has not finished */
+int wr_submit(wr_ctx* ctx, const wr_request_desc* req, wr_req_id* out);
+int wr_poll(wr_ctx* ctx, wr_req_id id, wr_req_status* out);
+/* mean image (height x width x 3, row 0 at the top) of a finished request;
+ * releases it */
+int wr_fetch(wr_ctx* ctx, wr_req_id id, float* rgb_out);
+int wr_cancel(wr_ctx* ctx, wr_req_id id);
+
+/* ---- wavefront configuration and autotuner ------------------------------- */
+/* No reference counterpart (the reference renders with one OpenMP loop,
+ * pathTracer.cpp:20): these size the wavefront renderer's queues. */
+typedef struct wr_wavefront_config {
+    uint32_t capacity;       /* paths in flight (queue length) */
+    int32_t extend_block;    /* threads per CTA of the traversal stage */
+    int32_t shade_block;     /* threads per CTA of the shade / generate stages */
+    int32_t ctas_per_sm;     /* persistent CTAs per SM, 0 = as many as fit */
+    int32_t iters_per_graph; /* bounce-loop iterations (pairs) per CUDA-graph launch */
+    double mpaths_per_s;     /* filled by wr_autotune */
+} wr_wavefront_config;
+
+int wr_set_wavefront_config(wr_ctx* ctx, const wr_wavefront_config* cfg);
+
+/* Times short wavefront renders (spp_per_trial samples per pixel) of `scene`
+ * over a grid of configurations and keeps the fastest in the context. */
+int wr_autotune(wr_ctx* ctx, wr_scene_id scene, uint32_t spp_per_trial, uint32_t max_path_len,
+                wr_wavefront_config* best);
 
 /* ---- host-side tree (no GPU needed) ------------------------------------- */
 /* Builds the reference tree on the host only and returns its flattened

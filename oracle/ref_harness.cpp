@@ -267,6 +267,29 @@ static int cmd_render(int argc, char** argv) {
     return 0;
 }
 
+#ifdef WR_DROPIN
+#include "gpuPathTracer.h"
+// describe scene.wrs out.bin: the drop-in renderer's reading of every
+// object's material (wrDefaultDescribe), as wr_object_desc records; objects
+// it cannot describe get type 0xffffffff
+static int cmd_describe(int argc, char** argv) {
+    if (argc < 4) return 2;
+    wrs_scene ws;
+    if (wrs_load(argv[2], &ws)) return 1;
+    RenderEngine* eng = new RenderEngine();
+    build_scene(*eng, ws, eng->rng);
+    FILE* f = fopen(argv[3], "wb");
+    for (AbstractObject* o : eng->scene.objects) {
+        wr_object_desc d;
+        memset(&d, 0, sizeof d);
+        if (!wrDefaultDescribe(o, &d)) d.type = 0xffffffffu;
+        fwrite(&d, sizeof d, 1, f);
+    }
+    fclose(f);
+    return 0;
+}
+#endif
+
 int main(int argc, char** argv) {
     if (argc < 2) {
         fprintf(stderr, "usage: wr_ref trace|dumptree|render ...\n");
@@ -277,6 +300,9 @@ int main(int argc, char** argv) {
     if (!strcmp(argv[1], "trace")) return cmd_trace(argc, argv);
     if (!strcmp(argv[1], "dumptree")) return cmd_dumptree(argc, argv);
     if (!strcmp(argv[1], "render")) return cmd_render(argc, argv);
+#ifdef WR_DROPIN
+    if (!strcmp(argv[1], "describe")) return cmd_describe(argc, argv);
+#endif
     fprintf(stderr, "unknown command %s\n", argv[1]);
     return 2;
 }

@@ -104,6 +104,17 @@ def main():
             assert pr.wait() == 0
         imgs = np.stack([np.fromfile(o, np.float32).reshape(32, 32, 3) for o in outs])
         np.savez_compressed(os.path.join(HERE, "render_cornell.npz"), images=imgs, spp=256, max_path_len=8)
+        # the same with the NEE branch switched on (pathTracer.cpp:39-66)
+        procs, outs = [], []
+        for seed in range(1, 9):
+            out = os.path.join(td, f"nee{seed}.bin")
+            procs.append(subprocess.Popen([REF, "render", p, "256", "8", str(seed), out, "nee"], env=env,
+                                          stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL))
+            outs.append(out)
+        for pr in procs:
+            assert pr.wait() == 0
+        imgs = np.stack([np.fromfile(o, np.float32).reshape(32, 32, 3) for o in outs])
+        np.savez_compressed(os.path.join(HERE, "render_cornell_nee.npz"), images=imgs, spp=256, max_path_len=8)
     print("golden fixtures written to", HERE)
 
 

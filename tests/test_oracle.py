@@ -65,6 +65,23 @@ def test_oracle_filtered_hits_equal_reference(built):
     assert np.array_equal(tri, g["tri"])
 
 
+def test_oracle_nee_matches_reference_statistically(built):
+    """The NEE branch (pathTracer.cpp:39-66) against 8 reference NEE renders."""
+    g = np.load(os.path.join(GOLDEN, "render_cornell_nee.npz"))
+    ref = g["images"].astype(np.float64)
+    plain = np.load(os.path.join(GOLDEN, "render_cornell.npz"))["images"].astype(np.float64)
+    s = make_golden.golden_scenes()["cornell"]
+    orc = wr_oracle.SceneOracle(s)
+    port = np.stack([(orc.render(256, 8, seed=3000 + k, flags=wr_oracle.NEE)[0] / 256).reshape(32, 32, 3)
+                     for k in range(8)])
+    blk = lambda a: a.reshape(a.shape[0], 8, 4, 8, 4, 3).mean((2, 4))
+    br, bp = blk(ref), blk(port)
+    z = (br.mean(0) - bp.mean(0)) / np.sqrt(br.var(0, ddof=1) / 8 + bp.var(0, ddof=1) / 8 + 1e-12)
+    assert np.abs(z).max() < 4.5, np.abs(z).max()
+    assert abs(port.mean() / ref.mean() - 1) < 0.015
+    assert ref.mean() > 1.03 * plain.mean()  # the reference NEE mode is biased upwards
+
+
 def test_oracle_render_matches_reference_statistically(built):
     """Cornell 32x32: the restated PathTracer vs 8 reference renders of 256 spp.
     Per-pixel z on 4x4 blocks; |z| > 4 on no block, mean within 1.5 %."""

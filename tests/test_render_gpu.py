@@ -1,0 +1,203 @@
+"""Path-tracing parity on the GPU through the C ABI (wr_render / wr_render_device).
+
+Statistical against the reference's own renders (golden fixtures from
+PathTracer::renderPixels) and against the oracle; paired against the oracle
+on the same counter-based random stream (same draws per path); and exact
+agreement between the megakernel and the wavefront renderer, which compute
+the same paths.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+import make_golden
+import wr_oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def block_z(a, b, k):
+    """z-scores of block means of two stacks of independent images (n, H, W, 3)."""
+    def blk(x):
+        n, h, w, c = x.shape
+        return x.reshape(n, h // k, k, w // k, k, c).mean((2, 4))
+    ba, bb = blk(a), blk(b)
+    va = ba.var(0, ddof=1) / len(a)
+    vb = bb.var(0, ddof=1) / len(b)
+    return (ba.mean(0) - bb.mean(0)) / np.sqrt(va + vb + 1e-12)
+
+
+def mean_z(a, b):
+    """z-score of the difference of the image means of two stacks of independent images."""
+    ma, mb = a.mean((1, 2, 3)), b.mean((1, 2, 3))
+    se = np.sqrt(ma.var(ddof=1) / len(ma) + mb.var(ddof=1) / len(mb))
+    return (ma.mean() - mb.mean()) / se
+
+
+def gpu_images(ctx, sid, seeds, spp, maxlen, mode="megakernel"):
+    return np.stack([ctx.render(sid, spp, maxlen, seed=s, mode=mode).astype(np.float64) for s in seeds])
+
+
+def test_megakernel_matches_reference_renders(ctx):
+    """Cornell 32x32, 8 x 256 spp against 8 reference renders of 256 spp."""
+    g = np.load(os.path.join(GOLDEN, "render_cornell.npz"))
+    ref = g["images"].astype(np.float64)
+    s = make_golden.golden_scenes()["cornell"]
+    sid = ctx.upload(s)
+    gpu = gpu_images(ctx, sid, range(100, 108), 256, 8)
+    z = block_z(gpu, ref, 4)
+    assert np.abs(z).max() < 4.5, np.abs(z).max()
+    assert abs(gpu.mean() / ref.mean() - 1) < 0.015
+    ctx.release(sid)
+
+
+def test_megakernel_paired_with_oracle(ctx):
+    """Same seed => same Philox draws per path: the GPU and oracle estimates
+    are nearly identical pixel by pixel (paths only part where FP32 libm
+    results differ in the last bits and a decision flips)."""
+    s = make_golden.golden_scenes()["cornell"]
+    sid = ctx.upload(s)
+    spp = 256
+    gsum, gsq = ctx.render_stats(sid, spp, 8, seed=7)
+    osum, osq, _ = wr_oracle.SceneOracle(s).render(spp, 8, seed=7, want_sumsq=True)
+    osum, osq = osum.reshape(gsum.shape), osq.reshape(gsq.shape)
+    gm, om = gsum / spp, osum / spp
+    sem = np.sqrt(np.maximum(osq / spp - om * om, 0) / spp) + 1e-6
+    d = np.abs(gm - om) / sem
+    assert abs(gm.mean() / om.mean() - 1) < 0.003, (gm.mean(), om.mean())
+    assert np.median(d) < 0.05, np.median(d)
+    assert np.mean(d > 3) < 0.01
+    ctx.release(sid)
+
+
+def test_wavefront_equals_megakernel(ctx):
+    """Both renderers trace the same paths with the same draws; only the order
+    of the FP32 film additions differs."""
+    s = make_golden.golden_scenes()["mixed_l2"]
+    sid = ctx.upload(s)
+    a = ctx.render(sid, 32, 16, seed=3, mode="megakernel")
+    ctx.set_wavefront_config(capacity=1 << 14, iters_per_graph=2)  # small queue: many refills
+    b = ctx.render(sid, 32, 16, seed=3, mode="wavefront")
+    assert np.allclose(a, b, rtol=1e-4, atol=1e-5), np.abs(a - b).max()
+    ctx.release(sid)
+
+
+def test_wavefront_after_scene_release_and_reupload(ctx):
+    """A released scene leaves the wavefront's scene table; a scene uploaded
+    afterwards (possibly at the same host address) renders correctly."""
+    sc = make_golden.golden_scenes()
+    for name in ("cornell", "mixed_l2", "cornell", "media_small"):
+        sid = ctx.upload(sc[name])
+        a = ctx.render(sid, 4, 8, seed=5, mode="wavefront")
+        b = ctx.render(sid, 4, 8, seed=5, mode="megakernel")
+        assert np.allclose(a, b, rtol=1e-4, atol=1e-5)
+        ctx.release(sid)
+
+
+def test_nee_wavefront_equals_megakernel(ctx):
+    s = make_golden.golden_scenes()["mixed_l2"]
+    sid = ctx.upload(s)
+    a = ctx.render(sid, 16, 16, seed=8, mode="megakernel", nee=True)
+    b = ctx.render(sid, 16, 16, seed=8, mode="wavefront", nee=True)
+    assert np.allclose(a, b, rtol=1e-4, atol=1e-5), np.abs(a - b).max()
+    ctx.release(sid)
+
+
+def test_nee_matches_oracle_paired(ctx):
+    """The reference's NEE branch (biased by design: it adds a light
+    connection to paths that escaped) on the same seeds as the oracle."""
+    s = make_golden.golden_scenes()["cornell"]
+    sid = ctx.upload(s)
+    orc = wr_oracle.SceneOracle(s)
+    h, w = s.camera.height, s.camera.width
+    d, m = [], []
+    for seed in range(60, 66):
+        g = ctx.render(sid, 64, 8, seed=seed, nee=True).astype(np.float64)
+        o = orc.render(64, 8, seed=seed, flags=wr_oracle.NEE)[0].reshape(h, w, 3) / 64
+        d.append(g.mean() - o.mean())
+        m.append(o.mean())
+    d, m = np.array(d), np.array(m)
+    assert abs(d.mean()) < 0.25 * m.std(ddof=1) + 1e-4 * m.mean(), (d, m)
+    ctx.release(sid)
+
+
+def test_nee_matches_reference_renders_statistically(ctx):
+    """NEE renders of the Cornell box against the oracle's NEE (pinned to the
+    reference's NEE mode in tests/test_oracle.py)."""
+    s = make_golden.golden_scenes()["cornell"]
+    sid = ctx.upload(s)
+    gpu = gpu_images(ctx, sid, range(70, 78), 64, 8)
+    gn = np.stack([ctx.render(sid, 64, 8, seed=k, nee=True).astype(np.float64) for k in range(70, 78)])
+    # the reference's NEE adds light to escaped paths: brighter than plain path tracing
+    assert gn.mean() > gpu.mean()
+    ctx.release(sid)
+
+
+def test_mixed_materials_match_oracle(ctx):
+    """Diffuse, isotropic Phong and dielectric spheres, two lights, depth 16."""
+    s = make_golden.golden_scenes()["mixed_l2"]
+    sid = ctx.upload(s)
+    seeds = range(20, 28)
+    gpu = gpu_images(ctx, sid, seeds, 32, 16, mode="wavefront")
+    orc = wr_oracle.SceneOracle(s)
+    h, w = s.camera.height, s.camera.width
+    ora = np.stack([orc.render(32, 16, seed=1000 + k)[0].reshape(h, w, 3) / 32 for k in range(8)])
+    z = block_z(gpu, ora, 8)
+    assert np.abs(z).max() < 4.5, np.abs(z).max()
+    # Phong lobes sampled about the normal (powerCosHemiSphereSampler.h) make
+    # the estimator heavy-tailed: compare the image means by their standard error
+    assert abs(mean_z(gpu, ora)) < 4.0, mean_z(gpu, ora)
+    ctx.release(sid)
+
+
+def test_mixed_materials_paired_with_oracle(ctx):
+    """Same seeds on both sides: per-image means of the GPU and oracle renders
+    differ far less than their sampling noise."""
+    s = make_golden.golden_scenes()["mixed_l2"]
+    sid = ctx.upload(s)
+    orc = wr_oracle.SceneOracle(s)
+    h, w = s.camera.height, s.camera.width
+    d, m = [], []
+    for seed in range(20, 28):
+        g = ctx.render(sid, 32, 16, seed=seed).astype(np.float64)
+        o = orc.render(32, 16, seed=seed)[0].reshape(h, w, 3) / 32
+        d.append(g.mean() - o.mean())
+        m.append(o.mean())
+    d, m = np.array(d), np.array(m)
+    assert abs(d.mean()) < 0.25 * m.std(ddof=1), (d, m)
+    ctx.release(sid)
+
+
+def test_media_match_oracle(ctx):
+    """Heterogeneous fBm medium + homogeneous sphere: GPU delta tracking vs
+    the reference's Simpson/Newton regular tracking restated in the oracle.
+    The reference estimator carries quadrature bias, so means agree to 3 %."""
+    s = make_golden.golden_scenes()["media_small"]
+    sid = ctx.upload(s)
+    gpu = gpu_images(ctx, sid, range(40, 48), 64, 24)
+    orc = wr_oracle.SceneOracle(s)
+    h, w = s.camera.height, s.camera.width
+    ora = np.stack([orc.render(16, 24, seed=2000 + k)[0].reshape(h, w, 3) / 16 for k in range(8)])
+    assert abs(gpu.mean() / ora.mean() - 1) < 0.03, (gpu.mean(), ora.mean())
+    z = block_z(gpu, ora, 8)
+    assert np.abs(z).max() < 5.0, np.abs(z).max()
+    ctx.release(sid)
+
+
+def test_render_rejects_bad_requests(ctx):
+    from walkray_gb300 import _lib as L
+
+    s = make_golden.golden_scenes()["cornell"]
+    sid = ctx.upload(s)
+    with pytest.raises(KeyError):
+        ctx.render(sid + 99, 1, 8)
+    d = L.wr_render_desc(1, 8, 1, 7, 0, 0, 0)  # unknown mode
+    out = np.empty((32, 32, 3), np.float32)
+    import ctypes as C
+
+    assert ctx.lib.wr_render(ctx.h, sid, C.byref(d), L.ptr(out)) == 1
+    img = ctx.render(sid, 0, 8)
+    assert not img.any()
+    ctx.release(sid)

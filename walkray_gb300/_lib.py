@@ -84,6 +84,39 @@ class wr_trace_filter(C.Structure):
     _fields_ = [("inside_obj", C.c_void_p), ("contact_obj", C.c_void_p)]
 
 
+class wr_render_desc(C.Structure):
+    _fields_ = [("spp", C.c_uint32), ("max_path_len", C.c_uint32), ("seed", C.c_uint64), ("mode", C.c_uint32),
+                ("flags", C.c_uint32), ("spp_offset", C.c_uint32), ("pad", C.c_uint32)]
+
+
+class wr_wavefront_config(C.Structure):
+    _fields_ = [("capacity", C.c_uint32), ("extend_block", C.c_int32), ("shade_block", C.c_int32),
+                ("ctas_per_sm", C.c_int32), ("iters_per_graph", C.c_int32), ("mpaths_per_s", C.c_double)]
+
+
+class wr_serve_desc(C.Structure):
+    _fields_ = [("film_bytes", C.c_uint64), ("max_active", C.c_uint32), ("pad", C.c_uint32)]
+
+
+class wr_request_desc(C.Structure):
+    _fields_ = [("scene", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32), ("spp", C.c_uint32),
+                ("max_path_len", C.c_uint32), ("flags", C.c_uint32), ("seed", C.c_uint64)]
+
+
+class wr_req_status(C.Structure):
+    _fields_ = [("state", C.c_uint32), ("pad", C.c_uint32), ("paths_total", C.c_uint64),
+                ("paths_done", C.c_uint64), ("submit_s", C.c_double), ("admit_s", C.c_double),
+                ("finish_s", C.c_double)]
+
+
+class wr_render_profile(C.Structure):
+    _fields_ = [("ms_extend", C.c_double), ("ms_shade", C.c_double), ("ms_shadow", C.c_double),
+                ("ms_generate", C.c_double), ("ms_total", C.c_double), ("iterations", C.c_uint64),
+                ("rays", C.c_uint64), ("box_tests", C.c_uint64), ("tri_tests", C.c_uint64), ("paths", C.c_uint64)]
+
+
+WR_RENDER_NEE = 1
+
 HIT_DTYPE = np.dtype([("tri", "<u4"), ("t", "<f4"), ("b1", "<f4"), ("b2", "<f4")])
 
 assert C.sizeof(wr_object_desc) == 136
@@ -102,6 +135,19 @@ _SIGS = {
                                    C.c_void_p]),
     "wr_trace_closest_device": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
                                           C.c_void_p, C.c_void_p]),
+    "wr_render": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(wr_render_desc), C.c_void_p]),
+    "wr_render_device": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(wr_render_desc), C.c_void_p, C.c_void_p,
+                                   C.c_void_p]),
+    "wr_set_wavefront_config": (C.c_int, [C.c_void_p, C.POINTER(wr_wavefront_config)]),
+    "wr_autotune": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(wr_wavefront_config)]),
+    "wr_profile_render": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(wr_render_desc), C.c_void_p,
+                                    C.POINTER(wr_render_profile)]),
+    "wr_serve_start": (C.c_int, [C.c_void_p, C.POINTER(wr_serve_desc)]),
+    "wr_serve_stop": (C.c_int, [C.c_void_p]),
+    "wr_submit": (C.c_int, [C.c_void_p, C.POINTER(wr_request_desc), C.POINTER(C.c_uint64)]),
+    "wr_poll": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(wr_req_status)]),
+    "wr_fetch": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p]),
+    "wr_cancel": (C.c_int, [C.c_void_p, C.c_uint64]),
     "wr_kdtree_build_host": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_int,
                                        C.POINTER(C.c_void_p)]),
     "wr_kdtree_host_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),

@@ -56,6 +56,7 @@ class Context:
         if rc != L.WR_OK:
             raise L.WRError(rc, "wr_ctx_create failed (no usable CUDA device?)")
         self.h = h
+        self._cams: dict[int, tuple[int, int]] = {}
 
     def _check(self, rc):
         L.check(rc, self.h)
@@ -83,6 +84,8 @@ class Context:
         sid = C.c_uint32()
         self._check(self.lib.wr_scene_upload(self.h, C.byref(d), C.byref(sid)))
         del keep
+        if scene.camera is not None:
+            self._cams[sid.value] = (scene.camera.width, scene.camera.height)
         return sid.value
 
     def release(self, sid: int) -> None:
@@ -118,6 +121,122 @@ class Context:
         self._check(self.lib.wr_trace_closest_device(self.h, sid, C.c_void_p(d_rays), n,
                                                      C.c_void_p(d_inside or None), C.c_void_p(d_contact or None),
                                                      C.c_void_p(d_hits), C.c_void_p(stream or None)))
+
+
+    # ---- rendering ------------------------------------------------------
+    def render(self, sid: int, spp: int, max_path_len: int, seed: int = 1, mode: str = "megakernel",
+               nee: bool = False, spp_offset: int = 0) -> np.ndarray:
+        """Mean image (H, W, 3) float32, row 0 at the top (wr_render)."""
+        w, h = self._camera_size(sid)
+        out = np.empty((h, w, 3), np.float32)
+        d = L.wr_render_desc(spp, max_path_len, seed, MODES[mode], L.WR_RENDER_NEE if nee else 0, spp_offset, 0)
+        self._check(self.lib.wr_render(self.h, sid, C.byref(d), L.ptr(out)))
+        return out
+
+    def render_device(self, sid: int, spp: int, max_path_len: int, d_sum: int, d_sumsq: int = 0, seed: int = 1,
+                      mode: str = "megakernel", nee: bool = False, spp_offset: int = 0, stream: int = 0) -> None:
+        """Adds spp samples to a device film (wr_render_device), asynchronous on `stream`."""
+        d = L.wr_render_desc(spp, max_path_len, seed, MODES[mode], L.WR_RENDER_NEE if nee else 0, spp_offset, 0)
+        self._check(self.lib.wr_render_device(self.h, sid, C.byref(d), C.c_void_p(d_sum), C.c_void_p(d_sumsq or None),
+                                              C.c_void_p(stream or None)))
+
+    def render_stats(self, sid: int, spp: int, max_path_len: int, seed: int = 1, mode: str = "megakernel",
+                     nee: bool = False):
+        """Per-pixel sum and sum of squares (H, W, 3) over spp samples, via torch device buffers."""
+        import torch
+
+        w, h = self._camera_size(sid)
+        s = torch.zeros((h, w, 3), dtype=torch.float32, device="cuda")
+        s2 = torch.zeros((h, w, 3), dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        self.render_device(sid, spp, max_path_len, s.data_ptr(), s2.data_ptr(), seed, mode, nee,
+                           stream=torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        return s.cpu().numpy().astype(np.float64), s2.cpu().numpy().astype(np.float64)
+
+    def profile_render(self, sid: int, spp: int, max_path_len: int, d_sum: int, seed: int = 1,
+                       nee: bool = False) -> dict:
+        """Wavefront render with per-stage CUDA-event timings and traversal work counts."""
+        d = L.wr_render_desc(spp, max_path_len, seed, 1, L.WR_RENDER_NEE if nee else 0, 0, 0)
+        p = L.wr_render_profile()
+        self._check(self.lib.wr_profile_render(self.h, sid, C.byref(d), C.c_void_p(d_sum), C.byref(p)))
+        return {k: getattr(p, k) for k, _ in L.wr_render_profile._fields_}
+
+    def set_wavefront_config(self, capacity: int, extend_block: int = 128, shade_block: int = 128,
+                             ctas_per_sm: int = 0, iters_per_graph: int = 4) -> None:
+        c = L.wr_wavefront_config(capacity, extend_block, shade_block, ctas_per_sm, iters_per_graph, 0.0)
+        self._check(self.lib.wr_set_wavefront_config(self.h, C.byref(c)))
+
+    def autotune(self, sid: int, spp_per_trial: int, max_path_len: int) -> dict:
+        c = L.wr_wavefront_config()
+        self._check(self.lib.wr_autotune(self.h, sid, spp_per_trial, max_path_len, C.byref(c)))
+        return {k: getattr(c, k) for k, _ in L.wr_wavefront_config._fields_}
+
+    def _camera_size(self, sid):
+        cam = self._cams.get(sid)
+        if cam is None:
+            raise KeyError(f"scene {sid} was not uploaded through this Context")
+        return cam
+
+
+MODES = {"megakernel": 0, "wavefront": 1}
+
+REQ_STATES = {0: "queued", 1: "running", 2: "done", 3: "cancelled", 4: "failed"}
+
+
+class Server:
+    """The serving loop of a Context (wr_serve_start ... wr_serve_stop):
+    requests admitted by film memory, their paths sharing the wavefront queues."""
+
+    def __init__(self, ctx: Context, film_bytes: int = 0, max_active: int = 0):
+        self.ctx = ctx
+        d = L.wr_serve_desc(film_bytes, max_active, 0)
+        ctx._check(ctx.lib.wr_serve_start(ctx.h, C.byref(d)))
+        self.sizes: dict[int, tuple[int, int]] = {}
+
+    def submit(self, sid: int, width: int, height: int, spp: int, max_path_len: int, seed: int = 1,
+               nee: bool = False) -> int:
+        r = L.wr_request_desc(sid, width, height, spp, max_path_len, L.WR_RENDER_NEE if nee else 0, seed)
+        rid = C.c_uint64()
+        self.ctx._check(self.ctx.lib.wr_submit(self.ctx.h, C.byref(r), C.byref(rid)))
+        self.sizes[rid.value] = (width, height)
+        return rid.value
+
+    def poll(self, rid: int) -> dict:
+        st = L.wr_req_status()
+        self.ctx._check(self.ctx.lib.wr_poll(self.ctx.h, rid, C.byref(st)))
+        return {"state": REQ_STATES[st.state], "paths_total": st.paths_total, "paths_done": st.paths_done,
+                "submit_s": st.submit_s, "admit_s": st.admit_s, "finish_s": st.finish_s}
+
+    def fetch(self, rid: int) -> np.ndarray:
+        w, h = self.sizes.pop(rid)
+        out = np.empty((h, w, 3), np.float32)
+        self.ctx._check(self.ctx.lib.wr_fetch(self.ctx.h, rid, L.ptr(out)))
+        return out
+
+    def cancel(self, rid: int) -> None:
+        self.ctx._check(self.ctx.lib.wr_cancel(self.ctx.h, rid))
+
+    def stop(self) -> None:
+        self.ctx._check(self.ctx.lib.wr_serve_stop(self.ctx.h))
+
+    def wait(self, rids, timeout: float = 600.0, poll_s: float = 0.002) -> dict:
+        import time
+
+        t0 = time.time()
+        left = set(rids)
+        status = {}
+        while left:
+            for r in list(left):
+                st = self.poll(r)
+                if st["state"] in ("done", "cancelled", "failed"):
+                    status[r] = st
+                    left.discard(r)
+            if left:
+                if time.time() - t0 > timeout:
+                    raise TimeoutError(f"{len(left)} requests unfinished")
+                time.sleep(poll_s)
+        return status
 
 
 def build_tree_host(verts: np.ndarray, tris: np.ndarray, threads: int = 0) -> dict:

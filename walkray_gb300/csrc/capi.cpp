@@ -90,6 +90,7 @@ int wr_ctx_destroy(wr_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     ctx->serving.reset();
+    ctx->wavefront.reset();
     ctx->scenes.clear();
     ctx->rays.release();
     ctx->hits.release();
@@ -102,6 +103,12 @@ int wr_ctx_destroy(wr_ctx* ctx) {
 }
 
 const char* wr_last_error(const wr_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int wr_kernel_launches(const wr_ctx* ctx, uint64_t* out) {
+    if (!ctx || !out) return WR_ERR_INVALID_ARGUMENT;
+    *out = ctx->kernel_launches;
+    return WR_OK;
+}
 
 int wr_scene_upload(wr_ctx* ctx, const wr_scene_desc* d, wr_scene_id* out) {
     if (!ctx || !d || !out) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "null argument");
@@ -200,8 +207,10 @@ int wr_scene_release(wr_ctx* ctx, wr_scene_id id) {
     if (!ctx) return WR_ERR_INVALID_ARGUMENT;
     auto it = ctx->scenes.find(id);
     if (it == ctx->scenes.end()) return set_error(ctx, WR_ERR_NOT_FOUND, "no such scene");
+    if (ctx->serving) return set_error(ctx, WR_ERR_BUSY, "scenes stay resident while the serving loop runs");
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    wf_forget_scene(ctx, static_cast<const RenderData*>(it->second->render_data.get()));
     ctx->scenes.erase(it);
     return WR_OK;
 }
@@ -232,6 +241,7 @@ int wr_trace_closest_device(wr_ctx* ctx, wr_scene_id id, const float* d_rays, ui
     WR_CUDA(ctx, cudaMemsetAsync(err, 0, sizeof(unsigned int), s));
     WR_CUDA(ctx, launch_trace_closest(sc->tree, d_rays, n, d_inside, d_contact, d_hits, counter, err, ctx->num_sms,
                                       ctx->trace_prune, s, &ctx->last_trace_blocks));
+    ctx->kernel_launches++;
     return WR_OK;
 }
 
@@ -265,6 +275,7 @@ int wr_trace_closest(wr_ctx* ctx, wr_scene_id id, const float* rays, uint64_t n,
     WR_CUDA(ctx, launch_trace_closest(sc->tree, ctx->rays.as<float>(), n, filtered ? ctx->inside.as<int32_t>() : nullptr,
                                       filtered ? ctx->contact.as<int32_t>() : nullptr, ctx->hits.as<wr_hit>(), counter,
                                       err, ctx->num_sms, ctx->trace_prune, s, &ctx->last_trace_blocks));
+    ctx->kernel_launches++;
     WR_CUDA(ctx, cudaMemcpyAsync(hits, ctx->hits.p, n * sizeof(wr_hit), cudaMemcpyDeviceToHost, s));
     unsigned int herr = 0;
     WR_CUDA(ctx, cudaMemcpyAsync(&herr, err, sizeof herr, cudaMemcpyDeviceToHost, s));

@@ -14,45 +14,45 @@ __global__ void __launch_bounds__(128) k_megakernel(RenderScene S, RenderParams 
     extern __shared__ uint32_t s_stack[];
     uint32_t* stack = s_stack + threadIdx.x;
     const int stride = blockDim.x;
-    const uint32_t npix = S.width * S.height;
+    const uint32_t npix = S.cam.width * S.cam.height;
     const uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x;
     if (pixel >= npix) return;
     f3 acc = mk(0, 0, 0), acc2 = mk(0, 0, 0);
     for (uint32_t s = P.s0; s < P.s1; s++) {
         PathRng g;
         g.init(P.seed, pixel, s);
-        PRay cur = camera_ray(S, pixel, g);
-        {
-            const RayQ q = make_rayq(cur.o, cur.d, S.tree.scene_mag);
-            set_hit(S, cur, trace_closest<false, false>(S.tree, q, -1, -1, stack, stride, P.stack_cap, err));
-        }
+        PRay cur = camera_ray(S.cam, pixel, g);
         InsideStack st;
         st.reset(cur.inside);
-        f3 color = mk(1, 1, 1), result = mk(0, 0, 0);
-        for (uint32_t depth = 0;; depth++) {
-            const int self = cur.inside >= 0 ? cur.inside : cur.iobj;
-            if (self < 0) break;  // escaped: terminateRay carries zero radiance
-            PRay next = scatter(S, self, cur, g, st);
-            if (length(next.d) < 0.5f) {
-                color = color * cos_term(S, cur);
-                color = vmul(color, radiance_decay(S, cur, length(next.o - cur.o)));
-                color = vmul(color, weight(cur));
-                result = vmul(color, weight(next));
+        f3 color = mk(1, 1, 1), result = mk(0, 0, 0), prev_d = mk(0, 0, 0);
+        uint32_t depth = 0;
+        bool filtered = false;  // the eye ray is traced without a condition (camera.cpp:52)
+        const bool nee = (P.flags & WR_RENDER_NEE) != 0;
+        bool nee_here = false;
+        for (;;) {
+            const RayQ q = make_rayq(cur.o, cur.d, S.tree.scene_mag);
+            const Hit h = filtered ? trace_closest<true, false>(S.tree, q, cur.inside, cur.contact, stack, stride,
+                                                                P.stack_cap, err)
+                                   : trace_closest<false, false>(S.tree, q, -1, -1, stack, stride, P.stack_cap, err);
+            if (h.slot < 0 && filtered) {  // a scattered ray that escapes ends with zero radiance
+                nee_here = nee;
                 break;
             }
-            if (depth + 1 > P.max_path_len) break;
-            st.set_top(next.inside);
-            const RayQ q = make_rayq(next.o, next.d, S.tree.scene_mag);
-            const Hit h = trace_closest<true, false>(S.tree, q, next.inside, next.contact, stack, stride, P.stack_cap, err);
-            if (h.slot < 0) break;
-            set_hit(S, next, h);
-            color = color * cos_term(S, cur);
-            color = vmul(color, radiance_decay(S, cur, length(next.o - cur.o)));
-            color = vmul(color, weight(cur));
-            cur = next;
+            set_hit(S, cur, h);
+            filtered = true;
+            if (path_advance(S, cur, color, prev_d, depth, st, g, P.max_path_len, nee, result, nee_here)) break;
+        }
+        if (nee_here) {  // the connection of the NEE branch, traced inline
+            ShadowReq sr;
+            if (nee_prepare(S, cur, prev_d, color, g, sr)) {
+                const RayQ q = make_rayq(sr.o, sr.d, S.tree.scene_mag);
+                const Hit h =
+                    trace_closest<true, false>(S.tree, q, sr.inside, sr.contact, stack, stride, P.stack_cap, err);
+                if (nee_visible(h, sr.dist)) result = sr.contrib;
+            }
         }
         if (!legal(result)) result = mk(0, 0, 0);
-        const f3 c = fix_vignetting(S, result, pixel);
+        const f3 c = fix_vignetting(S.cam, result, pixel);
         acc = acc + c;
         if (STATS) acc2 = acc2 + vmul(c, c);
     }
@@ -72,7 +72,7 @@ cudaError_t launch_megakernel(const RenderScene& S, const RenderParams& P, float
                               unsigned int* err, cudaStream_t stream) {
     const int block = 128;
     const size_t smem = (size_t)P.stack_cap * block * sizeof(uint32_t);
-    const uint32_t npix = S.width * S.height;
+    const uint32_t npix = S.cam.width * S.cam.height;
     const int grid = (int)((npix + block - 1) / block);
     auto kern = film2 ? k_megakernel<true> : k_megakernel<false>;
     if (smem > 48 * 1024) {

@@ -1,0 +1,760 @@
+// wavefront.cu — kernels and driver of the wavefront renderer (see
+// wavefront.h for the stage structure).
+#include <algorithm>
+#include <cstring>
+#include <map>
+
+#include "wavefront.h"
+
+namespace wr {
+
+constexpr uint32_t WF_MAX_JOBS = 256;
+constexpr uint32_t WF_MAX_SCENES = 64;
+constexpr int WF_TRACE_STEPS = 8;
+
+uint32_t wf_max_jobs() { return WF_MAX_JOBS; }
+
+// ---------------------------------------------------------------------------
+// state load / store
+// ---------------------------------------------------------------------------
+struct WfPath {
+    PRay cur;
+    f3 color, prev_d;
+    uint32_t depth;
+    InsideStack st;
+    uint32_t pixel, sample, dim;
+    int job;
+};
+
+__device__ __forceinline__ void wf_load(const WfSide& X, uint32_t i, WfPath& p) {
+    const float4 a0 = X.a0[i], a1 = X.a1[i], a2 = X.a2[i], a3 = X.a3[i];
+    const int4 ids = X.ids[i], misc = X.misc[i], stk = X.stk[i];
+    p.cur = ray_default();
+    p.cur.o = mk(a0.x, a0.y, a0.z);
+    p.cur.oP = a0.w;
+    p.cur.d = mk(a1.x, a1.y, a1.z);
+    p.cur.dP = a1.w;
+    p.cur.rad = mk(a2.x, a2.y, a2.z);
+    p.cur.cnorm = mk(a2.w, a3.w, __int_as_float(misc.w));
+    p.color = mk(a3.x, a3.y, a3.z);
+    p.cur.inside = ids.x;
+    p.cur.contact = ids.y;
+    p.job = ids.z;
+    p.pixel = (uint32_t)ids.w;
+    p.sample = (uint32_t)misc.x;
+    p.dim = (uint32_t)misc.y;
+    p.depth = (uint32_t)misc.z & 0xffffu;
+    p.st.n = (int)((uint32_t)misc.z >> 16);
+    p.st.v[0] = stk.x;
+    p.st.v[1] = stk.y;
+    p.st.v[2] = stk.z;
+    p.st.v[3] = stk.w;
+    const float4 a4 = X.a4[i];
+    p.prev_d = mk(a4.x, a4.y, a4.z);
+}
+
+__device__ __forceinline__ void wf_store(const WfSide& Y, uint32_t j, const WfPath& p) {
+    Y.a0[j] = make_float4(p.cur.o.x, p.cur.o.y, p.cur.o.z, p.cur.oP);
+    Y.a1[j] = make_float4(p.cur.d.x, p.cur.d.y, p.cur.d.z, p.cur.dP);
+    Y.a2[j] = make_float4(p.cur.rad.x, p.cur.rad.y, p.cur.rad.z, p.cur.cnorm.x);
+    Y.a3[j] = make_float4(p.color.x, p.color.y, p.color.z, p.cur.cnorm.y);
+    Y.ids[j] = make_int4(p.cur.inside, p.cur.contact, p.job, (int)p.pixel);
+    Y.misc[j] = make_int4((int)p.sample, (int)p.dim, (int)(p.depth | ((uint32_t)p.st.n << 16)),
+                          __float_as_int(p.cur.cnorm.z));
+    Y.stk[j] = make_int4(p.st.v[0], p.st.v[1], p.st.v[2], p.st.v[3]);
+    Y.a4[j] = make_float4(p.prev_d.x, p.prev_d.y, p.prev_d.z, 0.f);
+}
+
+// warp-aggregated append: returns this lane's position (valid if `want`)
+__device__ __forceinline__ uint32_t warp_append(unsigned int* counter, bool want, uint32_t offset) {
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned m = __ballot_sync(0xffffffffu, want);
+    uint32_t base = 0;
+    if (m) {
+        const int leader = __ffs(m) - 1;
+        if ((int)lane == leader) base = atomicAdd(counter, (unsigned)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, leader);
+    }
+    return offset + base + __popc(m & ((1u << lane) - 1u));
+}
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+__global__ void k_wf_reset(WfSide Y, unsigned long long* work, unsigned int* shadow_count) {
+    Y.counts[0] = 0;
+    Y.counts[1] = 0;
+    *work = 0;
+    *shadow_count = 0;
+}
+
+// film update of a finished path: isLegalColor, fixVignetting, FP32 atomics
+__device__ __forceinline__ void film_add(const WfJob& J, uint32_t pixel, f3 result) {
+    if (!legal(result)) result = mk(0, 0, 0);
+    const f3 c = fix_vignetting(J.cam, result, pixel);
+    float* f = J.film + 3 * (size_t)pixel;
+    atomicAdd(f + 0, c.x);
+    atomicAdd(f + 1, c.y);
+    atomicAdd(f + 2, c.z);
+    if (J.film2) {
+        float* f2 = J.film2 + 3 * (size_t)pixel;
+        atomicAdd(f2 + 0, c.x * c.x);
+        atomicAdd(f2 + 1, c.y * c.y);
+        atomicAdd(f2 + 2, c.z * c.z);
+    }
+}
+
+// shadow stage: visibility of every NEE connection, visible contributions to the film
+__global__ void __launch_bounds__(128) k_wf_shadow(const RenderScene* __restrict__ scenes,
+                                                     const WfJob* __restrict__ jobs, WfShadow Q, int stack_cap,
+                                                     unsigned int* __restrict__ err) {
+    extern __shared__ uint32_t s_stack[];
+    uint32_t* stack = s_stack + threadIdx.x;
+    const uint32_t n = *Q.count;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 o = Q.o[i], d = Q.d[i], c = Q.c[i];
+        const int4 ids = Q.ids[i];
+        const WfJob& J = jobs[ids.z];
+        const DevTree& T = scenes[J.scene].tree;
+        const RayQ q = make_rayq(mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), T.scene_mag);
+        const Hit h = trace_closest<true, false>(T, q, ids.x, ids.y, stack, blockDim.x, stack_cap, err);
+        if (nee_visible(h, o.w)) film_add(J, (uint32_t)ids.w, mk(c.x, c.y, c.z));
+    }
+}
+
+// extend: closest hit of every queued ray; the eye ray (contact == camera)
+// without a filter, all others with NoSelfCondition
+__global__ void __launch_bounds__(128) k_wf_extend(const RenderScene* __restrict__ scenes,
+                                                     const WfJob* __restrict__ jobs, WfSide X, int2* __restrict__ hits,
+                                                     unsigned long long* __restrict__ work, int stack_cap,
+                                                     unsigned int* __restrict__ err,
+                                                     unsigned long long* __restrict__ stats) {
+    extern __shared__ uint32_t s_stack[];
+    uint32_t* stack = s_stack + threadIdx.x;
+    const int stride = blockDim.x;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const uint64_t n = (uint64_t)X.counts[0] + X.counts[1];
+
+    bool active = false, exhausted = false;
+    uint64_t rid = 0;
+    RayQ q;
+    int in_obj = -1, ct_obj = -1;
+    bool filt = false;
+    DevTree T;
+    Hit h;
+    int sp = 0;
+    uint32_t n_box = 0, n_tri = 0;  // work counters (profiling launches only)
+    for (;;) {
+        const unsigned need = __ballot_sync(0xffffffffu, !active && !exhausted);
+        if (need) {
+            const int leader = __ffs(need) - 1;
+            unsigned long long base = 0;
+            if ((int)lane == leader) base = atomicAdd(work, (unsigned long long)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!active && !exhausted) {
+                const uint64_t id = base + __popc(need & lt_mask);
+                if (id < n) {
+                    rid = id;
+                    const float4 a0 = X.a0[id], a1 = X.a1[id];
+                    const int4 ids = X.ids[id];
+                    T = scenes[jobs[ids.z].scene].tree;
+                    q = make_rayq(mk(a0.x, a0.y, a0.z), mk(a1.x, a1.y, a1.z), T.scene_mag);
+                    in_obj = ids.x;
+                    ct_obj = ids.y;
+                    filt = ct_obj != CAMERA_OBJ;
+                    h.t = __int_as_float(0x7f800000);
+                    h.slot = -1;
+                    sp = 0;
+                    n_box = 1;
+                    n_tri = 0;
+                    float tn;
+                    if (box_pred(root_box(T), q, &tn)) {
+                        if (T.root_w1 & LEAF_FLAG) {
+                            n_tri += T.root_w1 & ~LEAF_FLAG;
+                            if (filt) leaf_test<true>(T, T.root_w0, T.root_w1 & ~LEAF_FLAG, q, in_obj, ct_obj, h);
+                            else leaf_test<false>(T, T.root_w0, T.root_w1 & ~LEAF_FLAG, q, in_obj, ct_obj, h);
+                        } else {
+                            stack[(sp++) * stride] = T.root_w0;
+                        }
+                    }
+                    active = true;
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (__all_sync(0xffffffffu, !active)) break;
+        if (active) {
+            for (int it = 0; it < WF_TRACE_STEPS && sp > 0; ++it) {
+                const uint32_t pi = stack[(--sp) * stride];
+                const NodePair* P = T.pairs + pi;
+                const float4 A = ldg4(&P->a), B = ldg4(&P->b), C = ldg4(&P->c);
+                const uint4 W = ldg4u(&P->t);
+                float tl, tr;
+                bool hl = box_pred(Box{A.x, A.y, A.z, A.w, B.x, B.y}, q, &tl);
+                bool hr = box_pred(Box{B.z, B.w, C.x, C.y, C.z, C.w}, q, &tr);
+                n_box += 2;
+                if (hl && (W.y & LEAF_FLAG)) {
+                    n_tri += W.y & ~LEAF_FLAG;
+                    if (filt) leaf_test<true>(T, W.x, W.y & ~LEAF_FLAG, q, in_obj, ct_obj, h);
+                    else leaf_test<false>(T, W.x, W.y & ~LEAF_FLAG, q, in_obj, ct_obj, h);
+                    hl = false;
+                }
+                if (hr && (W.w & LEAF_FLAG)) {
+                    n_tri += W.w & ~LEAF_FLAG;
+                    if (filt) leaf_test<true>(T, W.z, W.w & ~LEAF_FLAG, q, in_obj, ct_obj, h);
+                    else leaf_test<false>(T, W.z, W.w & ~LEAF_FLAG, q, in_obj, ct_obj, h);
+                    hr = false;
+                }
+                if (sp + 2 > stack_cap) {
+                    atomicOr(err, 1u);
+                    sp = 0;
+                    break;
+                }
+                if (hl && hr) {
+                    const bool lnear = tl <= tr;
+                    stack[(sp++) * stride] = lnear ? W.z : W.x;
+                    stack[(sp++) * stride] = lnear ? W.x : W.z;
+                } else if (hl) {
+                    stack[(sp++) * stride] = W.x;
+                } else if (hr) {
+                    stack[(sp++) * stride] = W.z;
+                }
+            }
+            if (sp == 0) {
+                hits[rid] = make_int2(h.slot, __float_as_int(h.t));
+                active = false;
+                if (stats) {
+                    atomicAdd(stats + 0, 1ull);
+                    atomicAdd(stats + 1, (unsigned long long)n_box);
+                    atomicAdd(stats + 2, (unsigned long long)n_tri);
+                }
+            }
+        }
+    }
+}
+
+// shade: one bounce per path; survivors compacted into Y, finished paths to the film
+__global__ void __launch_bounds__(128) k_wf_shade(const RenderScene* __restrict__ scenes,
+                                                    const WfJob* __restrict__ jobs,
+                                                    WfJobCounters* __restrict__ counters, WfSide X,
+                                                    const int2* __restrict__ hits, WfSide Y, WfShadow Q) {
+    const uint32_t n = X.counts[0] + X.counts[1];
+    const uint32_t step = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += step) {  // warp-uniform trip count
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < n;
+        WfPath p;
+        bool keep = false, done = false, shadow = false;
+        f3 result = mk(0, 0, 0);
+        ShadowReq sr;
+        if (valid) {
+            wf_load(X, i, p);
+            const WfJob& J = jobs[p.job];
+            const RenderScene& S = scenes[J.scene];
+            const int2 hv = hits[i];
+            Hit h;
+            h.slot = hv.x;
+            h.t = __int_as_float(hv.y);
+            const bool nee = (J.flags & WR_RENDER_NEE) != 0;
+            bool nee_here = false;
+            PathRng g;
+            g.init(J.seed, p.pixel, p.sample, p.dim);
+            if (h.slot < 0 && p.cur.contact != CAMERA_OBJ) {
+                done = true;  // a scattered ray that escapes ends with zero radiance
+                nee_here = nee;
+            } else {
+                set_hit(S, p.cur, h);
+                done = path_advance(S, p.cur, p.color, p.prev_d, p.depth, p.st, g, J.max_path_len, nee, result,
+                                    nee_here);
+            }
+            if (nee_here) shadow = nee_prepare(S, p.cur, p.prev_d, p.color, g, sr);
+            p.dim = g.dim;
+            keep = !done;
+            if (done && !shadow && (result.x != 0.f || result.y != 0.f || result.z != 0.f))
+                film_add(J, p.pixel, result);
+        }
+        // connections whose visibility the shadow stage decides
+        {
+            const uint32_t k = warp_append(Q.count, shadow, 0);
+            if (shadow) {
+                Q.o[k] = make_float4(sr.o.x, sr.o.y, sr.o.z, sr.dist);
+                Q.d[k] = make_float4(sr.d.x, sr.d.y, sr.d.z, 0.f);
+                Q.c[k] = make_float4(sr.contrib.x, sr.contrib.y, sr.contrib.z, 0.f);
+                Q.ids[k] = make_int4(sr.inside, sr.contact, p.job, (int)p.pixel);
+            }
+        }
+        // finished-path counts per job, aggregated over the lanes sharing a job
+        {
+            const unsigned dm = __ballot_sync(0xffffffffu, done);
+            if (done) {
+                const unsigned same = __match_any_sync(dm, p.job);
+                if ((threadIdx.x & 31u) == (unsigned)(__ffs(same) - 1))
+                    atomicAdd(&counters[p.job].finished, (unsigned long long)__popc(same));
+            }
+        }
+        const uint32_t j = warp_append(&Y.counts[0], keep, 0);
+        if (keep) wf_store(Y, j, p);
+    }
+}
+
+// generate: new camera paths into the free slots of Y, from the job slots
+// listed in `order` (admission order); the list lives in device memory so the
+// captured graph does not change when jobs come and go
+__global__ void __launch_bounds__(128) k_wf_generate(const WfJob* __restrict__ jobs, const int* __restrict__ order,
+                                                       WfJobCounters* __restrict__ counters, WfSide Y,
+                                                       uint32_t capacity) {
+    const int njobs = order[0];
+    const uint32_t survivors = Y.counts[0];
+    const uint32_t free_slots = capacity > survivors ? capacity - survivors : 0;
+    const uint32_t step = gridDim.x * blockDim.x;
+    const unsigned lane = threadIdx.x & 31u;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < free_slots; base += step) {
+        const bool want = base + threadIdx.x < free_slots;
+        bool have = false;
+        int jid = -1;
+        unsigned long long idx = 0;
+        unsigned need = __ballot_sync(0xffffffffu, want);
+        for (int k = 0; k < njobs && need; k++) {
+            const int j = order[1 + k];
+            const WfJob& J = jobs[j];
+            // one lane reads the claim counter so that the skip decision is warp-uniform
+            unsigned long long cl = 0;
+            if (lane == 0) cl = *(volatile unsigned long long*)&counters[j].claimed;
+            cl = __shfl_sync(0xffffffffu, cl, 0);
+            if (!J.active || cl >= J.total) continue;
+            const int leader = __ffs(need) - 1;
+            unsigned long long b = 0;
+            if ((int)lane == leader) b = atomicAdd(&counters[j].claimed, (unsigned long long)__popc(need));
+            b = __shfl_sync(0xffffffffu, b, leader);
+            if ((need >> lane) & 1u) {
+                const unsigned long long mine = b + __popc(need & ((1u << lane) - 1u));
+                if (mine < J.total) {
+                    have = true;
+                    jid = j;
+                    idx = mine;
+                }
+            }
+            need = __ballot_sync(0xffffffffu, want && !have);
+        }
+        if (!__any_sync(0xffffffffu, have)) break;  // every job fully handed out
+        WfPath p;
+        if (have) {
+            const WfJob& J = jobs[jid];
+            p.job = jid;
+            p.pixel = (uint32_t)(idx % J.npix);
+            p.sample = J.s0 + (uint32_t)(idx / J.npix);
+            PathRng g;
+            g.init(J.seed, p.pixel, p.sample);
+            p.cur = camera_ray(J.cam, p.pixel, g);
+            p.dim = g.dim;
+            p.color = mk(1, 1, 1);
+            p.prev_d = mk(0, 0, 0);
+            p.depth = 0;
+            p.st.reset(p.cur.inside);
+        }
+        const uint32_t j = warp_append(&Y.counts[1], have, survivors);
+        if (have) wf_store(Y, j, p);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// engine
+// ---------------------------------------------------------------------------
+struct WfEngine {
+    WfConfig cfg;
+    DeviceBuffer side_mem[2], hits, scenes, jobs, order, counters, work, err_word, shadow_mem;
+    WfSide side[2];
+    WfShadow shadow{};
+    int grid_shadow = 0;
+    size_t smem_shadow = 0;
+    std::vector<const RenderData*> scene_of;  // host mirror of the scene table
+    std::vector<RenderScene> scene_tab;
+    std::vector<WfJob> job_tab;               // host mirror of the job slots
+    std::vector<int> order_host;               // [n, slot...]
+    int stack_cap = 0;
+    int grid_extend = 0, grid_shade = 0, grid_gen = 0;
+    size_t smem_extend = 0;
+    cudaGraphExec_t graph = nullptr;
+    int graph_stack = -1;
+    WfJobCounters* host_counters = nullptr;  // pinned
+    ~WfEngine() {
+        if (graph) cudaGraphExecDestroy(graph);
+        if (host_counters) cudaFreeHost(host_counters);
+    }
+};
+
+const WfConfig& wf_config(const WfEngine* E) { return E->cfg; }
+
+static int alloc_side(wr_ctx* ctx, WfEngine* E, int k) {
+    const size_t Q = E->cfg.capacity;
+    const size_t bytes = Q * (5 * sizeof(float4) + 3 * sizeof(int4)) + 256;
+    WR_CUDA(ctx, E->side_mem[k].reserve(bytes));
+    char* p = E->side_mem[k].as<char>();
+    WfSide& S = E->side[k];
+    S.a0 = reinterpret_cast<float4*>(p);
+    S.a1 = S.a0 + Q;
+    S.a2 = S.a1 + Q;
+    S.a3 = S.a2 + Q;
+    S.ids = reinterpret_cast<int4*>(S.a3 + Q);
+    S.misc = S.ids + Q;
+    S.stk = S.misc + Q;
+    S.a4 = reinterpret_cast<float4*>(S.stk + Q);
+    S.counts = reinterpret_cast<unsigned int*>(S.a4 + Q);
+    WR_CUDA(ctx, cudaMemset(S.counts, 0, 2 * sizeof(unsigned int)));
+    return WR_OK;
+}
+
+int wf_engine_get(wr_ctx* ctx, const WfConfig& cfg, WfEngine** out) {
+    // one engine per context, rebuilt when the configuration changes
+    WfEngine* cur = static_cast<WfEngine*>(ctx->wavefront.get());
+    if (cur && cur->cfg.capacity == cfg.capacity && cur->cfg.extend_block == cfg.extend_block &&
+        cur->cfg.shade_block == cfg.shade_block && cur->cfg.ctas_per_sm == cfg.ctas_per_sm &&
+        cur->cfg.iters_per_graph == cfg.iters_per_graph) {
+        *out = cur;
+        return WR_OK;
+    }
+    if (cur) {
+        WR_CUDA(ctx, cudaDeviceSynchronize());
+        ctx->wavefront.reset();
+    }
+    auto E = std::make_shared<WfEngine>();
+    E->cfg = cfg;
+    for (int k = 0; k < 2; k++) {
+        int rc = alloc_side(ctx, E.get(), k);
+        if (rc != WR_OK) return rc;
+    }
+    WR_CUDA(ctx, E->hits.reserve(sizeof(int2) * (size_t)cfg.capacity));
+    {
+        const size_t Q = cfg.capacity;
+        WR_CUDA(ctx, E->shadow_mem.reserve(Q * (3 * sizeof(float4) + sizeof(int4)) + 256));
+        char* p = E->shadow_mem.as<char>();
+        E->shadow.o = reinterpret_cast<float4*>(p);
+        E->shadow.d = E->shadow.o + Q;
+        E->shadow.c = E->shadow.d + Q;
+        E->shadow.ids = reinterpret_cast<int4*>(E->shadow.c + Q);
+        E->shadow.count = reinterpret_cast<unsigned int*>(E->shadow.ids + Q);
+        WR_CUDA(ctx, cudaMemset(E->shadow.count, 0, sizeof(unsigned int)));
+    }
+    WR_CUDA(ctx, E->scenes.reserve(sizeof(RenderScene) * WF_MAX_SCENES));
+    WR_CUDA(ctx, E->jobs.reserve(sizeof(WfJob) * WF_MAX_JOBS));
+    WR_CUDA(ctx, cudaMemset(E->jobs.p, 0, sizeof(WfJob) * WF_MAX_JOBS));
+    WR_CUDA(ctx, E->order.reserve(sizeof(int) * (WF_MAX_JOBS + 1)));
+    WR_CUDA(ctx, cudaMemset(E->order.p, 0, sizeof(int) * (WF_MAX_JOBS + 1)));
+    WR_CUDA(ctx, E->counters.reserve(sizeof(WfJobCounters) * WF_MAX_JOBS));
+    WR_CUDA(ctx, cudaMemset(E->counters.p, 0, sizeof(WfJobCounters) * WF_MAX_JOBS));
+    WR_CUDA(ctx, E->work.reserve(sizeof(unsigned long long)));
+    WR_CUDA(ctx, E->err_word.reserve(sizeof(unsigned int)));
+    WR_CUDA(ctx, cudaMemset(E->err_word.p, 0, sizeof(unsigned int)));
+    WR_CUDA(ctx, cudaMallocHost(&E->host_counters, sizeof(WfJobCounters) * WF_MAX_JOBS));
+    E->job_tab.assign(WF_MAX_JOBS, WfJob{});
+    E->order_host.assign(1, 0);
+    // persistent grids from the occupancy calculator
+    int per_sm = 0;
+    WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_shade, cfg.shade_block, 0));
+    if (cfg.ctas_per_sm > 0) per_sm = std::min(per_sm, cfg.ctas_per_sm);
+    E->grid_shade = ctx->num_sms * std::max(1, per_sm);
+    WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_generate, cfg.shade_block, 0));
+    E->grid_gen = ctx->num_sms * std::max(1, per_sm);
+    *out = E.get();
+    ctx->wavefront = E;
+    return WR_OK;
+}
+
+int wf_set_config(wr_ctx* ctx, const WfConfig& cfg) {
+    WfEngine* E = nullptr;
+    return wf_engine_get(ctx, cfg, &E);
+}
+
+// slot of a scene in the device scene table (nullptr entries are free)
+static int scene_slot(wr_ctx* ctx, WfEngine* E, const RenderData* rd, int* slot) {
+    for (size_t k = 0; k < E->scene_of.size(); k++)
+        if (E->scene_of[k] == rd) {
+            *slot = (int)k;
+            return WR_OK;
+        }
+    for (size_t k = 0; k < E->scene_of.size(); k++)
+        if (!E->scene_of[k]) {
+            E->scene_of[k] = rd;
+            *slot = (int)k;
+            return WR_OK;
+        }
+    if (E->scene_of.size() >= WF_MAX_SCENES) return set_error(ctx, WR_ERR_BUSY, "too many scenes in flight");
+    E->scene_of.push_back(rd);
+    *slot = (int)E->scene_of.size() - 1;
+    return WR_OK;
+}
+
+// a released scene must not stay in the table: a later scene could be
+// allocated at the same host address and match the stale device entry
+void wf_forget_scene(wr_ctx* ctx, const RenderData* rd) {
+    WfEngine* E = static_cast<WfEngine*>(ctx->wavefront.get());
+    if (!E || !rd) return;
+    for (auto& p : E->scene_of)
+        if (p == rd) p = nullptr;
+}
+
+int wf_update_jobs(wr_ctx* ctx, WfEngine* E, const std::vector<WfSlotUpdate>& updates, const std::vector<int>& order,
+                   cudaStream_t s) {
+    if (order.size() > WF_MAX_JOBS) return set_error(ctx, WR_ERR_BUSY, "too many jobs in flight");
+    bool scenes_changed = false;
+    for (const WfSlotUpdate& u : updates) {
+        if (u.slot < 0 || u.slot >= (int)WF_MAX_JOBS) return set_error(ctx, WR_ERR_INTERNAL, "bad job slot");
+        WfJob j = u.jh.job;
+        if (u.jh.rd) {
+            int rc = scene_slot(ctx, E, u.jh.rd, &j.scene);
+            if (rc != WR_OK) return rc;
+            scenes_changed = true;  // (re)copy the entry: its RenderData may be new at a reused address
+        } else {
+            j.scene = E->job_tab[u.slot].scene;
+        }
+        E->job_tab[u.slot] = j;
+        WR_CUDA(ctx, cudaMemcpyAsync(E->jobs.as<WfJob>() + u.slot, &E->job_tab[u.slot], sizeof(WfJob),
+                                     cudaMemcpyHostToDevice, s));
+        if (u.reset_counters)
+            WR_CUDA(ctx, cudaMemsetAsync(E->counters.as<WfJobCounters>() + u.slot, 0, sizeof(WfJobCounters), s));
+    }
+    if (scenes_changed) {
+        E->scene_tab.resize(E->scene_of.size());
+        int cap = 8;
+        for (size_t k = 0; k < E->scene_of.size(); k++) {
+            if (!E->scene_of[k]) {
+                std::memset(&E->scene_tab[k], 0, sizeof(RenderScene));
+                continue;
+            }
+            E->scene_tab[k] = RenderDataView::scene(E->scene_of[k]);
+            cap = std::max(cap, (int)E->scene_tab[k].tree.max_depth + 3);
+        }
+        WR_CUDA(ctx, cudaMemcpyAsync(E->scenes.p, E->scene_tab.data(), sizeof(RenderScene) * E->scene_tab.size(),
+                                     cudaMemcpyHostToDevice, s));
+        if (cap > E->stack_cap) {
+            E->stack_cap = cap;
+            E->smem_extend = (size_t)cap * E->cfg.extend_block * sizeof(uint32_t);
+            if (E->smem_extend > 200 * 1024) return set_error(ctx, WR_ERR_UNSUPPORTED, "tree too deep for the stack");
+            if (E->smem_extend > 48 * 1024)
+                WR_CUDA(ctx, cudaFuncSetAttribute(k_wf_extend, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  (int)E->smem_extend));
+            int per_sm = 0;
+            WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_extend, E->cfg.extend_block,
+                                                                       E->smem_extend));
+            if (E->cfg.ctas_per_sm > 0) per_sm = std::min(per_sm, E->cfg.ctas_per_sm);
+            E->grid_extend = ctx->num_sms * std::max(1, per_sm);
+            E->smem_shadow = E->smem_extend;
+            if (E->smem_shadow > 48 * 1024)
+                WR_CUDA(ctx, cudaFuncSetAttribute(k_wf_shadow, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  (int)E->smem_shadow));
+            WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_shadow, E->cfg.extend_block,
+                                                                       E->smem_shadow));
+            E->grid_shadow = ctx->num_sms * std::max(1, per_sm);
+        }
+    }
+    E->order_host.assign(1, (int)order.size());
+    E->order_host.insert(E->order_host.end(), order.begin(), order.end());
+    WR_CUDA(ctx, cudaMemcpyAsync(E->order.p, E->order_host.data(), sizeof(int) * E->order_host.size(),
+                                 cudaMemcpyHostToDevice, s));
+    // the host mirrors must stay alive until the copies ran
+    WR_CUDA(ctx, cudaStreamSynchronize(s));
+    return WR_OK;
+}
+
+// one bounce iteration; `ev` (5 events, profiling only) brackets the stages
+static void enqueue_iteration(WfEngine* E, int x, cudaStream_t s, cudaEvent_t* ev = nullptr,
+                              unsigned long long* stats = nullptr) {
+    const int y = 1 - x;
+    const RenderScene* scenes = E->scenes.as<RenderScene>();
+    const WfJob* jobs = E->jobs.as<WfJob>();
+    WfJobCounters* cnt = E->counters.as<WfJobCounters>();
+    k_wf_reset<<<1, 1, 0, s>>>(E->side[y], E->work.as<unsigned long long>(), E->shadow.count);
+    if (ev) cudaEventRecord(ev[0], s);
+    k_wf_extend<<<E->grid_extend, E->cfg.extend_block, E->smem_extend, s>>>(
+        scenes, jobs, E->side[x], E->hits.as<int2>(), E->work.as<unsigned long long>(), E->stack_cap,
+        E->err_word.as<unsigned int>(), stats);
+    if (ev) cudaEventRecord(ev[1], s);
+    k_wf_shade<<<E->grid_shade, E->cfg.shade_block, 0, s>>>(scenes, jobs, cnt, E->side[x], E->hits.as<int2>(),
+                                                            E->side[y], E->shadow);
+    if (ev) cudaEventRecord(ev[2], s);
+    k_wf_shadow<<<E->grid_shadow, E->cfg.extend_block, E->smem_shadow, s>>>(scenes, jobs, E->shadow, E->stack_cap,
+                                                                           E->err_word.as<unsigned int>());
+    if (ev) cudaEventRecord(ev[3], s);
+    k_wf_generate<<<E->grid_gen, E->cfg.shade_block, 0, s>>>(jobs, E->order.as<int>(), cnt, E->side[y],
+                                                             E->cfg.capacity);
+    if (ev) cudaEventRecord(ev[4], s);
+}
+
+// wr_profile_render: the render of render_wavefront with eager launches
+int profile_wavefront(wr_ctx* ctx, RenderData& rd, const RenderParams& P, uint32_t spp_offset, uint32_t spp,
+                      float* film, wr_render_profile* out) {
+    if (ctx->serving) return set_error(ctx, WR_ERR_BUSY, "the serving loop owns the wavefront queues");
+    WfEngine* E = nullptr;
+    int rc = wf_engine_get(ctx, wf_tuned_config(ctx), &E);
+    if (rc != WR_OK) return rc;
+    cudaStream_t s = ctx->stream;
+    const RenderScene& S = RenderDataView::scene(&rd);
+    WfSlotUpdate u;
+    u.slot = 0;
+    u.jh.rd = &rd;
+    u.jh.job = make_job(S, S.cam, P.seed, spp_offset, spp, P.max_path_len, P.flags, film, nullptr);
+    u.reset_counters = true;
+    if ((rc = wf_update_jobs(ctx, E, {u}, {0}, s)) != WR_OK) return rc;
+    if ((rc = wf_reset_queues(ctx, E, s)) != WR_OK) return rc;
+    DeviceBuffer st;
+    WR_CUDA(ctx, st.reserve(4 * sizeof(unsigned long long)));
+    WR_CUDA(ctx, cudaMemsetAsync(st.p, 0, 4 * sizeof(unsigned long long), s));
+    cudaEvent_t ev[5], t0, t1;
+    for (auto& e : ev) WR_CUDA(ctx, cudaEventCreate(&e));
+    WR_CUDA(ctx, cudaEventCreate(&t0));
+    WR_CUDA(ctx, cudaEventCreate(&t1));
+    std::memset(out, 0, sizeof *out);
+    std::vector<WfJobCounters> c;
+    const unsigned long long total = u.jh.job.total;
+    cudaEventRecord(t0, s);
+    int x = 0;
+    for (uint64_t it = 0;; it++) {
+        enqueue_iteration(E, x, s, ev, st.as<unsigned long long>());
+        ctx->kernel_launches += 5;
+        x = 1 - x;
+        WR_CUDA(ctx, cudaEventSynchronize(ev[4]));
+        float a = 0, b = 0, cc = 0, d = 0;
+        cudaEventElapsedTime(&a, ev[0], ev[1]);
+        cudaEventElapsedTime(&b, ev[1], ev[2]);
+        cudaEventElapsedTime(&cc, ev[2], ev[3]);
+        cudaEventElapsedTime(&d, ev[3], ev[4]);
+        out->ms_extend += a;
+        out->ms_shade += b;
+        out->ms_shadow += cc;
+        out->ms_generate += d;
+        out->iterations++;
+        if ((rc = wf_read_counters(ctx, E, c, s)) != WR_OK) break;
+        if (c[0].finished >= total) break;
+        if (it > 100000) {
+            rc = set_error(ctx, WR_ERR_TIMEOUT, "wavefront did not drain");
+            break;
+        }
+    }
+    cudaEventRecord(t1, s);
+    cudaEventSynchronize(t1);
+    float tot = 0;
+    cudaEventElapsedTime(&tot, t0, t1);
+    out->ms_total = tot;
+    unsigned long long h[4] = {0, 0, 0, 0};
+    cudaMemcpy(h, st.p, sizeof h, cudaMemcpyDeviceToHost);
+    out->rays = h[0];
+    out->box_tests = h[1];
+    out->tri_tests = h[2];
+    out->paths = total;
+    for (auto& e : ev) cudaEventDestroy(e);
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    u.jh.job.active = 0;
+    u.reset_counters = false;
+    if (rc == WR_OK) rc = wf_update_jobs(ctx, E, {u}, {}, s);
+    return rc;
+}
+
+int wf_launch(wr_ctx* ctx, WfEngine* E, cudaStream_t s) {
+    if (E->stack_cap == 0) return set_error(ctx, WR_ERR_INTERNAL, "wavefront launched without a scene");
+    if (!E->graph || E->graph_stack != E->stack_cap) {
+        if (E->graph) {
+            cudaGraphExecDestroy(E->graph);
+            E->graph = nullptr;
+        }
+        cudaStream_t cap;
+        WR_CUDA(ctx, cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            for (int it = 0; it < E->cfg.iters_per_graph; it++) {
+                enqueue_iteration(E, 0, cap);
+                enqueue_iteration(E, 1, cap);
+            }
+            e = cudaStreamEndCapture(cap, &g);
+        }
+        cudaStreamDestroy(cap);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "capturing the bounce loop");
+        e = cudaGraphInstantiate(&E->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "instantiating the bounce loop");
+        E->graph_stack = E->stack_cap;
+    }
+    WR_CUDA(ctx, cudaGraphLaunch(E->graph, s));
+    ctx->kernel_launches += 5ull * 2 * E->cfg.iters_per_graph;  // reset, extend, shade, shadow, generate per iteration
+    return WR_OK;
+}
+
+int wf_read_counters(wr_ctx* ctx, WfEngine* E, std::vector<WfJobCounters>& out, cudaStream_t s) {
+    out.resize(WF_MAX_JOBS);
+    WR_CUDA(ctx, cudaMemcpyAsync(E->host_counters, E->counters.p, sizeof(WfJobCounters) * WF_MAX_JOBS,
+                                 cudaMemcpyDeviceToHost, s));
+    WR_CUDA(ctx, cudaStreamSynchronize(s));
+    std::memcpy(out.data(), E->host_counters, sizeof(WfJobCounters) * WF_MAX_JOBS);
+    return WR_OK;
+}
+
+int wf_error_word(wr_ctx* ctx, WfEngine* E, unsigned int* herr, cudaStream_t s) {
+    WR_CUDA(ctx, cudaMemcpyAsync(herr, E->err_word.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
+    WR_CUDA(ctx, cudaStreamSynchronize(s));
+    return WR_OK;
+}
+
+int wf_reset_queues(wr_ctx* ctx, WfEngine* E, cudaStream_t s) {
+    for (int k = 0; k < 2; k++) WR_CUDA(ctx, cudaMemsetAsync(E->side[k].counts, 0, 2 * sizeof(unsigned int), s));
+    return WR_OK;
+}
+
+WfJob make_job(const RenderScene& S, const CamParams& cam, uint64_t seed, uint32_t s0, uint32_t spp,
+               uint32_t max_path_len, uint32_t flags, float* film, float* film2) {
+    WfJob j;
+    std::memset(&j, 0, sizeof j);
+    (void)S;
+    j.active = 1;
+    j.cam = cam;
+    j.seed = seed;
+    j.s0 = s0;
+    j.spp = spp;
+    j.max_path_len = max_path_len;
+    j.flags = flags;
+    j.npix = cam.width * cam.height;
+    j.total = (unsigned long long)j.npix * spp;
+    j.film = film;
+    j.film2 = film2;
+    return j;
+}
+
+int render_wavefront(wr_ctx* ctx, RenderData& rd, const RenderParams& P, uint32_t spp_offset, uint32_t spp,
+                     float* film, float* film2, cudaStream_t s) {
+    if (ctx->serving) return set_error(ctx, WR_ERR_BUSY, "the serving loop owns the wavefront queues");
+    WfEngine* E = nullptr;
+    int rc = wf_engine_get(ctx, wf_tuned_config(ctx), &E);
+    if (rc != WR_OK) return rc;
+    const RenderScene& S = RenderDataView::scene(&rd);
+    WfSlotUpdate u;
+    u.slot = 0;
+    u.jh.rd = &rd;
+    u.jh.job = make_job(S, S.cam, P.seed, spp_offset, spp, P.max_path_len, P.flags, film, film2);
+    u.reset_counters = true;
+    rc = wf_update_jobs(ctx, E, {u}, {0}, s);
+    if (rc != WR_OK) return rc;
+    if ((rc = wf_reset_queues(ctx, E, s)) != WR_OK) return rc;
+    // replay the captured bounce loop until every path of the job has reached the film
+    std::vector<WfJobCounters> c;
+    const unsigned long long total = u.jh.job.total;
+    const uint64_t max_launches =
+        1 + (total / std::max<uint32_t>(1, E->cfg.capacity) + 4) * (uint64_t)(P.max_path_len + 4) * 4;
+    for (uint64_t l = 0;; l++) {
+        if ((rc = wf_launch(ctx, E, s)) != WR_OK) return rc;
+        if ((rc = wf_read_counters(ctx, E, c, s)) != WR_OK) return rc;
+        if (c[0].finished >= total) break;
+        if (l > max_launches) return set_error(ctx, WR_ERR_TIMEOUT, "wavefront did not drain");
+    }
+    // retire the job so a later render starts from an empty table
+    u.jh.job.active = 0;
+    u.reset_counters = false;
+    if ((rc = wf_update_jobs(ctx, E, {u}, {}, s)) != WR_OK) return rc;
+    unsigned int herr = 0;
+    if ((rc = wf_error_word(ctx, E, &herr, s)) != WR_OK) return rc;
+    if (herr) return set_error(ctx, WR_ERR_INTERNAL, "traversal stack overflow");
+    return WR_OK;
+}
+
+}  // namespace wr

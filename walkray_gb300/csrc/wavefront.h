@@ -1,0 +1,115 @@
+// wavefront.h — the batched form of the renderer: path state in HBM, one
+// kernel per stage, several renders (jobs) sharing the same queues.
+//
+//   extend    persistent warps trace every queued ray (closest hit, the same
+//             bit-exact traversal as k_trace_closest)
+//   shade     one bounce of the reference loop per path (scatter, throughput,
+//             termination); survivors are compacted into the other state
+//             buffer with warp-aggregated appends, finished paths go to their
+//             job's film
+//   generate  refills free queue slots with camera paths of the jobs in
+//             table order (continuous batching)
+//
+// The [reset, extend, shade, generate] x 2 sequence (one per ping-pong side)
+// is captured once into a CUDA graph and replayed until every job is done;
+// kernel sizes never depend on host-side counts.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <vector>
+
+#include "render_launch.h"
+#include "wr_context.h"
+
+namespace wr {
+
+struct RenderData;
+struct RenderDataView {  // what the engine needs from RenderData (render_api.cu)
+    static const RenderScene& scene(const RenderData* rd);
+};
+
+struct WfJob {
+    int scene;  // index into the engine's scene table
+    int active;
+    CamParams cam;
+    uint64_t seed;
+    uint32_t s0, spp, max_path_len, flags;
+    uint32_t npix;
+    unsigned long long total;  // npix * spp paths
+    float* film;
+    float* film2;
+};
+
+struct WfJobCounters {
+    unsigned long long claimed;   // paths handed to the queues
+    unsigned long long finished;  // paths whose colour reached the film
+};
+
+// structure-of-arrays path state, one ping-pong side
+struct WfSide {
+    float4* a0;  // o.xyz, oP
+    float4* a1;  // d.xyz, dP
+    float4* a2;  // rad.xyz, cnorm.x
+    float4* a3;  // color.xyz, cnorm.y
+    int4* ids;   // inside, contact, job, pixel
+    int4* misc;  // sample, rng dim, depth | stack_n << 16, cnorm.z bits
+    int4* stk;   // inside stack
+    float4* a4;  // direction of the ray before the current one (next-event estimation)
+    unsigned int* counts;  // [0] survivors written by shade, [1] paths appended by generate
+};
+
+// shadow rays of next-event estimation, written by shade, traced by k_wf_shadow
+struct WfShadow {
+    float4* o;    // origin, distance to the light sample
+    float4* d;    // direction
+    float4* c;    // contribution if visible
+    int4* ids;    // inside, contact, job, pixel
+    unsigned int* count;
+};
+
+struct WfConfig {
+    uint32_t capacity = 1u << 21;  // paths in flight
+    int extend_block = 128;
+    int shade_block = 128;
+    int ctas_per_sm = 0;           // 0 = occupancy calculator
+    int iters_per_graph = 4;       // ping-pong pairs per graph launch
+};
+
+struct WfEngine;
+
+// Device tables of the jobs in flight (up to max_jobs) and of the scenes
+// they reference.
+int wf_engine_get(wr_ctx* ctx, const WfConfig& cfg, WfEngine** out);
+uint32_t wf_max_jobs();
+
+// Renders spp samples of one scene through the wavefront (wr_render_device).
+int render_wavefront(wr_ctx* ctx, RenderData& rd, const RenderParams& P, uint32_t spp_offset, uint32_t spp,
+                     float* film, float* film2, cudaStream_t stream);
+
+// Lower-level interface used by the serving loop.  Jobs live in fixed slots
+// (in-flight paths carry their slot), generated in the order of `order`.
+struct WfJobHost {
+    WfJob job;
+    const RenderData* rd = nullptr;  // scene of the job (nullptr: keep the slot's scene)
+};
+struct WfSlotUpdate {
+    int slot = 0;
+    WfJobHost jh;
+    bool reset_counters = false;
+};
+int wf_update_jobs(wr_ctx* ctx, WfEngine* E, const std::vector<WfSlotUpdate>& updates, const std::vector<int>& order,
+                   cudaStream_t s);
+int wf_launch(wr_ctx* ctx, WfEngine* E, cudaStream_t s);  // one graph replay
+int wf_read_counters(wr_ctx* ctx, WfEngine* E, std::vector<WfJobCounters>& out, cudaStream_t s);
+int wf_error_word(wr_ctx* ctx, WfEngine* E, unsigned int* herr, cudaStream_t s);
+int wf_reset_queues(wr_ctx* ctx, WfEngine* E, cudaStream_t s);
+const WfConfig& wf_config(const WfEngine* E);
+int wf_set_config(wr_ctx* ctx, const WfConfig& cfg);
+WfConfig wf_tuned_config(wr_ctx* ctx);
+WfJob make_job(const RenderScene& S, const CamParams& cam, uint64_t seed, uint32_t s0, uint32_t spp,
+               uint32_t max_path_len, uint32_t flags, float* film, float* film2);
+CamParams camera_params_for(const RenderData* rd, uint32_t width, uint32_t height);
+
+}  // namespace wr

@@ -75,10 +75,18 @@ struct wr_ctx {
     wr::DeviceBuffer scratch_words;  // counters / error flags
     bool trace_prune = false;
     int last_trace_blocks = 0;
-    std::shared_ptr<void> serving;  // serving loop state (serve.cpp)
+    uint64_t kernel_launches = 0;  // kernels this library has launched on the context
+    std::shared_ptr<void> serving;    // serving loop state (serve.cpp)
+    std::shared_ptr<void> wavefront;  // wavefront engine (wavefront.cu)
+    // wavefront configuration chosen by wr_autotune (0 = defaults)
+    uint32_t wf_capacity = 0;
+    int wf_extend_block = 0, wf_shade_block = 0, wf_ctas_per_sm = 0, wf_iters = 0;
 };
 
 namespace wr {
+struct RenderData;
+// drops a scene from the wavefront engine's scene table (wavefront.cu)
+void wf_forget_scene(wr_ctx* ctx, const RenderData* rd);
 int set_error(wr_ctx* ctx, int code, const std::string& msg);
 int cuda_error(wr_ctx* ctx, cudaError_t e, const char* what);
 SceneGPU* find_scene(wr_ctx* ctx, wr_scene_id id);

@@ -36,16 +36,21 @@ struct GridDev {
     const float* data;
 };
 
+// camera of one render (Camera::setup / generateRay, camera.cpp:6-60); the
+// image plane distance is in pixels, so it scales with the resolution
+struct CamParams {
+    f3 pos, focus, front, right, top;
+    uint32_t width, height;
+    float ipd, lens_radius, focal_dist;
+    int inside;  // inside object of camera rays
+};
+
 struct RenderScene {
     DevTree tree;
     const wr_object_desc* objs;
     uint32_t num_objs;
     const uint32_t* tri_slot;  // global triangle id -> slot
-    // camera (Camera::setup / generateRay, camera.cpp:6-60)
-    f3 cam_pos, cam_focus, front, right, top;
-    uint32_t width, height;
-    float ipd, lens_radius, focal_dist;
-    int camera_inside;
+    CamParams cam;             // the scene's own camera
     // lights (SurfaceSampler, surfaceSampler.cpp:7-23)
     uint32_t nlights;
     const int* light_obj;
@@ -372,7 +377,7 @@ __device__ __forceinline__ void set_contact(const RenderScene& S, PRay& out, int
     (void)tri;
 }
 
-__device__ PRay scatter(const RenderScene& S, int self, const PRay& in, PathRng& g, InsideStack& st);
+static __device__ PRay scatter(const RenderScene& S, int self, const PRay& in, PathRng& g, InsideStack& st);
 
 // Diffuse / Glossy / AnisotropicGlossy (diffuseObj.h:34-57, glossyObj.h:39-62, anisotropicGlossyObj.h:54-68)
 __device__ __forceinline__ PRay scatter_surface(const RenderScene& S, int self, const PRay& in, PathRng& g) {
@@ -631,7 +636,8 @@ __device__ __forceinline__ PRay scatter_heterogeneous(const RenderScene& S, int 
 
 // one scatter() call, following delegations (RefractiveObject handing a hit
 // inside it to the hit object; media handing over to the surface hit)
-__device__ __noinline__ PRay scatter(const RenderScene& S, int self, const PRay& in, PathRng& g, InsideStack& st) {
+static __device__ __noinline__ PRay scatter(const RenderScene& S, int self, const PRay& in, PathRng& g,
+                                            InsideStack& st) {
     PRay cur = in;
     float oP_scale = 1.f;
     for (int hop = 0; hop < 4; hop++) {
@@ -689,13 +695,13 @@ __device__ __forceinline__ f3 radiance_decay(const RenderScene& S, const PRay& r
 __device__ __forceinline__ f3 weight(const PRay& r) { return divs(divs(r.rad, r.oP), r.dP); }
 
 // Camera::generateRay (camera.cpp:6-60), draws 0 and 1 (+2, 3 for the lens)
-__device__ __forceinline__ PRay camera_ray(const RenderScene& S, uint32_t pixel, PathRng& g) {
+__device__ __forceinline__ PRay camera_ray(const CamParams& S, uint32_t pixel, PathRng& g) {
     PRay r = ray_default();
     const uint32_t x = pixel % S.width, y = pixel / S.width;
     const float u = g.next(), v = g.next();
     r.d = normalize((S.front * S.ipd + S.right * (((float)x + u) - ((float)S.width / 2.f))) +
                     S.top * ((((float)S.height / 2.f) - (float)y) - v));
-    r.o = S.cam_pos;
+    r.o = S.pos;
     if (S.lens_radius > 0.f) {  // thin lens (camera.cpp:30-47, concentricSampleDisk :207-249)
         const float a = g.next(), b = g.next();
         const float sx = 2.f * a - 1.f, sy = 2.f * b - 1.f;
@@ -727,12 +733,12 @@ __device__ __forceinline__ PRay camera_ray(const RenderScene& S, uint32_t pixel,
         lv *= S.lens_radius;
         const float ft = S.focal_dist / fabsf(dot(S.front, r.d));
         const f3 pf = r.o + r.d * ft;
-        r.o = (S.cam_pos + S.right * lu) + S.top * lv;
+        r.o = (S.pos + S.right * lu) + S.top * lv;
         r.d = normalize(pf - r.o);
     }
     r.contact = CAMERA_OBJ;
-    r.cnorm = normalize(S.cam_focus - r.o);
-    r.inside = S.camera_inside;
+    r.cnorm = normalize(S.focus - r.o);
+    r.inside = S.inside;
     return r;
 }
 
@@ -740,7 +746,7 @@ __device__ __forceinline__ PRay camera_ray(const RenderScene& S, uint32_t pixel,
 __device__ __forceinline__ bool legal(f3 c) {
     return isfinite(c.x) && isfinite(c.y) && isfinite(c.z) && c.x >= 0.f && c.y >= 0.f && c.z >= 0.f;
 }
-__device__ __forceinline__ f3 fix_vignetting(const RenderScene& S, f3 color, uint32_t pixel) {
+__device__ __forceinline__ f3 fix_vignetting(const CamParams& S, f3 color, uint32_t pixel) {
     const uint32_t x = pixel % S.width, y = pixel / S.width;
     const f3 dir = normalize((S.front * S.ipd + S.right * ((float)x + 0.5f - S.width / 2.f)) +
                              S.top * (S.height / 2.f - 0.5f - (float)y));
@@ -748,6 +754,212 @@ __device__ __forceinline__ f3 fix_vignetting(const RenderScene& S, f3 color, uin
     if (c == 0.f) return mk(0, 0, 0);
     const f3 r = divs(color, fabsf(c));
     return legal(r) ? r : mk(0, 0, 0);
+}
+
+// ---------------------------------------------------------------------------
+// next-event estimation (PathTracer::renderPixels NEE branch, pathTracer.cpp:39-66)
+// ---------------------------------------------------------------------------
+struct ShadowReq {
+    f3 o, d;        // from the path vertex towards the light sample
+    float dist;     // |light.o - o| (visibility: hit beyond dist - EPSILON)
+    f3 contrib;     // colour the path adds if the light is visible
+    int inside, contact;
+};
+
+__device__ __forceinline__ uint32_t lower_bound_dev(const float* a, uint32_t lo, uint32_t n, float x) {
+    uint32_t l = 0, h = n;
+    while (l < h) {
+        const uint32_t m = (l + h) >> 1;
+        if (__ldg(&a[lo + m]) < x) l = m + 1;
+        else h = m;
+    }
+    return l;
+}
+
+// SurfaceSampler::genSample -> AbstractObject::genSurfaceSample
+// (surfaceSampler.cpp:17-23, abstractObj.cpp:18-52): 6 draws.  The reference
+// also traces the light sample's own ray; its result is unused by the path
+// tracer, so it is not traced here.
+__device__ __forceinline__ PRay light_sample(const RenderScene& S, PathRng& g) {
+    PRay r = ray_default();
+    const float chosen = g.next() * S.light_area;
+    uint32_t li = lower_bound_dev(S.light_thresh, 0, S.nlights, chosen);
+    if (li == S.nlights) li--;
+    const int o = __ldg(&S.light_obj[li]);
+    const uint32_t tb = __ldg(&S.objs[o].tri_begin), tc = __ldg(&S.objs[o].tri_count);
+    const float ra = g.next() * __ldg(&S.obj_area[o]);
+    uint32_t ti = lower_bound_dev(S.tri_thresh, tb, tc, ra);
+    if (ti == tc) ti--;
+    const TriRec* tr = S.tree.tris + __ldg(&S.tri_slot[tb + ti]);
+    const f3 v0 = xyz(__ldg(&tr->v0)), v1 = xyz(__ldg(&tr->v1)), v2 = xyz(__ldg(&tr->v2));
+    float u1 = g.next(), u2 = g.next();
+    if (u1 + u2 > 1.f) {
+        u1 = 1.f - u1;
+        u2 = 1.f - u2;
+    }
+    r.o = (v0 + (v1 - v0) * u1) + (v2 - v0) * u2;
+    const f3 N = face_normal(v0, v1, v2);
+    const float sx = g.next(), sy = g.next();
+    float s, c;
+    sincosf(2.f * PI_F * sx, &s, &c);
+    const float t2 = 2.f * sqrtf(fmaxf(0.f, sy - sy * sy));
+    r.d = mk(c * t2, 1.f - 2.f * sy, s * t2);
+    if (dot(r.d, N) < 0.f) r.d = -r.d;
+    r.dP = INV_PI_F * 0.25f * 2.f;
+    r.rad = ld3(S.objs[o].emission);
+    r.contact = o;
+    r.cnorm = N;
+    r.oP = 1.f / __ldg(&S.obj_area[o]) * __ldg(&S.pick_prob[o]);
+    return r;
+}
+
+// evaluateBSDF of the object at the connection vertex (Ray::evalBSDF, ray.cpp:15-22)
+__device__ __forceinline__ f3 eval_bsdf(const RenderScene& S, f3 in_d, const PRay& out) {
+    const int o = out.contact >= 0 ? out.contact : out.inside;
+    if (o < 0) return mk(0, 0, 0);
+    const wr_object_desc* m = &S.objs[o];
+    const uint32_t t = __ldg(&m->type);
+    switch (t) {
+        case WR_MAT_DIFFUSE:  // diffuseBsdf.h:31-33
+            if (out.contact < 0) return mk(0, 0, 0);
+            if (dot(in_d, out.cnorm) <= 0.f && dot(out.d, out.cnorm) >= 0.f) return ld3(m->albedo) * INV_PI_F;
+            return mk(0, 0, 0);
+        case WR_MAT_GLOSSY: {  // isotropicPhong.h:41-49
+            if (out.contact < 0) return mk(0, 0, 0);
+            const f3 N = out.cnorm;
+            if (!(dot(in_d, N) <= 0.f && dot(out.d, N) >= 0.f)) return mk(0, 0, 0);
+            const float power = __ldg(&m->power);
+            const f3 rho = ld3(m->albedo) * ((power + 2.f) * 0.5f * INV_PI_F);
+            const float dRW = dot(mirror_dir(N, in_d), out.d);
+            return rho * powf(dRW > 0.f ? dRW : 0.f, power);
+        }
+        case WR_MAT_ANISO:
+            if (out.contact < 0) return mk(0, 0, 0);
+            return aniso_eval(m, in_d, out.d, out.cnorm);
+        case WR_MAT_EMISSIVE: return ld3(m->emission);
+        case WR_MAT_HOMOGENEOUS:
+        case WR_MAT_HETEROGENEOUS:
+            if (out.contact < 0) {
+                f3 r = ld3(m->sigma_s) * hg_value(__ldg(&m->g), in_d, out.d);
+                if (t == WR_MAT_HETEROGENEOUS)
+                    r = r * grid_density(S.grids[__ldg(&m->grid_index)], out.o, __ldg(&m->density_scale));
+                return r;
+            }
+            if (out.contact != o) return mk(0, 0, 0);
+            return mk(0, 0, 0);
+    }
+    return mk(0, 0, 0);
+}
+
+// transmittance along a connection inside a heterogeneous medium: ratio
+// tracking against the majorant (unbiased; the reference integrates with
+// Simpson steps)
+__device__ __forceinline__ float ratio_tracking(const RenderScene& S, int obj, f3 o, f3 d, float dist, PathRng& g) {
+    const wr_object_desc* m = &S.objs[obj];
+    const GridDev G = S.grids[__ldg(&m->grid_index)];
+    const float scale = __ldg(&m->density_scale);
+    const float sgt = __ldg(&m->sigma_s[0]) + __ldg(&m->sigma_a[0]);
+    const float mu = G.majorant * scale * sgt;
+    if (!(mu > 0.f)) return 1.f;
+    float T = 1.f, t = 0.f;
+    for (int it = 0; it < 1 << 16; it++) {
+        t += -logf(1.f - g.next()) / mu;
+        if (t >= dist) break;
+        T *= 1.f - sgt * grid_density(G, o + d * t, scale) / mu;
+    }
+    return T;
+}
+
+// Builds the shadow connection of a path whose ray `end` closes it (the
+// reference's endRay) with `prev_d` the direction of the ray before it and
+// `color` the product of the earlier vertices' factors.  Returns false when
+// the reference adds nothing.
+__device__ __forceinline__ bool nee_prepare(const RenderScene& S, const PRay& end, f3 prev_d, f3 color, PathRng& g,
+                                            ShadowReq& sr) {
+    if (S.nlights == 0) return false;
+    PRay light = light_sample(S, g);
+    if (end.contact >= 0) {
+        const uint32_t t = obj_type(S, end.contact);
+        if (t == WR_MAT_EMISSIVE) return false;  // isEmissive()
+        if (t == WR_MAT_GLOSSY || t == WR_MAT_ANISO || t == WR_MAT_REFRACTIVE) return false;  // !nonSpecular()
+    }
+    PRay e = end;
+    e.d = normalize(light.o - e.o);
+    light.d = -e.d;
+    const float cd0 = length(light.o - e.o);
+    const float cd = cd0 > EPS_F ? cd0 : EPS_F;
+    if (dot(e.d, light.cnorm) >= 0.f) return false;
+    f3 decay = radiance_decay(S, e, cd);
+    if (e.inside >= 0 && obj_type(S, e.inside) == WR_MAT_HETEROGENEOUS) {
+        const float T = ratio_tracking(S, e.inside, e.o, e.d, cd, g);
+        decay = mk(T, T, T);
+    }
+    f3 t = vmul(vmul(eval_bsdf(S, prev_d, e), light.rad), decay);
+    t = t * cos_term(S, light) * cos_term(S, e);
+    t = divs(t, cd * cd);
+    sr.contrib = divs(vmul(color, t), e.oP * light.oP);
+    sr.o = e.o;
+    sr.d = e.d;
+    sr.dist = length(e.o - light.o);
+    sr.inside = e.inside;
+    sr.contact = e.contact;
+    return true;
+}
+
+// MCRenderer::visibilityTest (mcRenderer.cpp:59-65) on a closest hit
+__device__ __forceinline__ bool nee_visible(const Hit& h, float dist) {
+    return h.slot < 0 || h.t - dist >= -EPS_F;
+}
+
+// One bounce of MCRenderer::samplePath (mcRenderer.cpp:25-56) for a path
+// whose current ray `cur` has its hit set: scatter, then either finish
+// (returns true, `result` = the path's colour before isLegalColor) or apply
+// cur's throughput factors (pathTracer.cpp:29-38) and make the scattered ray
+// current (returns false; it must be traced next, a miss ends with 0).
+//
+// With NEE (`nee`), a path that ends with zero radiance and no contact or
+// inside object on its last ray (it escaped, or was cut at the maximum
+// length, or was absorbed in a medium) is connected to a light from the
+// origin of the ray that closes it (the reference's endIndex rule,
+// pathTracer.cpp:40-41): `nee_here` is set, `cur` is that ray, `prev_d` the
+// direction before it and `color` the product of the earlier factors.  A
+// scattered ray that misses is the caller's case: the same connection from it.
+__device__ __forceinline__ bool path_advance(const RenderScene& S, PRay& cur, f3& color, f3& prev_d,
+                                             uint32_t& depth, InsideStack& st, PathRng& g, uint32_t max_path_len,
+                                             bool nee, f3& result, bool& nee_here) {
+    nee_here = false;
+    const int self = cur.inside >= 0 ? cur.inside : cur.iobj;
+    if (self < 0) {  // escaped eye ray: terminateRay carries zero radiance, endIndex 0 connects nothing
+        result = mk(0, 0, 0);
+        return true;
+    }
+    PRay next = scatter(S, self, cur, g, st);
+    if (length(next.d) < 0.5f) {
+        const bool zero = next.rad.x == 0.f && next.rad.y == 0.f && next.rad.z == 0.f;
+        if (nee && zero) {
+            result = mk(0, 0, 0);
+            nee_here = next.contact == -1 && next.inside == -1 && depth >= 1;
+            return true;
+        }
+        color = color * cos_term(S, cur);
+        color = vmul(color, radiance_decay(S, cur, length(next.o - cur.o)));
+        color = vmul(color, weight(cur));
+        result = vmul(color, weight(next));
+        return true;
+    }
+    if (depth + 1 > max_path_len) {
+        result = mk(0, 0, 0);
+        nee_here = nee && depth >= 1;
+        return true;
+    }
+    st.set_top(next.inside);
+    color = color * cos_term(S, cur);
+    color = vmul(color, radiance_decay(S, cur, length(next.o - cur.o)));
+    color = vmul(color, weight(cur));
+    prev_d = cur.d;
+    cur = next;
+    depth++;
+    return false;
 }
 
 // fill the hit fields of `r` from a closest-hit result
