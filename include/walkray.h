@@ -214,6 +214,25 @@ int wr_render(wr_ctx* ctx, wr_scene_id scene, const wr_render_desc* desc, float*
 int wr_render_device(wr_ctx* ctx, wr_scene_id scene, const wr_render_desc* desc, float* d_sum, float* d_sumsq,
                      void* stream);
 
+/* Rendering without any device allocation.  No counterpart in the reference
+ * (the reference renders on the CPU).  wr_render allocates an accumulation
+ * film on every call, which callers that may not allocate device memory while
+ * rendering cannot use: code running during CUDA-graph capture in global
+ * mode, real-time loops that avoid allocation because it can synchronise the
+ * device, applications with their own memory pools.  This entry point renders
+ * like wr_render in WR_MODE_MEGAKERNEL but keeps the film in a fixed array
+ * inside the library (WR_NOALLOC_MAX_PIXELS pixels, 12 MiB per GPU that loads
+ * the library, held until exit) and writes the W*H*3 mean image to the
+ * caller's device buffer d_rgb_out, asynchronously on `stream` (NULL = the
+ * context's stream).  Larger images are rejected with WR_ERR_INVALID_ARGUMENT.
+ * It calls no allocation routine: the scene must have been rendered once
+ * before (wr_render / wr_render_device build its rendering tables), and the
+ * first call on a device looks up the array's device address, so make that
+ * first call before any stream capture.  All calls share the array: calls
+ * whose work overlaps on the GPU race and must be serialised. */
+#define WR_NOALLOC_MAX_PIXELS 1048576u
+int wr_render_noalloc(wr_ctx* ctx, wr_scene_id scene, const wr_render_desc* desc, float* d_rgb_out, void* stream);
+
 /* Per-stage profile of one wavefront render (no reference counterpart: the
  * reference has no timers).  The stages are launched one by one instead of
  * as a graph, each between CUDA events on the context's stream; the
