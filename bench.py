@@ -318,11 +318,14 @@ def reference_pt(args):
 # ---------------------------------------------------------------------------
 # kd: closest-hit microbenchmark
 # ---------------------------------------------------------------------------
+KD_RAYS = 1 << 24
+
+
 def kd_inputs(seed_rank: int):
     from walkray_gb300 import scenes as S
 
     s = S.icosphere_kd(8, seed=1)
-    rays = S.kd_rays(s, 1 << 24, seed=1 + seed_rank)
+    rays = S.kd_rays(s, KD_RAYS, seed=1 + seed_rank)
     return s, rays
 
 
@@ -442,7 +445,11 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--cpu-rows", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--kd-rays", type=int, default=1 << 24, help="rays per step (kd); smaller for ncu captures")
+    ap.add_argument("--pt-size", type=int, default=PT_SIZE, help="image side (pt); smaller for ncu captures")
     args = ap.parse_args()
+    globals()["PT_SIZE"] = args.pt_size
+    globals()["KD_RAYS"] = args.kd_rays
     world, rank, local = dist_setup()
     if args.warmup < 3:
         args.warmup = 3

@@ -64,7 +64,7 @@ void wro_scene_free(wro_scene* s);
 
 #define WRO_RNG_PHILOX 0   /* counter-based stream shared with the GPU */
 #define WRO_NEE 1u         /* PathTracer NEE branch (pathTracer.cpp:39-66) */
-#define WRO_INSIDE_STACK 2u /* track inside objects per path instead of findInsideObject */
+#define WRO_DELTA 4u       /* heterogeneous media by delta / ratio tracking (the GPU's scheme) */
 
 /* PathTracer::renderPixels inner loop for pixels [p0, p1) and samples
  * [s0, s1): accumulates per-pixel sums of the path contribution (after

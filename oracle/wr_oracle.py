@@ -17,6 +17,7 @@ LIB = os.path.join(HERE, "build", "libwr_oracle.so")
 _lib = None
 
 NEE = 1
+DELTA = 4  # heterogeneous media by delta / ratio tracking (the GPU's scheme)
 
 
 def build() -> None:

@@ -82,6 +82,18 @@ def test_oracle_nee_matches_reference_statistically(built):
     assert ref.mean() > 1.03 * plain.mean()  # the reference NEE mode is biased upwards
 
 
+def test_oracle_delta_tracking_agrees_with_regular_tracking(built):
+    """The heterogeneous medium by delta tracking (the GPU's scheme) against
+    the reference's Simpson/Newton regular tracking, both in the oracle, on
+    the media scene: image means within 4 standard errors."""
+    s = make_golden.golden_scenes()["media_small"]
+    orc = wr_oracle.SceneOracle(s)
+    reg = np.array([orc.render(8, 24, seed=700 + k)[0].mean() / 8 for k in range(8)])
+    dlt = np.array([orc.render(64, 24, seed=800 + k, flags=wr_oracle.DELTA)[0].mean() / 64 for k in range(8)])
+    se = np.sqrt(reg.var(ddof=1) / 8 + dlt.var(ddof=1) / 8)
+    assert abs(reg.mean() - dlt.mean()) < 4 * se, (reg.mean(), dlt.mean(), se)
+
+
 def test_oracle_render_matches_reference_statistically(built):
     """Cornell 32x32: the restated PathTracer vs 8 reference renders of 256 spp.
     Per-pixel z on 4x4 blocks; |z| > 4 on no block, mean within 1.5 %."""

@@ -170,17 +170,37 @@ def test_mixed_materials_paired_with_oracle(ctx):
     ctx.release(sid)
 
 
-def test_media_match_oracle(ctx):
-    """Heterogeneous fBm medium + homogeneous sphere: GPU delta tracking vs
-    the reference's Simpson/Newton regular tracking restated in the oracle.
-    The reference estimator carries quadrature bias, so means agree to 3 %."""
+def test_media_paired_with_oracle_delta_tracking(ctx):
+    """Heterogeneous fBm medium + homogeneous sphere, the oracle in its delta
+    tracking mode (the GPU's scheme): same seeds, same draws, per-image means
+    equal far below their noise."""
+    s = make_golden.golden_scenes()["media_small"]
+    sid = ctx.upload(s)
+    orc = wr_oracle.SceneOracle(s)
+    h, w = s.camera.height, s.camera.width
+    d, m = [], []
+    for seed in range(40, 46):
+        g = ctx.render(sid, 16, 24, seed=seed).astype(np.float64)
+        o = orc.render(16, 24, seed=seed, flags=wr_oracle.DELTA)[0].reshape(h, w, 3) / 16
+        d.append(g.mean() - o.mean())
+        m.append(o.mean())
+    d, m = np.array(d), np.array(m)
+    assert abs(d.mean()) < 0.25 * m.std(ddof=1), (d, m)
+    ctx.release(sid)
+
+
+def test_media_match_reference_algorithm(ctx):
+    """GPU delta tracking against the reference's own free-flight algorithm
+    (Simpson integration + Newton inversion, restated in the oracle): image
+    means agree within their standard error (the reference's quadrature bias
+    is below it at this sample count)."""
     s = make_golden.golden_scenes()["media_small"]
     sid = ctx.upload(s)
     gpu = gpu_images(ctx, sid, range(40, 48), 64, 24)
     orc = wr_oracle.SceneOracle(s)
     h, w = s.camera.height, s.camera.width
     ora = np.stack([orc.render(16, 24, seed=2000 + k)[0].reshape(h, w, 3) / 16 for k in range(8)])
-    assert abs(gpu.mean() / ora.mean() - 1) < 0.03, (gpu.mean(), ora.mean())
+    assert abs(mean_z(gpu, ora)) < 4.0, (gpu.mean(), ora.mean(), mean_z(gpu, ora))
     z = block_z(gpu, ora, 8)
     assert np.abs(z).max() < 5.0, np.abs(z).max()
     ctx.release(sid)

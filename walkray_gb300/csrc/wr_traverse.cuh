@@ -29,7 +29,8 @@ namespace wr {
 
 struct RayQ {
     f3 o, d, inv;
-    float M;  // grown-box margin for this ray
+    f3 olo, ohi;  // o + M and o - M: the slab planes of the box grown by M
+    float M;      // grown-box margin for this ray
 };
 
 __device__ __forceinline__ RayQ make_rayq(f3 o, f3 d, float scene_mag) {
@@ -39,8 +40,10 @@ __device__ __forceinline__ RayQ make_rayq(f3 o, f3 d, float scene_mag) {
     q.inv = mk(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
     float om = fmaxf(fabsf(o.x), fmaxf(fabsf(o.y), fabsf(o.z)));
     // reference predicate rounding <= ~4.1 eps (B + |o|), slab test rounding
-    // <= ~3 eps (B + |o|) (eps = 2^-24); 2e-6 is ~33 eps
+    // <= ~4 eps (B + |o|) (eps = 2^-24); 2e-6 is ~33 eps
     q.M = 2e-6f * (scene_mag + om) + 1e-30f;
+    q.olo = mk(o.x + q.M, o.y + q.M, o.z + q.M);
+    q.ohi = mk(o.x - q.M, o.y - q.M, o.z - q.M);
     return q;
 }
 
@@ -83,12 +86,32 @@ __device__ __forceinline__ bool all_faces(const Box& bx, const RayQ& q) {
            face_pass<4>(bx, q) || face_pass<5>(bx, q);
 }
 
+__device__ __forceinline__ float pick3(int k, float x, float y, float z) { return k == 0 ? x : (k == 1 ? y : z); }
+
+// The reference face test on the face given at run time (axis `a`, max plane
+// if `hi`), with register selects instead of a per-lane switch so that lanes
+// testing different faces do not diverge.  Same operations as face_pass<I>.
+__device__ __forceinline__ bool face_pass_sel(int a, bool hi, const Box& bx, const RayQ& q) {
+    const int b = a == 2 ? 0 : a + 1, c = b == 2 ? 0 : b + 1;
+    const float dA = pick3(a, q.d.x, q.d.y, q.d.z);
+    const float oA = pick3(a, q.o.x, q.o.y, q.o.z);
+    const float plane = hi ? pick3(a, bx.hx, bx.hy, bx.hz) : pick3(a, bx.lx, bx.ly, bx.lz);
+    const float oB = pick3(b, q.o.x, q.o.y, q.o.z), dB = pick3(b, q.d.x, q.d.y, q.d.z);
+    const float oC = pick3(c, q.o.x, q.o.y, q.o.z), dC = pick3(c, q.d.x, q.d.y, q.d.z);
+    const float loB = pick3(b, bx.lx, bx.ly, bx.lz), hiB = pick3(b, bx.hx, bx.hy, bx.hz);
+    const float loC = pick3(c, bx.lx, bx.ly, bx.lz), hiC = pick3(c, bx.hx, bx.hy, bx.hz);
+    if (dA == 0.f) return false;
+    const float dist = (plane - oA) / dA;
+    const float pb = oB + dist * dB;
+    const float pc = oC + dist * dC;
+    return dist >= 0.f && loB <= pb && hiB >= pb && loC <= pc && hiC >= pc;
+}
+
 // The reference box predicate; *tnear gets the grown-box entry distance.
 __device__ __forceinline__ bool box_pred(const Box& bx, const RayQ& q, float* tnear) {
-    const float M = q.M;
-    float ax = (bx.lx - M - q.o.x) * q.inv.x, bxx = (bx.hx + M - q.o.x) * q.inv.x;
-    float ay = (bx.ly - M - q.o.y) * q.inv.y, by = (bx.hy + M - q.o.y) * q.inv.y;
-    float az = (bx.lz - M - q.o.z) * q.inv.z, bz = (bx.hz + M - q.o.z) * q.inv.z;
+    float ax = (bx.lx - q.olo.x) * q.inv.x, bxx = (bx.hx - q.ohi.x) * q.inv.x;
+    float ay = (bx.ly - q.olo.y) * q.inv.y, by = (bx.hy - q.ohi.y) * q.inv.y;
+    float az = (bx.lz - q.olo.z) * q.inv.z, bz = (bx.hz - q.ohi.z) * q.inv.z;
     // fminf/fmaxf drop NaN (0 * inf on a zero direction component): no constraint
     float nx = fminf(ax, bxx), fx = fmaxf(ax, bxx);
     float ny = fminf(ay, by), fy = fmaxf(ay, by);
@@ -102,17 +125,14 @@ __device__ __forceinline__ bool box_pred(const Box& bx, const RayQ& q, float* tn
         if (tn == tn && tf == tf) return false;
         return all_faces(bx, q);
     }
-    int face;
-    if (tn >= 0.f) {  // entry face: axis of the largest near distance
-        int ax_i = (nx >= ny && nx >= nz) ? 0 : (ny >= nz ? 1 : 2);
-        float da = ax_i == 0 ? q.d.x : (ax_i == 1 ? q.d.y : q.d.z);
-        face = ax_i + (da > 0.f ? 0 : 3);
-    } else {  // origin inside: exit face
-        int ax_i = (fx <= fy && fx <= fz) ? 0 : (fy <= fz ? 1 : 2);
-        float da = ax_i == 0 ? q.d.x : (ax_i == 1 ? q.d.y : q.d.z);
-        face = ax_i + (da > 0.f ? 3 : 0);
-    }
-    if (face_pass_dyn(face, bx, q)) return true;
+    // entry face (axis of the largest near distance), or the exit face (axis
+    // of the smallest far distance) when the origin is inside
+    const bool entry = tn >= 0.f;
+    const int ea = (nx >= ny && nx >= nz) ? 0 : (ny >= nz ? 1 : 2);
+    const int xa = (fx <= fy && fx <= fz) ? 0 : (fy <= fz ? 1 : 2);
+    const int a = entry ? ea : xa;
+    const bool pos = pick3(a, q.d.x, q.d.y, q.d.z) > 0.f;
+    if (face_pass_sel(a, entry ? !pos : pos, bx, q)) return true;
     return all_faces(bx, q);
 }
 
