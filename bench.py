@@ -25,6 +25,7 @@ all host threads) on a bounded sample of the same workload.
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import statistics
@@ -316,6 +317,135 @@ def reference_pt(args):
 
 
 # ---------------------------------------------------------------------------
+# serve: a seeded Poisson stream of render requests through the serving loop
+# ---------------------------------------------------------------------------
+SERVE_RATE = 20.0                       # requests per second
+SERVE_RES = (128, 256, 512, 1024)       # square resolutions, drawn uniformly
+SERVE_SPP = (16, 64, 256)
+METRIC_SERVE = "request latency p50/p99 (s) and Mpaths/s, Poisson request stream through the serving loop"
+
+
+def serve_scenes():
+    """(name, scene, max path length): Cornell box, the mixed-material scene, the media scene."""
+    from walkray_gb300 import scenes as S
+
+    return [("cornell", S.cornell(256, 256), 8), ("mixed", S.mixed_spheres(1024, 1024, seed=PT_SEED), 16),
+            ("media", S.cornell_media(512, 512), 24)]
+
+
+def serve_stream(seconds: float, rate: float, seed: int):
+    """Seeded arrivals: (time, scene index, side, spp), exponential gaps at `rate`."""
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= seconds:
+            return out
+        out.append((t, int(rng.integers(3)), SERVE_RES[rng.integers(4)], SERVE_SPP[rng.integers(3)]))
+
+
+def run_stream(srv, sids, depths, stream):
+    """Submits each request at its arrival time; returns per-request statuses (library clock)."""
+    t0 = time.perf_counter()
+    rids = []
+    for (t, k, side, spp) in stream:
+        dt = t - (time.perf_counter() - t0)
+        if dt > 0:
+            time.sleep(dt)
+        rids.append(srv.submit(sids[k], side, side, spp, depths[k], seed=len(rids) + 1))
+    st = srv.wait(rids, timeout=3600)
+    for r in rids:
+        srv.fetch(r)
+    return [st[r] for r in rids]
+
+
+def serve_stats(stream, st):
+    lat = np.array([s["finish_s"] - s["submit_s"] for s in st])
+    wait = np.array([s["admit_s"] - s["submit_s"] for s in st])
+    paths = sum(s["paths_total"] for s in st)
+    span = max(s["finish_s"] for s in st) - min(s["submit_s"] for s in st)
+    return {"requests": len(st), "p50_s": round(float(np.percentile(lat, 50)), 4),
+            "p99_s": round(float(np.percentile(lat, 99)), 4),
+            "p99_over_p50": round(float(np.percentile(lat, 99) / np.percentile(lat, 50)), 3),
+            "admission_wait_p50_s": round(float(np.percentile(wait, 50)), 4),
+            "mpaths_per_s": round(paths / span / 1e6, 2), "paths": int(paths), "makespan_s": round(span, 3),
+            "offered_mpaths_per_s": round(paths / (stream[-1][0] if stream else 1.0) / 1e6, 2)}
+
+
+def run_serve(args, world, rank, local):
+    import torch
+
+    from walkray_gb300.api import Context, Server
+
+    torch.cuda.set_device(local)
+    scenes = serve_scenes()
+    ctx = Context(device=local)
+    sids = [ctx.upload(sc) for _, sc, _ in scenes]
+    depths = [d for _, _, d in scenes]
+    # per-sample relMSE of each (scene, resolution): variance of 16 spp per pixel
+    # against an independent 64-spp image, mean of Var/(R^2 + 1e-2); a request
+    # of s spp then has relMSE = that / s (unbiased estimator)
+    rel1 = {}
+    if not args.quick:
+        for k, (name, sc, d) in enumerate(scenes):
+            for side in SERVE_RES:
+                sid = ctx.upload(scene_at(sc, side))
+                s1, s2 = ctx.render_stats(sid, 16, d, seed=5, mode="wavefront")
+                ref = ctx.render(sid, 64, d, seed=6, mode="wavefront").astype(np.float64)
+                var = np.maximum(s2 / 16 - (s1 / 16) ** 2, 0) * 16 / 15
+                rel1[(k, side)] = float(np.mean(var / (ref ** 2 + 1e-2)))
+                ctx.release(sid)
+    srv = Server(ctx, film_bytes=2 << 30, max_active=64)
+    # warm-up: one small request per scene
+    run_stream(srv, sids, depths, [(0.0, k, 128, 16) for k in range(3)])
+    seconds = args.serve_seconds
+    legs = {}
+    stream = serve_stream(seconds, SERVE_RATE, seed=2024 + rank)
+    with ClockSampler(local) as clk:
+        st = run_stream(srv, sids, depths, stream)
+    legs["stream"] = serve_stats(stream, st)
+    if rel1:
+        rr = [rel1[(k, side)] / spp for (_, k, side, spp) in stream]
+        legs["stream"]["relmse_per_request"] = {"p50": float(np.percentile(rr, 50)), "max": float(max(rr))}
+    # the same stream slowed to 60 % of the sustained throughput: latency without a backlog
+    load = legs["stream"]["offered_mpaths_per_s"] / max(1e-9, legs["stream"]["mpaths_per_s"])
+    if load > 0.6 and not args.quick:
+        f = load / 0.6
+        st2 = run_stream(srv, sids, depths, [(t * f, k, side, spp) for (t, k, side, spp) in stream])
+        legs["stream_at_60pct_load"] = serve_stats([(t * f, *x) for (t, *x) in stream], st2)
+        legs["stream_at_60pct_load"]["rate_req_per_s"] = round(SERVE_RATE / f, 3)
+    srv.stop()
+    ctx.close()
+    main_leg = legs["stream"]
+    line = {
+        "metric": METRIC_SERVE, "value": main_leg["mpaths_per_s"], "unit": "Mpaths/s", "n_gpus": world,
+        "steps": 1, "warmup": 1, "ms_per_step": round(main_leg["makespan_s"] * 1e3, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes and arrivals)",
+        "config": {"workload": f"serve: Poisson {SERVE_RATE:g} req/s for {seconds:g} s over Cornell (depth 8), "
+                               "mixed-material (depth 16) and media (depth 24) scenes, resolution "
+                               "U{128^2..1024^2}, spp U{16,64,256}", "parallelism": f"replicas x{world}"},
+        "p50_s": main_leg["p50_s"], "p99_s": main_leg["p99_s"], "legs": legs, "clocks": clk.summary(),
+        "relmse_formula": "mean((I-R)^2/(R^2+1e-2)) = mean(Var/(R^2+1e-2))/spp, Var from 16 spp per pixel, "
+                          "R = independent 64-spp image",
+    }
+    if rel1:
+        line["relmse_1spp"] = {f"{scenes[k][0]}_{side}": round(v, 4) for (k, side), v in rel1.items()}
+    return line
+
+
+def scene_at(scene, side):
+    """The same scene with a square camera of the given side."""
+    import copy
+
+    s = copy.copy(scene)
+    c = s.camera
+    # the image plane distance is in pixels: keep the field of view (as the serving loop does)
+    ipd = float(np.float32(c.image_plane_dist) * np.float32(side / c.height))
+    s.camera = dataclasses.replace(c, width=side, height=side, image_plane_dist=ipd)
+    return s
+
+
+# ---------------------------------------------------------------------------
 # kd: closest-hit microbenchmark
 # ---------------------------------------------------------------------------
 KD_RAYS = 1 << 24
@@ -439,7 +569,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["pt", "kd"], default=os.environ.get("WR_BENCH_WORKLOAD", "pt"))
+    ap.add_argument("--workload", choices=["pt", "kd", "serve"], default=os.environ.get("WR_BENCH_WORKLOAD", "pt"))
     ap.add_argument("--tune", action="store_true", help="run the wavefront autotuner first (pt)")
     ap.add_argument("--quick", action="store_true", help="skip the roofline profile, relMSE and CPU legs (pt)")
     ap.add_argument("--cpu-sample", type=int, default=0)
@@ -447,6 +577,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--kd-rays", type=int, default=1 << 24, help="rays per step (kd); smaller for ncu captures")
     ap.add_argument("--pt-size", type=int, default=PT_SIZE, help="image side (pt); smaller for ncu captures")
+    ap.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window of the request stream (serve)")
     args = ap.parse_args()
     globals()["PT_SIZE"] = args.pt_size
     globals()["KD_RAYS"] = args.kd_rays
@@ -466,7 +597,8 @@ def main():
     from walkray_gb300 import build
 
     build.build_lib()
-    line = run_pt(args, world, rank, local) if args.workload == "pt" else run_kd(args, world, rank, local)
+    run = {"pt": run_pt, "kd": run_kd, "serve": run_serve}[args.workload]
+    line = run(args, world, rank, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

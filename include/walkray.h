@@ -193,6 +193,13 @@ int wr_trace_closest_device(wr_ctx* ctx, wr_scene_id scene, const float* d_rays,
 #define WR_MODE_WAVEFRONT 1u  /* generate / extend / shade queues, persistent kernels, graph bounce loop */
 
 #define WR_RENDER_NEE 1u      /* PathTracer's next-event-estimation branch (pathTracer.cpp:39-66) */
+/* Rendering traverses front to back and skips a box whose entry distance is
+ * beyond the closest hit found so far (with a 0.1 % relative margin).  That
+ * gives the reference's closest hit except for a ray that grazes a triangle
+ * so nearly in its plane that the triangle test's rounding moves the hit
+ * outside the triangle's box.  This flag visits every box the reference
+ * visits (KDTree::intersect, kdtree.cpp:308-347), as wr_trace_closest does. */
+#define WR_RENDER_EXACT_TRAVERSAL 2u
 
 typedef struct wr_render_desc {
     uint32_t spp;          /* samples per pixel (PathTracer spp) */

@@ -221,3 +221,33 @@ def test_render_rejects_bad_requests(ctx):
     img = ctx.render(sid, 0, 8)
     assert not img.any()
     ctx.release(sid)
+
+
+def test_pruned_traversal_equals_exact_traversal(ctx):
+    """Front-to-back pruning (the renderers' default) against the reference's
+    visit-every-passing-box traversal (WR_RENDER_EXACT_TRAVERSAL) on the same
+    random stream: the same closest hits give the same paths, so the images
+    agree pixel for pixel but for rays grazing a triangle in its plane."""
+    s = make_golden.golden_scenes()["mixed_l2"]
+    sid = ctx.upload(s)
+    for mode in ("megakernel", "wavefront"):
+        a = ctx.render(sid, 16, 16, seed=41, mode=mode).astype(np.float64)
+        b = ctx.render(sid, 16, 16, seed=41, mode=mode, exact=True).astype(np.float64)
+        close = np.isclose(a, b, rtol=1e-4, atol=1e-5).all(-1)
+        assert close.mean() > 0.999, (mode, close.mean())
+        assert abs(a.mean() / b.mean() - 1) < 1e-3
+    ctx.release(sid)
+
+
+def test_pruning_reduces_traversal_work(ctx):
+    import torch
+
+    s = make_golden.golden_scenes()["mixed_l2"]
+    sid = ctx.upload(s)
+    w, h = s.camera.width, s.camera.height
+    film = torch.zeros(w * h * 3, dtype=torch.float32, device="cuda")
+    pr = ctx.profile_render(sid, 1, 16, film.data_ptr(), seed=3)
+    ex = ctx.profile_render(sid, 1, 16, film.data_ptr(), seed=3, exact=True)
+    assert abs(pr["rays"] - ex["rays"]) <= 1e-3 * ex["rays"]
+    assert pr["box_tests"] < ex["box_tests"]
+    ctx.release(sid)

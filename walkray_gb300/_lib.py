@@ -116,6 +116,7 @@ class wr_render_profile(C.Structure):
 
 
 WR_RENDER_NEE = 1
+WR_RENDER_EXACT_TRAVERSAL = 2
 
 HIT_DTYPE = np.dtype([("tri", "<u4"), ("t", "<f4"), ("b1", "<f4"), ("b2", "<f4")])
 

@@ -125,23 +125,24 @@ class Context:
 
     # ---- rendering ------------------------------------------------------
     def render(self, sid: int, spp: int, max_path_len: int, seed: int = 1, mode: str = "megakernel",
-               nee: bool = False, spp_offset: int = 0) -> np.ndarray:
+               nee: bool = False, spp_offset: int = 0, exact: bool = False) -> np.ndarray:
         """Mean image (H, W, 3) float32, row 0 at the top (wr_render)."""
         w, h = self._camera_size(sid)
         out = np.empty((h, w, 3), np.float32)
-        d = L.wr_render_desc(spp, max_path_len, seed, MODES[mode], L.WR_RENDER_NEE if nee else 0, spp_offset, 0)
+        d = L.wr_render_desc(spp, max_path_len, seed, MODES[mode], _flags(nee, exact), spp_offset, 0)
         self._check(self.lib.wr_render(self.h, sid, C.byref(d), L.ptr(out)))
         return out
 
     def render_device(self, sid: int, spp: int, max_path_len: int, d_sum: int, d_sumsq: int = 0, seed: int = 1,
-                      mode: str = "megakernel", nee: bool = False, spp_offset: int = 0, stream: int = 0) -> None:
+                      mode: str = "megakernel", nee: bool = False, spp_offset: int = 0, stream: int = 0,
+                      exact: bool = False) -> None:
         """Adds spp samples to a device film (wr_render_device), asynchronous on `stream`."""
-        d = L.wr_render_desc(spp, max_path_len, seed, MODES[mode], L.WR_RENDER_NEE if nee else 0, spp_offset, 0)
+        d = L.wr_render_desc(spp, max_path_len, seed, MODES[mode], _flags(nee, exact), spp_offset, 0)
         self._check(self.lib.wr_render_device(self.h, sid, C.byref(d), C.c_void_p(d_sum), C.c_void_p(d_sumsq or None),
                                               C.c_void_p(stream or None)))
 
     def render_stats(self, sid: int, spp: int, max_path_len: int, seed: int = 1, mode: str = "megakernel",
-                     nee: bool = False):
+                     nee: bool = False, exact: bool = False):
         """Per-pixel sum and sum of squares (H, W, 3) over spp samples, via torch device buffers."""
         import torch
 
@@ -150,14 +151,14 @@ class Context:
         s2 = torch.zeros((h, w, 3), dtype=torch.float32, device="cuda")
         torch.cuda.synchronize()
         self.render_device(sid, spp, max_path_len, s.data_ptr(), s2.data_ptr(), seed, mode, nee,
-                           stream=torch.cuda.current_stream().cuda_stream)
+                           stream=torch.cuda.current_stream().cuda_stream, exact=exact)
         torch.cuda.synchronize()
         return s.cpu().numpy().astype(np.float64), s2.cpu().numpy().astype(np.float64)
 
     def profile_render(self, sid: int, spp: int, max_path_len: int, d_sum: int, seed: int = 1,
-                       nee: bool = False) -> dict:
+                       nee: bool = False, exact: bool = False) -> dict:
         """Wavefront render with per-stage CUDA-event timings and traversal work counts."""
-        d = L.wr_render_desc(spp, max_path_len, seed, 1, L.WR_RENDER_NEE if nee else 0, 0, 0)
+        d = L.wr_render_desc(spp, max_path_len, seed, 1, _flags(nee, exact), 0, 0)
         p = L.wr_render_profile()
         self._check(self.lib.wr_profile_render(self.h, sid, C.byref(d), C.c_void_p(d_sum), C.byref(p)))
         return {k: getattr(p, k) for k, _ in L.wr_render_profile._fields_}
@@ -181,6 +182,11 @@ class Context:
 
 MODES = {"megakernel": 0, "wavefront": 1}
 
+
+def _flags(nee: bool, exact: bool) -> int:
+    """WR_RENDER_* bits: the NEE branch; exact = no distance pruning in traversal."""
+    return (L.WR_RENDER_NEE if nee else 0) | (L.WR_RENDER_EXACT_TRAVERSAL if exact else 0)
+
 REQ_STATES = {0: "queued", 1: "running", 2: "done", 3: "cancelled", 4: "failed"}
 
 
@@ -195,8 +201,8 @@ class Server:
         self.sizes: dict[int, tuple[int, int]] = {}
 
     def submit(self, sid: int, width: int, height: int, spp: int, max_path_len: int, seed: int = 1,
-               nee: bool = False) -> int:
-        r = L.wr_request_desc(sid, width, height, spp, max_path_len, L.WR_RENDER_NEE if nee else 0, seed)
+               nee: bool = False, exact: bool = False) -> int:
+        r = L.wr_request_desc(sid, width, height, spp, max_path_len, _flags(nee, exact), seed)
         rid = C.c_uint64()
         self.ctx._check(self.ctx.lib.wr_submit(self.ctx.h, C.byref(r), C.byref(rid)))
         self.sizes[rid.value] = (width, height)

@@ -201,7 +201,7 @@ int wr_render_device(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, fl
     if (!sc) return set_error(ctx, WR_ERR_NOT_FOUND, "no such scene");
     if (desc->mode != WR_MODE_MEGAKERNEL && desc->mode != WR_MODE_WAVEFRONT)
         return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "unknown render mode");
-    if (desc->flags & ~(WR_RENDER_NEE)) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "unknown render flags");
+    if (desc->flags & ~RENDER_KNOWN_FLAGS) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "unknown render flags");
     if ((uint64_t)desc->spp_offset + desc->spp > 0xffffffffull)
         return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "sample index range overflows 32 bits");
     try {
@@ -294,7 +294,7 @@ extern "C" int wr_profile_render(wr_ctx* ctx, wr_scene_id id, const wr_render_de
     if (!ctx || !desc || !d_sum || !out) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "null argument");
     SceneGPU* sc = find_scene(ctx, id);
     if (!sc) return set_error(ctx, WR_ERR_NOT_FOUND, "no such scene");
-    if (desc->flags & ~(WR_RENDER_NEE)) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "unknown render flags");
+    if (desc->flags & ~RENDER_KNOWN_FLAGS) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "unknown render flags");
     WR_CUDA(ctx, cudaSetDevice(ctx->device));
     RenderData* rd = nullptr;
     int rc = prepare_render(ctx, sc, &rd);

@@ -7,6 +7,13 @@
 
 namespace wr {
 
+constexpr uint32_t RENDER_KNOWN_FLAGS = WR_RENDER_NEE | WR_RENDER_EXACT_TRAVERSAL;
+
+// factor on the closest hit's distance beyond which a box is skipped
+__host__ __device__ __forceinline__ float prune_factor(uint32_t flags) {
+    return (flags & WR_RENDER_EXACT_TRAVERSAL) ? INFINITY : 1.001f;
+}
+
 struct RenderParams {
     uint64_t seed;
     uint32_t s0, s1;          // sample range [s0, s1)

@@ -18,6 +18,7 @@ __global__ void __launch_bounds__(128) k_megakernel(RenderScene S, RenderParams 
     const uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x;
     if (pixel >= npix) return;
     f3 acc = mk(0, 0, 0), acc2 = mk(0, 0, 0);
+    const float pf = prune_factor(P.flags);
     for (uint32_t s = P.s0; s < P.s1; s++) {
         PathRng g;
         g.init(P.seed, pixel, s);
@@ -30,10 +31,11 @@ __global__ void __launch_bounds__(128) k_megakernel(RenderScene S, RenderParams 
         const bool nee = (P.flags & WR_RENDER_NEE) != 0;
         bool nee_here = false;
         for (;;) {
-            const RayQ q = make_rayq(cur.o, cur.d, S.tree.scene_mag);
-            const Hit h = filtered ? trace_closest<true, false>(S.tree, q, cur.inside, cur.contact, stack, stride,
-                                                                P.stack_cap, err)
-                                   : trace_closest<false, false>(S.tree, q, -1, -1, stack, stride, P.stack_cap, err);
+            RayQ q = make_rayq(cur.o, cur.d, S.tree.scene_mag);
+            q.pf = pf;
+            const Hit h = filtered ? trace_closest<true, true>(S.tree, q, cur.inside, cur.contact, stack, stride,
+                                                               P.stack_cap, err)
+                                   : trace_closest<false, true>(S.tree, q, -1, -1, stack, stride, P.stack_cap, err);
             if (h.slot < 0 && filtered) {  // a scattered ray that escapes ends with zero radiance
                 nee_here = nee;
                 break;
@@ -45,9 +47,10 @@ __global__ void __launch_bounds__(128) k_megakernel(RenderScene S, RenderParams 
         if (nee_here) {  // the connection of the NEE branch, traced inline
             ShadowReq sr;
             if (nee_prepare(S, cur, prev_d, color, g, sr)) {
-                const RayQ q = make_rayq(sr.o, sr.d, S.tree.scene_mag);
+                RayQ q = make_rayq(sr.o, sr.d, S.tree.scene_mag);
+                q.pf = pf;
                 const Hit h =
-                    trace_closest<true, false>(S.tree, q, sr.inside, sr.contact, stack, stride, P.stack_cap, err);
+                    trace_closest<true, true>(S.tree, q, sr.inside, sr.contact, stack, stride, P.stack_cap, err);
                 if (nee_visible(h, sr.dist)) result = sr.contrib;
             }
         }

@@ -78,7 +78,7 @@ extern "C" int wr_render_noalloc(wr_ctx* ctx, wr_scene_id id, const wr_render_de
     if (!sc) return set_error(ctx, WR_ERR_NOT_FOUND, "no such scene");
     if (desc->mode != WR_MODE_MEGAKERNEL)
         return set_error(ctx, WR_ERR_UNSUPPORTED, "wr_render_noalloc renders with the megakernel (WR_MODE_MEGAKERNEL)");
-    if (desc->flags & ~(WR_RENDER_NEE)) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "unknown render flags");
+    if (desc->flags & ~RENDER_KNOWN_FLAGS) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "unknown render flags");
     const uint64_t npix = (uint64_t)sc->camera.width * sc->camera.height;
     if (npix > WR_NOALLOC_MAX_PIXELS)
         return set_error(ctx, WR_ERR_INVALID_ARGUMENT,

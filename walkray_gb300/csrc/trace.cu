@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(256) k_trace_closest(DevTree T, const float* _
                 bool hl = box_pred(Box{A.x, A.y, A.z, A.w, B.x, B.y}, q, &tl);
                 bool hr = box_pred(Box{B.z, B.w, C.x, C.y, C.z, C.w}, q, &tr);
                 if (PRUNE) {
-                    const float lim = h.t * 1.001f + q.M;
+                    const float lim = h.t * q.pf + q.M;
                     hl = hl && !(tl > lim);
                     hr = hr && !(tr > lim);
                 }

@@ -116,8 +116,9 @@ __global__ void __launch_bounds__(128) k_wf_shadow(const RenderScene* __restrict
         const int4 ids = Q.ids[i];
         const WfJob& J = jobs[ids.z];
         const DevTree& T = scenes[J.scene].tree;
-        const RayQ q = make_rayq(mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), T.scene_mag);
-        const Hit h = trace_closest<true, false>(T, q, ids.x, ids.y, stack, blockDim.x, stack_cap, err);
+        RayQ q = make_rayq(mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), T.scene_mag);
+        q.pf = prune_factor(J.flags);
+        const Hit h = trace_closest<true, true>(T, q, ids.x, ids.y, stack, blockDim.x, stack_cap, err);
         if (nee_visible(h, o.w)) film_add(J, (uint32_t)ids.w, mk(c.x, c.y, c.z));
     }
 }
@@ -158,8 +159,10 @@ __global__ void __launch_bounds__(128) k_wf_extend(const RenderScene* __restrict
                     rid = id;
                     const float4 a0 = X.a0[id], a1 = X.a1[id];
                     const int4 ids = X.ids[id];
-                    T = scenes[jobs[ids.z].scene].tree;
+                    const WfJob& J = jobs[ids.z];
+                    T = scenes[J.scene].tree;
                     q = make_rayq(mk(a0.x, a0.y, a0.z), mk(a1.x, a1.y, a1.z), T.scene_mag);
+                    q.pf = prune_factor(J.flags);
                     in_obj = ids.x;
                     ct_obj = ids.y;
                     filt = ct_obj != CAMERA_OBJ;
@@ -195,6 +198,11 @@ __global__ void __launch_bounds__(128) k_wf_extend(const RenderScene* __restrict
                 bool hl = box_pred(Box{A.x, A.y, A.z, A.w, B.x, B.y}, q, &tl);
                 bool hr = box_pred(Box{B.z, B.w, C.x, C.y, C.z, C.w}, q, &tr);
                 n_box += 2;
+                {  // front-to-back pruning against the closest hit so far
+                    const float lim = h.t * q.pf + q.M;
+                    hl = hl && !(tl > lim);
+                    hr = hr && !(tr > lim);
+                }
                 if (hl && (W.y & LEAF_FLAG)) {
                     n_tri += W.y & ~LEAF_FLAG;
                     if (filt) leaf_test<true>(T, W.x, W.y & ~LEAF_FLAG, q, in_obj, ct_obj, h);

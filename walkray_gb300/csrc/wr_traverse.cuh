@@ -18,9 +18,11 @@
 //    (entry face, or exit face when the origin is inside) and on all six only
 //    if that one fails.  Every "pass" is decided by the reference's own
 //    arithmetic, every "fail" either by it or by the proof above.
-//  * Optional pruning (PRUNE): a child whose grown-box entry distance exceeds
-//    the best hit by a relative margin is skipped.  Not covered by the proof
-//    for grazing triangles; off in the parity path.
+//  * Optional pruning (PRUNE, used by the renderers): a child whose grown-box
+//    entry distance exceeds q.pf times the best hit (plus M) is skipped.  A
+//    triangle's hit lies inside its box, so this keeps the closest hit unless
+//    the triangle test's rounding puts a hit far from the triangle (a ray
+//    almost in the triangle's plane); off in wr_trace_closest.
 #pragma once
 
 #include "wr_device.cuh"
@@ -31,6 +33,7 @@ struct RayQ {
     f3 o, d, inv;
     f3 olo, ohi;  // o + M and o - M: the slab planes of the box grown by M
     float M;      // grown-box margin for this ray
+    float pf;     // pruning: boxes entered beyond pf * (closest hit) + M are skipped
 };
 
 __device__ __forceinline__ RayQ make_rayq(f3 o, f3 d, float scene_mag) {
@@ -44,6 +47,7 @@ __device__ __forceinline__ RayQ make_rayq(f3 o, f3 d, float scene_mag) {
     q.M = 2e-6f * (scene_mag + om) + 1e-30f;
     q.olo = mk(o.x + q.M, o.y + q.M, o.z + q.M);
     q.ohi = mk(o.x - q.M, o.y - q.M, o.z - q.M);
+    q.pf = 1.001f;
     return q;
 }
 
@@ -226,7 +230,7 @@ __device__ __forceinline__ Hit trace_closest(const DevTree& T, const RayQ& q, in
         bool hl = box_pred(Box{A.x, A.y, A.z, A.w, B.x, B.y}, q, &tl);
         bool hr = box_pred(Box{B.z, B.w, C.x, C.y, C.z, C.w}, q, &tr);
         if (PRUNE) {
-            const float lim = h.t * 1.001f + q.M;
+            const float lim = h.t * q.pf + q.M;
             hl = hl && !(tl > lim);
             hr = hr && !(tr > lim);
         }
