@@ -51,6 +51,7 @@ RAY_IO_BYTES, BOX_BYTES, TRI_BYTES = 40, 32, 52
 KD_BYTES_PER_RAY = RAY_IO_BYTES + KD_BOX_TESTS * BOX_BYTES + KD_TRI_TESTS * TRI_BYTES
 
 PT_SIZE, PT_DEPTH, PT_SEED = 1024, 16, 7
+PT_SPP = 16  # samples per pixel per step (one render call)
 METRIC_PT = "Mpaths/s (wavefront path tracing, 1024^2 mixed-material scene; time-to-relMSE 1e-3 beside it)"
 
 
@@ -176,12 +177,17 @@ def pt_scene():
     return S.mixed_spheres(PT_SIZE, PT_SIZE, seed=PT_SEED)
 
 
-def relmse_variance(a, b, ref):
-    """relMSE of one of two independent renders a, b (same spp) against the
-    converged image: mean over pixels and channels of Var/(R^2 + 1e-2), the
-    variance estimated as (a-b)^2/2 (the estimator is unbiased, so the bias
-    term is zero)."""
-    return float(np.mean(((a - b) ** 2 / 2.0) / (ref ** 2 + 1e-2)))
+def relmse_per_sample(s1, s2, spp, ref):
+    """relMSE of a 1-spp image against the converged image R: mean over pixels
+    and channels of Var/(R^2 + 1e-2), with the per-sample variance of each
+    pixel from its sum s1 and sum of squares s2 over `spp` samples (the
+    estimator is unbiased, so MSE = variance and an n-spp image has 1/n of
+    it).  Also the share of the total that comes from the top 0.1 % of
+    entries: a large share means a heavy-tailed estimator."""
+    var = np.maximum(s2 / spp - (s1 / spp) ** 2, 0.0) * spp / (spp - 1)
+    e = var / (ref ** 2 + 1e-2)
+    top = np.sort(e.ravel())[::-1][: max(1, e.size // 1000)]
+    return float(e.mean()), float(top.sum() / max(e.sum(), 1e-30))
 
 
 def cpu_baseline_pt(scene, rows: int, threads: int):
@@ -215,8 +221,8 @@ def run_pt(args, world, rank, local):
     seed = 1000 + rank
 
     def step_mode(mode):
-        return lambda i: ctx.render_device(sid, 1, PT_DEPTH, film.data_ptr(), seed=seed, mode=mode, spp_offset=i,
-                                           stream=stream.cuda_stream)
+        return lambda i: ctx.render_device(sid, PT_SPP, PT_DEPTH, film.data_ptr(), seed=seed, mode=mode,
+                                           spp_offset=i * PT_SPP, stream=stream.cuda_stream)
 
     with torch.cuda.stream(stream):
         for i in range(args.warmup):
@@ -230,29 +236,32 @@ def run_pt(args, world, rank, local):
         n_launch = launches(ctx) - l0
         ms_mk = timed_steps(step_mode("megakernel"), args.steps, stream, flush)
     ms_max = allreduce(world, ms, "max")
-    units = allreduce(world, float(npix * args.steps), "sum")
+    paths = float(npix * PT_SPP * args.steps)
+    units = allreduce(world, paths, "sum")
     value = units / (ms_max / 1e3) / 1e6
-    mk_value = allreduce(world, float(npix * args.steps), "sum") / (allreduce(world, ms_mk, "max") / 1e3) / 1e6
+    mk_value = allreduce(world, paths, "sum") / (allreduce(world, ms_mk, "max") / 1e3) / 1e6
 
-    # e2e: wr_render returning the image to the host, one sample per pixel per step
+    # e2e: wr_render returning the image to the host, PT_SPP samples per pixel per step
     barrier(world)
     t0 = time.perf_counter()
     for i in range(args.steps):
-        ctx.render(sid, 1, PT_DEPTH, seed=seed + 1, mode="wavefront", spp_offset=i)
+        ctx.render(sid, PT_SPP, PT_DEPTH, seed=seed + 1, mode="wavefront", spp_offset=i * PT_SPP)
     e2e_s = allreduce(world, time.perf_counter() - t0, "max")
-    e2e = allreduce(world, float(npix * args.steps), "sum") / e2e_s / 1e6
+    e2e = allreduce(world, paths, "sum") / e2e_s / 1e6
 
     line = {
         "metric": METRIC_PT, "value": round(value, 2), "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
         "config": {"workload": "pt: 25 displaced level-5 icospheres (512,006 tris) on a ground plane, 40% diffuse / "
-                               "40% Phong / 20% refractive, two area lights, 1024x1024, max depth 16, 1 spp per step",
+                               f"40% Phong / 20% refractive, two area lights, 1024x1024, max depth 16, {PT_SPP} spp "
+                               "per step (one render call)",
                    "renderer": "wavefront (generate/extend/shade/shadow queues, CUDA-graph bounce loop)",
                    "l2": "flushed (512 MiB write) before every step", "parallelism": f"replicas x{world}"},
         "e2e": {"value": round(e2e, 2), "unit": "Mpaths/s", "h2d_bytes_per_step": 256 + 4 * 257,
                 "d2h_bytes_per_step": npix * 12},
         "megakernel": {"value": round(mk_value, 2), "unit": "Mpaths/s", "ms_per_step": round(ms_mk / args.steps, 3)},
+        "paths_per_step": npix * PT_SPP,
         "wavefront_over_megakernel": round(value / mk_value, 3),
         "gpu_launches": int(n_launch), "clocks": clk.summary(),
     }
@@ -260,38 +269,49 @@ def run_pt(args, world, rank, local):
         line["config"]["autotuned"] = {k: tuned[k] for k in ("capacity", "extend_block", "shade_block",
                                                              "ctas_per_sm", "iters_per_graph")}
     if rank == 0 and not args.quick:
-        # roofline of the dominant kernel (the extend / traversal stage), from a profiled frame
-        prof = ctx.profile_render(sid, 1, PT_DEPTH, film.data_ptr(), seed=seed + 2)
+        # roofline of the dominant kernel (the extend / traversal stage), from a
+        # profiled render of one step.  Algorithmic bytes count the reference's
+        # traversal work (every box and triangle KDTree::intersect visits: the
+        # same render with WR_RENDER_EXACT_TRAVERSAL); the time is that of the
+        # default (pruned) extend stage.
+        prof = ctx.profile_render(sid, PT_SPP, PT_DEPTH, film.data_ptr(), seed=seed + 2)
+        refw = ctx.profile_render(sid, PT_SPP, PT_DEPTH, film.data_ptr(), seed=seed + 2, exact=True)
         peak, peak_kind = peaks()
-        alg = prof["rays"] * RAY_IO_BYTES + prof["box_tests"] * BOX_BYTES + prof["tri_tests"] * TRI_BYTES
+        alg = refw["rays"] * RAY_IO_BYTES + refw["box_tests"] * BOX_BYTES + refw["tri_tests"] * TRI_BYTES
         achieved = alg / (prof["ms_extend"] / 1e3) / 1e9
         traffic = None
         pf = os.path.join(ROOT, "profiles", "wf_extend_pt.json")
         if os.path.exists(pf):
             per_ray = json.load(open(pf)).get("dram_bytes_per_ray")
             traffic = round(per_ray * prof["rays"] / max(1, prof["iterations"]), 0) if per_ray else None
+        nr = max(1, refw["rays"])
         line["roofline"] = {
             "bound": "hbm", "kernel": "k_wf_extend", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
-            "algorithmic_bytes_per_ray": round(alg / max(1, prof["rays"]), 1),
-            "box_tests_per_ray": round(prof["box_tests"] / max(1, prof["rays"]), 3),
-            "tri_tests_per_ray": round(prof["tri_tests"] / max(1, prof["rays"]), 3),
+            "algorithmic_bytes_per_ray": round(alg / nr, 1),
+            "reference_box_tests_per_ray": round(refw["box_tests"] / nr, 3),
+            "reference_tri_tests_per_ray": round(refw["tri_tests"] / nr, 3),
+            "executed_box_tests_per_ray": round(prof["box_tests"] / max(1, prof["rays"]), 3),
+            "executed_tri_tests_per_ray": round(prof["tri_tests"] / max(1, prof["rays"]), 3),
             "stage_ms": {k: round(prof[k], 2) for k in ("ms_extend", "ms_shade", "ms_shadow", "ms_generate")},
-            "rays_per_frame": prof["rays"], "iterations": prof["iterations"],
+            "rays_per_step": prof["rays"], "iterations": prof["iterations"],
+            "rays_per_s_extend": round(prof["rays"] / (prof["ms_extend"] / 1e3) / 1e6, 1),
         }
-        # time to relMSE 1e-3: the variance of a k-spp render (two independent k-spp
-        # renders) against a 256-spp wavefront render, scaled as 1/spp
-        k = 16
+        # time to relMSE 1e-3: per-pixel variance from 64 spp (sum and sum of
+        # squares), R = an independent 256-spp image; an n-spp image has
+        # relMSE = rel_1spp / n, so n = rel_1spp / 1e-3
         ref = ctx.render(sid, 256, PT_DEPTH, seed=99, mode="wavefront").astype(np.float64)
-        a = ctx.render(sid, k, PT_DEPTH, seed=11, mode="wavefront").astype(np.float64)
-        b = ctx.render(sid, k, PT_DEPTH, seed=12, mode="wavefront").astype(np.float64)
-        rel_k = relmse_variance(a, b, ref)
-        spp_needed = k * rel_k / 1e-3
+        s1, s2 = ctx.render_stats(sid, 64, PT_DEPTH, seed=11, mode="wavefront")
+        rel1, top_share = relmse_per_sample(s1, s2, 64, ref)
+        spp_needed = rel1 / 1e-3
+        ms_per_spp, ms_per_spp_mk = ms / args.steps / PT_SPP, ms_mk / args.steps / PT_SPP
         line["time_to_relmse_1e-3"] = {
-            "wavefront_s": round(spp_needed * (ms / args.steps) / 1e3, 3),
-            "megakernel_s": round(spp_needed * (ms_mk / args.steps) / 1e3, 3),
-            "spp_needed": round(spp_needed, 1), "relmse_16spp": round(rel_k, 6),
-            "formula": "mean((I-R)^2/(R^2+1e-2)), variance from two independent 16-spp renders, R = 256 spp",
+            "wavefront_s": round(spp_needed * ms_per_spp / 1e3, 3),
+            "megakernel_s": round(spp_needed * ms_per_spp_mk / 1e3, 3),
+            "spp_needed": round(spp_needed, 1), "relmse_1spp": round(rel1, 4),
+            "share_of_top_0.1pct_entries": round(top_share, 4),
+            "formula": "mean((I-R)^2/(R^2+1e-2)) = mean(Var/(R^2+1e-2))/spp; Var per pixel from 64 spp "
+                       "(sum, sum of squares), R = independent 256-spp wavefront image",
         }
         if world == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_pt(scene, args.cpu_rows or 64, os.cpu_count() or 1)
@@ -446,6 +466,66 @@ def scene_at(scene, side):
 
 
 # ---------------------------------------------------------------------------
+# relmse: each path-tracing configuration at its own spp against a converged
+# image (16,384 spp, FP64 accumulation of 256-spp FP32 passes)
+# ---------------------------------------------------------------------------
+RELMSE_CONFIGS = (  # name, scene builder, spp of the configuration, max depth
+    ("cornell_256x256", lambda S: S.cornell(256, 256), 64, 8),
+    ("mixed_1024x1024", lambda S: S.mixed_spheres(1024, 1024, seed=PT_SEED), 256, 16),
+    ("media_512x512", lambda S: S.cornell_media(512, 512), 512, 24),
+)
+CONVERGED_SPP, CONVERGED_PASS = 16384, 256
+
+
+def relmse(img, ref):
+    return float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+
+def run_relmse(args, world, rank, local):
+    import torch
+
+    from walkray_gb300 import scenes as S
+    from walkray_gb300.api import Context
+
+    torch.cuda.set_device(local)
+    ctx = Context(device=local)
+    out = {}
+    for name, build, spp, depth in RELMSE_CONFIGS:
+        scene = build(S)
+        sid = ctx.upload(scene)
+        conv_spp = args.converged_spp or CONVERGED_SPP
+        acc = None
+        t0 = time.perf_counter()
+        for k in range(conv_spp // CONVERGED_PASS):
+            img = ctx.render(sid, CONVERGED_PASS, depth, seed=7000 + k, mode="wavefront").astype(np.float64)
+            acc = img if acc is None else acc + img
+        conv = acc / (conv_spp // CONVERGED_PASS)
+        t_conv = time.perf_counter() - t0
+        row = {"spp": spp, "max_depth": depth, "converged_spp": conv_spp, "converged_s": round(t_conv, 2)}
+        for mode in ("wavefront", "megakernel"):
+            ctx.render(sid, 1, depth, seed=5, mode=mode)  # warm
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            img = ctx.render(sid, spp, depth, seed=1, mode=mode).astype(np.float64)
+            dt = time.perf_counter() - t0
+            row[mode] = {"relmse": round(relmse(img, conv), 6), "seconds": round(dt, 4),
+                         "mpaths_per_s": round(img.shape[0] * img.shape[1] * spp / dt / 1e6, 2)}
+        # the variance part alone: relMSE of the image against itself rendered again
+        b = ctx.render(sid, spp, depth, seed=2, mode="wavefront").astype(np.float64)
+        a = ctx.render(sid, spp, depth, seed=1, mode="wavefront").astype(np.float64)
+        row["relmse_between_two_renders_div2"] = round(relmse(a, b) / 2, 6)
+        out[name] = row
+        ctx.release(sid)
+    ctx.close()
+    return {"metric": "relMSE at each configuration's spp vs a converged image", "value": None,
+            "unit": "relMSE", "n_gpus": world, "higher_is_better": False, "dtype": "f32",
+            "data": "synthetic (seeded scene generators)", "configs": out,
+            "formula": "mean over pixels and channels of (I-R)^2/(R^2+1e-2); R = 16,384-spp wavefront render "
+                       "accumulated in FP64 from 256-spp FP32 passes (seeds 7000+), I = one render at the "
+                       "configuration's spp (seed 1); times are wall-clock through wr_render (host image)"}
+
+
+# ---------------------------------------------------------------------------
 # kd: closest-hit microbenchmark
 # ---------------------------------------------------------------------------
 KD_RAYS = 1 << 24
@@ -569,7 +649,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["pt", "kd", "serve"], default=os.environ.get("WR_BENCH_WORKLOAD", "pt"))
+    ap.add_argument("--workload", choices=["pt", "kd", "serve", "relmse"], default=os.environ.get("WR_BENCH_WORKLOAD", "pt"))
     ap.add_argument("--tune", action="store_true", help="run the wavefront autotuner first (pt)")
     ap.add_argument("--quick", action="store_true", help="skip the roofline profile, relMSE and CPU legs (pt)")
     ap.add_argument("--cpu-sample", type=int, default=0)
@@ -578,6 +658,7 @@ def main():
     ap.add_argument("--kd-rays", type=int, default=1 << 24, help="rays per step (kd); smaller for ncu captures")
     ap.add_argument("--pt-size", type=int, default=PT_SIZE, help="image side (pt); smaller for ncu captures")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window of the request stream (serve)")
+    ap.add_argument("--converged-spp", type=int, default=0, help="spp of the converged image (relmse)")
     args = ap.parse_args()
     globals()["PT_SIZE"] = args.pt_size
     globals()["KD_RAYS"] = args.kd_rays
@@ -597,7 +678,7 @@ def main():
     from walkray_gb300 import build
 
     build.build_lib()
-    run = {"pt": run_pt, "kd": run_kd, "serve": run_serve}[args.workload]
+    run = {"pt": run_pt, "kd": run_kd, "serve": run_serve, "relmse": run_relmse}[args.workload]
     line = run(args, world, rank, local)
     if rank == 0:
         print(json.dumps(line), flush=True)

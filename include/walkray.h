@@ -312,6 +312,9 @@ typedef struct wr_wavefront_config {
     int32_t shade_block;     /* threads per CTA of the shade / generate stages */
     int32_t ctas_per_sm;     /* persistent CTAs per SM, 0 = as many as fit */
     int32_t iters_per_graph; /* bounce-loop iterations (pairs) per CUDA-graph launch */
+    int32_t refill_min;      /* traversal: idle lanes of a warp that trigger a ray refill (1..32, 0 = default) */
+    int32_t leaf_min;        /* traversal: lanes holding leaves that start a warp's leaf tests (1..32,
+                                0 = default); both also apply to wr_trace_closest */
     double mpaths_per_s;     /* filled by wr_autotune */
 } wr_wavefront_config;
 

@@ -79,7 +79,10 @@ def test_wavefront_equals_megakernel(ctx):
     sid = ctx.upload(s)
     a = ctx.render(sid, 32, 16, seed=3, mode="megakernel")
     ctx.set_wavefront_config(capacity=1 << 14, iters_per_graph=2)  # small queue: many refills
-    b = ctx.render(sid, 32, 16, seed=3, mode="wavefront")
+    try:
+        b = ctx.render(sid, 32, 16, seed=3, mode="wavefront")
+    finally:
+        ctx.set_wavefront_config(capacity=1 << 22)
     assert np.allclose(a, b, rtol=1e-4, atol=1e-5), np.abs(a - b).max()
     ctx.release(sid)
 

@@ -63,6 +63,25 @@ def test_filtered_trace_matches_reference_golden(ctx):
     ctx.release(sid)
 
 
+@pytest.mark.parametrize("refill_min,leaf_min", [(1, 1), (32, 32), (4, 3)])
+def test_traversal_loop_settings_do_not_change_hits(ctx, refill_min, leaf_min):
+    """The warp loop's refill threshold and leaf postponement change only the
+    order of work: filtered hits stay equal to the reference's."""
+    s = make_golden.golden_scenes()["mixed_l2"]
+    g = np.load(os.path.join(GOLDEN, "trace_filtered.npz"))
+    rays, ids = make_golden.filtered_rays(s, 32768, seed=5)
+    sid = ctx.upload(s)
+    ctx.set_wavefront_config(capacity=1 << 22, refill_min=refill_min, leaf_min=leaf_min)
+    try:
+        h = ctx.trace_closest(sid, rays, ids[:, 0], ids[:, 1])
+    finally:
+        ctx.set_wavefront_config(capacity=1 << 22)
+    assert np.array_equal(h["tri"], g["tri"])
+    hit = h["tri"] != NO_HIT
+    assert np.array_equal(h["t"][hit].view(np.uint32), g["t"][hit].view(np.uint32))
+    ctx.release(sid)
+
+
 def test_full_size_icosphere_matches_oracle(ctx):
     """1,310,720 triangles, 2^24 rays: every id and distance bit-identical to
     the oracle (which is pinned to the reference in test_oracle)."""

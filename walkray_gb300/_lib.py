@@ -91,7 +91,7 @@ class wr_render_desc(C.Structure):
 
 class wr_wavefront_config(C.Structure):
     _fields_ = [("capacity", C.c_uint32), ("extend_block", C.c_int32), ("shade_block", C.c_int32),
-                ("ctas_per_sm", C.c_int32), ("iters_per_graph", C.c_int32), ("mpaths_per_s", C.c_double)]
+                ("ctas_per_sm", C.c_int32), ("iters_per_graph", C.c_int32), ("refill_min", C.c_int32), ("leaf_min", C.c_int32), ("mpaths_per_s", C.c_double)]
 
 
 class wr_serve_desc(C.Structure):

@@ -164,8 +164,13 @@ class Context:
         return {k: getattr(p, k) for k, _ in L.wr_render_profile._fields_}
 
     def set_wavefront_config(self, capacity: int, extend_block: int = 128, shade_block: int = 128,
-                             ctas_per_sm: int = 0, iters_per_graph: int = 4) -> None:
-        c = L.wr_wavefront_config(capacity, extend_block, shade_block, ctas_per_sm, iters_per_graph, 0.0)
+                             ctas_per_sm: int = 0, iters_per_graph: int = 4, refill_min: int = 0,
+                             leaf_min: int = 0) -> None:
+        """Queue sizes and block shapes of the wavefront renderer; refill_min and
+        leaf_min (0 = defaults) tune the warp traversal loop of both the
+        extend stage and trace_closest."""
+        c = L.wr_wavefront_config(capacity, extend_block, shade_block, ctas_per_sm, iters_per_graph, refill_min,
+                                  leaf_min, 0.0)
         self._check(self.lib.wr_set_wavefront_config(self.h, C.byref(c)))
 
     def autotune(self, sid: int, spp_per_trial: int, max_path_len: int) -> dict:

@@ -239,8 +239,9 @@ int wr_trace_closest_device(wr_ctx* ctx, wr_scene_id id, const float* d_rays, ui
     unsigned long long* counter = ctx->scratch_words.as<unsigned long long>();
     unsigned int* err = reinterpret_cast<unsigned int*>(counter + 1);
     WR_CUDA(ctx, cudaMemsetAsync(err, 0, sizeof(unsigned int), s));
+    const TraceTune tt = trace_tune_of(ctx);
     WR_CUDA(ctx, launch_trace_closest(sc->tree, d_rays, n, d_inside, d_contact, d_hits, counter, err, ctx->num_sms,
-                                      ctx->trace_prune, s, &ctx->last_trace_blocks));
+                                      ctx->trace_prune, s, &ctx->last_trace_blocks, &tt));
     ctx->kernel_launches++;
     return WR_OK;
 }
@@ -272,9 +273,10 @@ int wr_trace_closest(wr_ctx* ctx, wr_scene_id id, const float* rays, uint64_t n,
     unsigned long long* counter = ctx->scratch_words.as<unsigned long long>();
     unsigned int* err = reinterpret_cast<unsigned int*>(counter + 1);
     WR_CUDA(ctx, cudaMemsetAsync(err, 0, sizeof(unsigned int), s));
+    const TraceTune tt = trace_tune_of(ctx);
     WR_CUDA(ctx, launch_trace_closest(sc->tree, ctx->rays.as<float>(), n, filtered ? ctx->inside.as<int32_t>() : nullptr,
                                       filtered ? ctx->contact.as<int32_t>() : nullptr, ctx->hits.as<wr_hit>(), counter,
-                                      err, ctx->num_sms, ctx->trace_prune, s, &ctx->last_trace_blocks));
+                                      err, ctx->num_sms, ctx->trace_prune, s, &ctx->last_trace_blocks, &tt));
     ctx->kernel_launches++;
     WR_CUDA(ctx, cudaMemcpyAsync(hits, ctx->hits.p, n * sizeof(wr_hit), cudaMemcpyDeviceToHost, s));
     unsigned int herr = 0;

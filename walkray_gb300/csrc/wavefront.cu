@@ -5,12 +5,12 @@
 #include <map>
 
 #include "wavefront.h"
+#include "wr_warp_trace.cuh"
 
 namespace wr {
 
 constexpr uint32_t WF_MAX_JOBS = 256;
 constexpr uint32_t WF_MAX_SCENES = 64;
-constexpr int WF_TRACE_STEPS = 8;
 
 uint32_t wf_max_jobs() { return WF_MAX_JOBS; }
 
@@ -124,123 +124,50 @@ __global__ void __launch_bounds__(128) k_wf_shadow(const RenderScene* __restrict
 }
 
 // extend: closest hit of every queued ray; the eye ray (contact == camera)
-// without a filter, all others with NoSelfCondition
+// without a filter, all others with NoSelfCondition.  Rays of different jobs
+// (and scenes) share the queue; each lane follows its own ray's tree.
+struct ExtendSrc {
+    const RenderScene* __restrict__ scenes;
+    const WfJob* __restrict__ jobs;
+    WfSide X;
+    int2* __restrict__ hits;
+    unsigned long long* __restrict__ stats;
+
+    __device__ __forceinline__ void load(uint64_t id, TraceLane& L, uint32_t* stack, int stride) {
+        const float4 a0 = X.a0[id], a1 = X.a1[id];
+        const int4 ids = X.ids[id];
+        const WfJob& J = jobs[ids.z];
+        const DevTree& T = scenes[J.scene].tree;
+        L.pairs = T.pairs;
+        L.tris = T.tris;
+        L.q = make_rayq(mk(a0.x, a0.y, a0.z), mk(a1.x, a1.y, a1.z), T.scene_mag);
+        L.q.pf = prune_factor(J.flags);
+        L.inside = ids.x;
+        L.contact = ids.y;
+        L.filt = ids.y != CAMERA_OBJ;
+        const Box root{T.root_lo[0], T.root_lo[1], T.root_lo[2], T.root_hi[0], T.root_hi[1], T.root_hi[2]};
+        lane_start(L, root, T.root_w0, T.root_w1, stack, stride);
+    }
+    __device__ __forceinline__ void store(uint64_t id, const TraceLane& L) {
+        hits[id] = make_int2(L.h.slot, __float_as_int(L.h.t));
+        if (stats) {
+            atomicAdd(stats + 0, 1ull);
+            atomicAdd(stats + 1, (unsigned long long)L.n_box);
+            atomicAdd(stats + 2, (unsigned long long)L.n_tri);
+        }
+    }
+};
+
+template <bool STATS>
 __global__ void __launch_bounds__(128) k_wf_extend(const RenderScene* __restrict__ scenes,
                                                      const WfJob* __restrict__ jobs, WfSide X, int2* __restrict__ hits,
                                                      unsigned long long* __restrict__ work, int stack_cap,
-                                                     unsigned int* __restrict__ err,
+                                                     TraceTune tune, unsigned int* __restrict__ err,
                                                      unsigned long long* __restrict__ stats) {
     extern __shared__ uint32_t s_stack[];
-    uint32_t* stack = s_stack + threadIdx.x;
-    const int stride = blockDim.x;
-    const unsigned lane = threadIdx.x & 31u;
-    const unsigned lt_mask = (1u << lane) - 1u;
     const uint64_t n = (uint64_t)X.counts[0] + X.counts[1];
-
-    bool active = false, exhausted = false;
-    uint64_t rid = 0;
-    RayQ q;
-    int in_obj = -1, ct_obj = -1;
-    bool filt = false;
-    DevTree T;
-    Hit h;
-    int sp = 0;
-    uint32_t n_box = 0, n_tri = 0;  // work counters (profiling launches only)
-    for (;;) {
-        const unsigned need = __ballot_sync(0xffffffffu, !active && !exhausted);
-        if (need) {
-            const int leader = __ffs(need) - 1;
-            unsigned long long base = 0;
-            if ((int)lane == leader) base = atomicAdd(work, (unsigned long long)__popc(need));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (!active && !exhausted) {
-                const uint64_t id = base + __popc(need & lt_mask);
-                if (id < n) {
-                    rid = id;
-                    const float4 a0 = X.a0[id], a1 = X.a1[id];
-                    const int4 ids = X.ids[id];
-                    const WfJob& J = jobs[ids.z];
-                    T = scenes[J.scene].tree;
-                    q = make_rayq(mk(a0.x, a0.y, a0.z), mk(a1.x, a1.y, a1.z), T.scene_mag);
-                    q.pf = prune_factor(J.flags);
-                    in_obj = ids.x;
-                    ct_obj = ids.y;
-                    filt = ct_obj != CAMERA_OBJ;
-                    h.t = __int_as_float(0x7f800000);
-                    h.slot = -1;
-                    sp = 0;
-                    n_box = 1;
-                    n_tri = 0;
-                    float tn;
-                    if (box_pred(root_box(T), q, &tn)) {
-                        if (T.root_w1 & LEAF_FLAG) {
-                            n_tri += T.root_w1 & ~LEAF_FLAG;
-                            if (filt) leaf_test<true>(T, T.root_w0, T.root_w1 & ~LEAF_FLAG, q, in_obj, ct_obj, h);
-                            else leaf_test<false>(T, T.root_w0, T.root_w1 & ~LEAF_FLAG, q, in_obj, ct_obj, h);
-                        } else {
-                            stack[(sp++) * stride] = T.root_w0;
-                        }
-                    }
-                    active = true;
-                } else {
-                    exhausted = true;
-                }
-            }
-        }
-        if (__all_sync(0xffffffffu, !active)) break;
-        if (active) {
-            for (int it = 0; it < WF_TRACE_STEPS && sp > 0; ++it) {
-                const uint32_t pi = stack[(--sp) * stride];
-                const NodePair* P = T.pairs + pi;
-                const float4 A = ldg4(&P->a), B = ldg4(&P->b), C = ldg4(&P->c);
-                const uint4 W = ldg4u(&P->t);
-                float tl, tr;
-                bool hl = box_pred(Box{A.x, A.y, A.z, A.w, B.x, B.y}, q, &tl);
-                bool hr = box_pred(Box{B.z, B.w, C.x, C.y, C.z, C.w}, q, &tr);
-                n_box += 2;
-                {  // front-to-back pruning against the closest hit so far
-                    const float lim = h.t * q.pf + q.M;
-                    hl = hl && !(tl > lim);
-                    hr = hr && !(tr > lim);
-                }
-                if (hl && (W.y & LEAF_FLAG)) {
-                    n_tri += W.y & ~LEAF_FLAG;
-                    if (filt) leaf_test<true>(T, W.x, W.y & ~LEAF_FLAG, q, in_obj, ct_obj, h);
-                    else leaf_test<false>(T, W.x, W.y & ~LEAF_FLAG, q, in_obj, ct_obj, h);
-                    hl = false;
-                }
-                if (hr && (W.w & LEAF_FLAG)) {
-                    n_tri += W.w & ~LEAF_FLAG;
-                    if (filt) leaf_test<true>(T, W.z, W.w & ~LEAF_FLAG, q, in_obj, ct_obj, h);
-                    else leaf_test<false>(T, W.z, W.w & ~LEAF_FLAG, q, in_obj, ct_obj, h);
-                    hr = false;
-                }
-                if (sp + 2 > stack_cap) {
-                    atomicOr(err, 1u);
-                    sp = 0;
-                    break;
-                }
-                if (hl && hr) {
-                    const bool lnear = tl <= tr;
-                    stack[(sp++) * stride] = lnear ? W.z : W.x;
-                    stack[(sp++) * stride] = lnear ? W.x : W.z;
-                } else if (hl) {
-                    stack[(sp++) * stride] = W.x;
-                } else if (hr) {
-                    stack[(sp++) * stride] = W.z;
-                }
-            }
-            if (sp == 0) {
-                hits[rid] = make_int2(h.slot, __float_as_int(h.t));
-                active = false;
-                if (stats) {
-                    atomicAdd(stats + 0, 1ull);
-                    atomicAdd(stats + 1, (unsigned long long)n_box);
-                    atomicAdd(stats + 2, (unsigned long long)n_tri);
-                }
-            }
-        }
-    }
+    ExtendSrc src{scenes, jobs, X, hits, STATS ? stats : nullptr};
+    warp_trace<true, STATS>(src, n, work, tune, s_stack + threadIdx.x, blockDim.x, stack_cap, err);
 }
 
 // shade: one bounce per path; survivors compacted into Y, finished paths to the film
@@ -419,7 +346,8 @@ int wf_engine_get(wr_ctx* ctx, const WfConfig& cfg, WfEngine** out) {
     WfEngine* cur = static_cast<WfEngine*>(ctx->wavefront.get());
     if (cur && cur->cfg.capacity == cfg.capacity && cur->cfg.extend_block == cfg.extend_block &&
         cur->cfg.shade_block == cfg.shade_block && cur->cfg.ctas_per_sm == cfg.ctas_per_sm &&
-        cur->cfg.iters_per_graph == cfg.iters_per_graph) {
+        cur->cfg.iters_per_graph == cfg.iters_per_graph && cur->cfg.trace.refill_min == cfg.trace.refill_min &&
+        cur->cfg.trace.leaf_min == cfg.trace.leaf_min) {
         *out = cur;
         return WR_OK;
     }
@@ -540,12 +468,15 @@ int wf_update_jobs(wr_ctx* ctx, WfEngine* E, const std::vector<WfSlotUpdate>& up
             E->stack_cap = cap;
             E->smem_extend = (size_t)cap * E->cfg.extend_block * sizeof(uint32_t);
             if (E->smem_extend > 200 * 1024) return set_error(ctx, WR_ERR_UNSUPPORTED, "tree too deep for the stack");
-            if (E->smem_extend > 48 * 1024)
-                WR_CUDA(ctx, cudaFuncSetAttribute(k_wf_extend, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            if (E->smem_extend > 48 * 1024) {
+                WR_CUDA(ctx, cudaFuncSetAttribute(k_wf_extend<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                   (int)E->smem_extend));
+                WR_CUDA(ctx, cudaFuncSetAttribute(k_wf_extend<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  (int)E->smem_extend));
+            }
             int per_sm = 0;
-            WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_extend, E->cfg.extend_block,
-                                                                       E->smem_extend));
+            WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_extend<false>,
+                                                                       E->cfg.extend_block, E->smem_extend));
             if (E->cfg.ctas_per_sm > 0) per_sm = std::min(per_sm, E->cfg.ctas_per_sm);
             E->grid_extend = ctx->num_sms * std::max(1, per_sm);
             E->smem_shadow = E->smem_extend;
@@ -575,8 +506,8 @@ static void enqueue_iteration(WfEngine* E, int x, cudaStream_t s, cudaEvent_t* e
     WfJobCounters* cnt = E->counters.as<WfJobCounters>();
     k_wf_reset<<<1, 1, 0, s>>>(E->side[y], E->work.as<unsigned long long>(), E->shadow.count);
     if (ev) cudaEventRecord(ev[0], s);
-    k_wf_extend<<<E->grid_extend, E->cfg.extend_block, E->smem_extend, s>>>(
-        scenes, jobs, E->side[x], E->hits.as<int2>(), E->work.as<unsigned long long>(), E->stack_cap,
+    (stats ? k_wf_extend<true> : k_wf_extend<false>)<<<E->grid_extend, E->cfg.extend_block, E->smem_extend, s>>>(
+        scenes, jobs, E->side[x], E->hits.as<int2>(), E->work.as<unsigned long long>(), E->stack_cap, E->cfg.trace,
         E->err_word.as<unsigned int>(), stats);
     if (ev) cudaEventRecord(ev[1], s);
     k_wf_shade<<<E->grid_shade, E->cfg.shade_block, 0, s>>>(scenes, jobs, cnt, E->side[x], E->hits.as<int2>(),

@@ -70,11 +70,12 @@ struct WfShadow {
 };
 
 struct WfConfig {
-    uint32_t capacity = 1u << 21;  // paths in flight
+    uint32_t capacity = 1u << 22;  // paths in flight (4M x 128 B of state per side)
     int extend_block = 128;
     int shade_block = 128;
     int ctas_per_sm = 0;           // 0 = occupancy calculator
     int iters_per_graph = 4;       // ping-pong pairs per graph launch
+    TraceTune trace = default_trace_tune();  // warp traversal loop of the extend stage
 };
 
 struct WfEngine;

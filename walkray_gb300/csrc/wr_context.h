@@ -81,6 +81,7 @@ struct wr_ctx {
     // wavefront configuration chosen by wr_autotune (0 = defaults)
     uint32_t wf_capacity = 0;
     int wf_extend_block = 0, wf_shade_block = 0, wf_ctas_per_sm = 0, wf_iters = 0;
+    int trace_refill_min = 0, trace_leaf_min = 0;  // warp traversal loop (0 = defaults)
 };
 
 namespace wr {
@@ -90,6 +91,13 @@ void wf_forget_scene(wr_ctx* ctx, const RenderData* rd);
 int set_error(wr_ctx* ctx, int code, const std::string& msg);
 int cuda_error(wr_ctx* ctx, cudaError_t e, const char* what);
 SceneGPU* find_scene(wr_ctx* ctx, wr_scene_id id);
+// the traversal loop's knobs: set by wr_set_wavefront_config / wr_autotune, else defaults
+inline TraceTune trace_tune_of(const wr_ctx* ctx) {
+    TraceTune t = default_trace_tune();
+    if (ctx->trace_refill_min) t.refill_min = ctx->trace_refill_min;
+    if (ctx->trace_leaf_min) t.leaf_min = ctx->trace_leaf_min;
+    return t;
+}
 }  // namespace wr
 
 #define WR_CUDA(ctx, call)                                        \

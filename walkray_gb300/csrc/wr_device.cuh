@@ -53,6 +53,13 @@ struct DevTree {
     uint32_t num_pairs, num_slots;
 };
 
+// Knobs of the warp-persistent traversal loop (wr_warp_trace.cuh)
+struct TraceTune {
+    int refill_min;  // refill idle lanes once at least this many are idle (or none is busy)
+    int leaf_min;    // lanes holding postponed leaves that start the warp's leaf phase
+};
+inline TraceTune default_trace_tune() { return TraceTune{8, 8}; }  // fastest of a sweep on GB300
+
 struct f3 {
     float x, y, z;
 };

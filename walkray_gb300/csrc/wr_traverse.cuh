@@ -74,17 +74,6 @@ __device__ __forceinline__ bool face_pass(const Box& bx, const RayQ& q) {
     return dist >= 0.f && lo_<B>(bx) <= pb && hi_<B>(bx) >= pb && lo_<C>(bx) <= pc && hi_<C>(bx) >= pc;
 }
 
-__device__ __forceinline__ bool face_pass_dyn(int i, const Box& bx, const RayQ& q) {
-    switch (i) {
-        case 0: return face_pass<0>(bx, q);
-        case 1: return face_pass<1>(bx, q);
-        case 2: return face_pass<2>(bx, q);
-        case 3: return face_pass<3>(bx, q);
-        case 4: return face_pass<4>(bx, q);
-        default: return face_pass<5>(bx, q);
-    }
-}
-
 __device__ __forceinline__ bool all_faces(const Box& bx, const RayQ& q) {
     return face_pass<0>(bx, q) || face_pass<1>(bx, q) || face_pass<2>(bx, q) || face_pass<3>(bx, q) ||
            face_pass<4>(bx, q) || face_pass<5>(bx, q);
@@ -104,14 +93,19 @@ __device__ __forceinline__ bool face_pass_sel(int a, bool hi, const Box& bx, con
     const float oC = pick3(c, q.o.x, q.o.y, q.o.z), dC = pick3(c, q.d.x, q.d.y, q.d.z);
     const float loB = pick3(b, bx.lx, bx.ly, bx.lz), hiB = pick3(b, bx.hx, bx.hy, bx.hz);
     const float loC = pick3(c, bx.lx, bx.ly, bx.lz), hiC = pick3(c, bx.hx, bx.hy, bx.hz);
-    if (dA == 0.f) return false;
+    // a zero direction component skips the face (kdtree.cpp:51); the division
+    // is still evaluated so that every lane runs the same instructions
     const float dist = (plane - oA) / dA;
     const float pb = oB + dist * dB;
     const float pc = oC + dist * dC;
-    return dist >= 0.f && loB <= pb && hiB >= pb && loC <= pc && hiC >= pc;
+    return (dA != 0.f) & (dist >= 0.f) & (loB <= pb) & (hiB >= pb) & (loC <= pc) & (hiC >= pc);
 }
 
 // The reference box predicate; *tnear gets the grown-box entry distance.
+// Straight-line code but for one rare branch: the slab test on the grown box
+// and the reference test of the likely face are both evaluated, and only a
+// box that the slab test keeps but that face rejects (or a NaN interval)
+// goes to the six-face test.
 __device__ __forceinline__ bool box_pred(const Box& bx, const RayQ& q, float* tnear) {
     float ax = (bx.lx - q.olo.x) * q.inv.x, bxx = (bx.hx - q.ohi.x) * q.inv.x;
     float ay = (bx.ly - q.olo.y) * q.inv.y, by = (bx.hy - q.ohi.y) * q.inv.y;
@@ -123,12 +117,10 @@ __device__ __forceinline__ bool box_pred(const Box& bx, const RayQ& q, float* tn
     float tn = fmaxf(nx, fmaxf(ny, nz));
     float tf = fminf(fx, fminf(fy, fz));
     *tnear = tn;
-    if (!(tn <= tf) || tf < 0.f) {
-        // grown box missed: every reference face test fails.  A NaN interval
-        // (not expected) is decided by the reference test itself.
-        if (tn == tn && tf == tf) return false;
-        return all_faces(bx, q);
-    }
+    // a box the grown box misses fails every reference face test (see the
+    // header); a NaN interval (not expected) is left to the reference test
+    const bool slab = (tn <= tf) & (tf >= 0.f);
+    const bool nan = (tn != tn) | (tf != tf);
     // entry face (axis of the largest near distance), or the exit face (axis
     // of the smallest far distance) when the origin is inside
     const bool entry = tn >= 0.f;
@@ -136,8 +128,9 @@ __device__ __forceinline__ bool box_pred(const Box& bx, const RayQ& q, float* tn
     const int xa = (fx <= fy && fx <= fz) ? 0 : (fy <= fz ? 1 : 2);
     const int a = entry ? ea : xa;
     const bool pos = pick3(a, q.d.x, q.d.y, q.d.z) > 0.f;
-    if (face_pass_sel(a, entry ? !pos : pos, bx, q)) return true;
-    return all_faces(bx, q);
+    const bool face = face_pass_sel(a, entry ? !pos : pos, bx, q);
+    if ((slab & !face) | nan) return all_faces(bx, q);
+    return slab;
 }
 
 // KDTree::intersect(ray, tri) geometric part (kdtree.cpp:279-301); returns
@@ -203,6 +196,24 @@ __device__ __forceinline__ void leaf_test(const DevTree& T, uint32_t first, uint
     }
 }
 
+// The same with the filter chosen per ray (eye rays are traced without one)
+__device__ __forceinline__ void leaf_test_dyn(const TriRec* tris, uint32_t first, uint32_t count, const RayQ& q,
+                                              bool filt, int inside, int contact, Hit& h) {
+    for (uint32_t k = 0; k < count; k++) {
+        const int slot = (int)(first + k);
+        const TriRec* tr = tris + slot;
+        const float4 a = ldg4(&tr->v0), b = ldg4(&tr->v1), c = ldg4(&tr->v2);
+        const f3 v0 = xyz(a), v1 = xyz(b), v2 = xyz(c);
+        const float t = tri_test(v0, v1, v2, q);
+        if (t >= 0.f && (t < h.t || (t == h.t && slot > h.slot))) {
+            if (filt && !noself_legal(inside, contact, (int)__float_as_uint(b.w), q.d, face_normal(v0, v1, v2)))
+                continue;
+            h.t = t;
+            h.slot = slot;
+        }
+    }
+}
+
 // Closest hit.  `stack` is this thread's stack: entries at stack[k * stride],
 // at most `cap` of them (cap >= tree depth + 2 always suffices; a traversal
 // that would exceed it stops and sets bit 0 of *err instead of writing past).
@@ -234,16 +245,16 @@ __device__ __forceinline__ Hit trace_closest(const DevTree& T, const RayQ& q, in
             hl = hl && !(tl > lim);
             hr = hr && !(tr > lim);
         }
-        // leaves first (they can tighten the bound), then push internal
-        // children far-first so the near one is popped next
-        if (hl && (W.y & LEAF_FLAG)) {
-            leaf_test<FILTERED>(T, W.x, W.y & ~LEAF_FLAG, q, inside, contact, h);
-            hl = false;
+        // leaves first (they can tighten the bound), both through one code
+        // path; then push internal children far-first so the near one is
+        // popped next
+        const bool ll = hl && (W.y & LEAF_FLAG), lr = hr && (W.w & LEAF_FLAG);
+        for (int k = 0, nk = (int)ll + (int)lr; k < nk; k++) {
+            const bool right = k == 1 || !ll;
+            leaf_test<FILTERED>(T, right ? W.z : W.x, (right ? W.w : W.y) & ~LEAF_FLAG, q, inside, contact, h);
         }
-        if (hr && (W.w & LEAF_FLAG)) {
-            leaf_test<FILTERED>(T, W.z, W.w & ~LEAF_FLAG, q, inside, contact, h);
-            hr = false;
-        }
+        hl = hl && !ll;
+        hr = hr && !lr;
         if (sp + 2 > cap) {
             atomicOr(err, 1u);
             break;
