@@ -11,13 +11,25 @@
 //  * Its winner is the smallest t, ties to the right child / first in a leaf;
 //    with the slot layout of wr_device.cuh that is "smallest t, then largest
 //    slot", an order-free rule.
-//  * The predicate itself is evaluated cheaply: a slab test on the box grown
-//    by a margin M that covers the predicate's rounding proves most misses
-//    (a box missed by the grown box fails all six reference face tests); for
-//    the rest the reference face test is run on the most likely face first
-//    (entry face, or exit face when the origin is inside) and on all six only
-//    if that one fails.  Every "pass" is decided by the reference's own
-//    arithmetic, every "fail" either by it or by the proof above.
+//  * The predicate itself is evaluated cheaply, by two slab tests: one on the
+//    box grown by a margin M, one on the box shrunk by M.  M (about 33 units
+//    of FP32 rounding of the coordinates involved) is larger than the error
+//    of the reference's face test and of the slab tests themselves, so:
+//      - a ray that misses the grown box fails all six reference face tests
+//        (each of them needs a plane point within rounding of the box);
+//      - a ray that passes the shrunk box, and whose entry axis is
+//        unambiguous (the grown-box entry distance T1 = max of the grown
+//        near distances is at least the shrunk near distance of every other
+//        axis), enters the real box through a point at least ~M inside the
+//        entry face on both other axes, at a distance >= 0; the reference's
+//        test of that face therefore passes.  With the origin inside (T1 <
+//        0) the same holds for the exit face (U1 = min of the grown far
+//        distances at most the shrunk far distance of every other axis).
+//    Everything else (a ray within ~M of an edge, a box thinner than 2M,
+//    a NaN) runs the reference's face test itself: the likely face first,
+//    all six if that one fails.
+//    Rays must be finite; a NaN or infinite direction gets no hit here, as
+//    in the reference (its triangle test fails for it).
 //  * Optional pruning (PRUNE, used by the renderers): a child whose grown-box
 //    entry distance exceeds q.pf times the best hit (plus M) is skipped.  A
 //    triangle's hit lies inside its box, so this keeps the closest hit unless
@@ -31,8 +43,12 @@ namespace wr {
 
 struct RayQ {
     f3 o, d, inv;
-    f3 olo, ohi;  // o + M and o - M: the slab planes of the box grown by M
-    float M;      // grown-box margin for this ray
+    // per axis, with s = +1 where the direction is positive (inv > 0), else -1:
+    // gno = o + s M and gfo = o - s M.  (near corner - gno) * inv is the
+    // grown-box near distance, (near corner - gfo) * inv the shrunk one, and
+    // the far corner with the roles swapped.
+    f3 gno, gfo;
+    float M;      // box margin for this ray
     float pf;     // pruning: boxes entered beyond pf * (closest hit) + M are skipped
 };
 
@@ -45,8 +61,10 @@ __device__ __forceinline__ RayQ make_rayq(f3 o, f3 d, float scene_mag) {
     // reference predicate rounding <= ~4.1 eps (B + |o|), slab test rounding
     // <= ~4 eps (B + |o|) (eps = 2^-24); 2e-6 is ~33 eps
     q.M = 2e-6f * (scene_mag + om) + 1e-30f;
-    q.olo = mk(o.x + q.M, o.y + q.M, o.z + q.M);
-    q.ohi = mk(o.x - q.M, o.y - q.M, o.z - q.M);
+    const float lo_x = o.x + q.M, lo_y = o.y + q.M, lo_z = o.z + q.M;
+    const float hi_x = o.x - q.M, hi_y = o.y - q.M, hi_z = o.z - q.M;
+    q.gno = mk(q.inv.x > 0.f ? lo_x : hi_x, q.inv.y > 0.f ? lo_y : hi_y, q.inv.z > 0.f ? lo_z : hi_z);
+    q.gfo = mk(q.inv.x > 0.f ? hi_x : lo_x, q.inv.y > 0.f ? hi_y : lo_y, q.inv.z > 0.f ? hi_z : lo_z);
     q.pf = 1.001f;
     return q;
 }
@@ -101,36 +119,71 @@ __device__ __forceinline__ bool face_pass_sel(int a, bool hi, const Box& bx, con
     return (dA != 0.f) & (dist >= 0.f) & (loB <= pb) & (hiB >= pb) & (loC <= pc) & (hiC >= pc);
 }
 
-// The reference box predicate; *tnear gets the grown-box entry distance.
-// Straight-line code but for one rare branch: the slab test on the grown box
-// and the reference test of the likely face are both evaluated, and only a
-// box that the slab test keeps but that face rejects (or a NaN interval)
-// goes to the six-face test.
-__device__ __forceinline__ bool box_pred(const Box& bx, const RayQ& q, float* tnear) {
-    float ax = (bx.lx - q.olo.x) * q.inv.x, bxx = (bx.hx - q.ohi.x) * q.inv.x;
-    float ay = (bx.ly - q.olo.y) * q.inv.y, by = (bx.hy - q.ohi.y) * q.inv.y;
-    float az = (bx.lz - q.olo.z) * q.inv.z, bz = (bx.hz - q.ohi.z) * q.inv.z;
-    // fminf/fmaxf drop NaN (0 * inf on a zero direction component): no constraint
-    float nx = fminf(ax, bxx), fx = fmaxf(ax, bxx);
-    float ny = fminf(ay, by), fy = fmaxf(ay, by);
-    float nz = fminf(az, bz), fz = fmaxf(az, bz);
-    float tn = fmaxf(nx, fmaxf(ny, nz));
-    float tf = fminf(fx, fminf(fy, fz));
-    *tnear = tn;
-    // a box the grown box misses fails every reference face test (see the
-    // header); a NaN interval (not expected) is left to the reference test
-    const bool slab = (tn <= tf) & (tf >= 0.f);
-    const bool nan = (tn != tn) | (tf != tf);
-    // entry face (axis of the largest near distance), or the exit face (axis
-    // of the smallest far distance) when the origin is inside
-    const bool entry = tn >= 0.f;
+// The reference's test run on the likely face (entry face, or the exit face
+// when the grown-box entry is behind the origin), on all six if that fails:
+// exactly BoundingBox::intersect's pass/fail.
+__device__ __forceinline__ bool box_exact(const Box& bx, const RayQ& q) {
+    const bool px = q.inv.x > 0.f, py = q.inv.y > 0.f, pz = q.inv.z > 0.f;
+    const float nx = ((px ? bx.lx : bx.hx) - q.gno.x) * q.inv.x, fx = ((px ? bx.hx : bx.lx) - q.gfo.x) * q.inv.x;
+    const float ny = ((py ? bx.ly : bx.hy) - q.gno.y) * q.inv.y, fy = ((py ? bx.hy : bx.ly) - q.gfo.y) * q.inv.y;
+    const float nz = ((pz ? bx.lz : bx.hz) - q.gno.z) * q.inv.z, fz = ((pz ? bx.hz : bx.lz) - q.gfo.z) * q.inv.z;
+    const bool entry = fmaxf(nx, fmaxf(ny, nz)) >= 0.f;
     const int ea = (nx >= ny && nx >= nz) ? 0 : (ny >= nz ? 1 : 2);
     const int xa = (fx <= fy && fx <= fz) ? 0 : (fy <= fz ? 1 : 2);
     const int a = entry ? ea : xa;
     const bool pos = pick3(a, q.d.x, q.d.y, q.d.z) > 0.f;
-    const bool face = face_pass_sel(a, entry ? !pos : pos, bx, q);
-    if ((slab & !face) | nan) return all_faces(bx, q);
-    return slab;
+    if (face_pass_sel(a, entry ? !pos : pos, bx, q)) return true;
+    return all_faces(bx, q);
+}
+
+enum : int { BOX_MISS = 0, BOX_HIT = 1, BOX_UNSURE = 2 };
+
+// The two slab tests of the header: BOX_MISS and BOX_HIT are the reference's
+// answer, BOX_UNSURE needs box_exact().  *tnear = grown-box entry distance.
+__device__ __forceinline__ int box_classify(const Box& bx, const RayQ& q, float* tnear) {
+    const bool px = q.inv.x > 0.f, py = q.inv.y > 0.f, pz = q.inv.z > 0.f;
+    const float cnx = px ? bx.lx : bx.hx, cfx = px ? bx.hx : bx.lx;
+    const float cny = py ? bx.ly : bx.hy, cfy = py ? bx.hy : bx.ly;
+    const float cnz = pz ? bx.lz : bx.hz, cfz = pz ? bx.hz : bx.lz;
+    // grown box; fmaxf/fminf drop a NaN (0 * inf: parallel ray on a plane)
+    const float gnx = (cnx - q.gno.x) * q.inv.x, gfx = (cfx - q.gfo.x) * q.inv.x;
+    const float gny = (cny - q.gno.y) * q.inv.y, gfy = (cfy - q.gfo.y) * q.inv.y;
+    const float gnz = (cnz - q.gno.z) * q.inv.z, gfz = (cfz - q.gfo.z) * q.inv.z;
+    // shrunk box (empty, so never "sure", when thinner than 2M)
+    const float snx = (cnx - q.gfo.x) * q.inv.x, sfx = (cfx - q.gno.x) * q.inv.x;
+    const float sny = (cny - q.gfo.y) * q.inv.y, sfy = (cfy - q.gno.y) * q.inv.y;
+    const float snz = (cnz - q.gfo.z) * q.inv.z, sfz = (cfz - q.gno.z) * q.inv.z;
+    const float T1 = fmaxf(gnx, fmaxf(gny, gnz)), U1 = fminf(gfx, fminf(gfy, gfz));
+    const float T2 = fmaxf(snx, fmaxf(sny, snz)), U2 = fminf(sfx, fminf(sfy, sfz));
+    *tnear = T1;
+    const bool grown = (T1 <= U1) & (U1 >= 0.f);
+    const bool shrunk = (T2 <= U2) & (U2 >= 0.f);
+    const int cin = (int)(snx > T1) + (int)(sny > T1) + (int)(snz > T1);
+    const int cout = (int)(sfx < U1) + (int)(sfy < U1) + (int)(sfz < U1);
+    const bool sure = shrunk & ((T1 >= 0.f) ? (cin <= 1) : (cout <= 1));
+    return grown ? (sure ? BOX_HIT : BOX_UNSURE) : BOX_MISS;
+}
+
+// The reference box predicate; *tnear gets the grown-box entry distance.
+__device__ __forceinline__ bool box_pred(const Box& bx, const RayQ& q, float* tnear) {
+    const int c = box_classify(bx, q, tnear);
+    if (c == BOX_UNSURE) return box_exact(bx, q);
+    return c == BOX_HIT;
+}
+
+// Both children of a pair: the rare exact tests share one code path.
+__device__ __forceinline__ void pair_pred(const Box& L, const Box& R, const RayQ& q, bool* hl, bool* hr, float* tl,
+                                          float* tr) {
+    int cl = box_classify(L, q, tl), cr = box_classify(R, q, tr);
+    const bool el = cl == BOX_UNSURE, er = cr == BOX_UNSURE;
+    for (int k = 0, nk = (int)el + (int)er; k < nk; ++k) {
+        const bool right = k == 1 || !el;
+        const bool r = box_exact(right ? R : L, q);
+        if (right) cr = r ? BOX_HIT : BOX_MISS;
+        else cl = r ? BOX_HIT : BOX_MISS;
+    }
+    *hl = cl == BOX_HIT;
+    *hr = cr == BOX_HIT;
 }
 
 // KDTree::intersect(ray, tri) geometric part (kdtree.cpp:279-301); returns
@@ -238,8 +291,8 @@ __device__ __forceinline__ Hit trace_closest(const DevTree& T, const RayQ& q, in
         const float4 A = ldg4(&P->a), B = ldg4(&P->b), C = ldg4(&P->c);
         const uint4 W = ldg4u(&P->t);
         float tl, tr;
-        bool hl = box_pred(Box{A.x, A.y, A.z, A.w, B.x, B.y}, q, &tl);
-        bool hr = box_pred(Box{B.z, B.w, C.x, C.y, C.z, C.w}, q, &tr);
+        bool hl, hr;
+        pair_pred(Box{A.x, A.y, A.z, A.w, B.x, B.y}, Box{B.z, B.w, C.x, C.y, C.z, C.w}, q, &hl, &hr, &tl, &tr);
         if (PRUNE) {
             const float lim = h.t * q.pf + q.M;
             hl = hl && !(tl > lim);

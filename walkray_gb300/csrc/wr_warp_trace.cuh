@@ -13,8 +13,8 @@
 //  * ray refill: lanes whose ray is finished fetch new rays from a global
 //    counter (one atomicAdd per warp) as soon as `refill_min` of them are
 //    idle, instead of waiting for the whole warp;
-//  * the box predicate is straight-line code (wr_traverse.cuh), so lanes
-//    testing different boxes do not split.
+//  * the box predicate (wr_traverse.cuh) is straight-line code but for the
+//    rare exact face test, which both children share.
 //
 // A source class supplies the rays: `load(id, lane, stack, stride)` fills the
 // lane's ray and tree and calls lane_start(); `store(id, lane)` writes the
@@ -69,8 +69,8 @@ __device__ __forceinline__ void lane_step(TraceLane& L, uint32_t* stack, int str
     const float4 A = ldg4(&P->a), B = ldg4(&P->b), C = ldg4(&P->c);
     const uint4 W = ldg4u(&P->t);
     float tl, tr;
-    bool hl = box_pred(Box{A.x, A.y, A.z, A.w, B.x, B.y}, L.q, &tl);
-    bool hr = box_pred(Box{B.z, B.w, C.x, C.y, C.z, C.w}, L.q, &tr);
+    bool hl, hr;
+    pair_pred(Box{A.x, A.y, A.z, A.w, B.x, B.y}, Box{B.z, B.w, C.x, C.y, C.z, C.w}, L.q, &hl, &hr, &tl, &tr);
     if (STATS) L.n_box += 2;
     if (PRUNE) {
         const float lim = L.h.t * L.q.pf + L.q.M;
