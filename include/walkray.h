@@ -308,9 +308,12 @@ int wr_cancel(wr_ctx* ctx, wr_req_id id);
  * pathTracer.cpp:20): these size the wavefront renderer's queues. */
 typedef struct wr_wavefront_config {
     uint32_t capacity;       /* paths in flight (queue length) */
-    int32_t extend_block;    /* threads per CTA of the traversal stage */
+    int32_t extend_block;    /* threads per CTA of the traversal stage (32..128) */
     int32_t shade_block;     /* threads per CTA of the shade / generate stages */
-    int32_t ctas_per_sm;     /* persistent CTAs per SM, 0 = as many as fit */
+    int32_t ctas_per_sm;     /* traversal kernels compiled for at least 1-5, 6-7 or 8+ resident CTAs
+                                per SM (fewer registers per thread as it grows), launched with at most
+                                that many; 0 = tuned defaults (6 for rendering, 8 for
+                                wr_trace_closest); also applies to wr_trace_closest */
     int32_t iters_per_graph; /* bounce-loop iterations (pairs) per CUDA-graph launch */
     int32_t refill_min;      /* traversal: idle lanes of a warp that trigger a ray refill (1..32, 0 = default) */
     int32_t leaf_min;        /* traversal: lanes holding leaves that start a warp's leaf tests (1..32,

@@ -241,7 +241,7 @@ int wr_trace_closest_device(wr_ctx* ctx, wr_scene_id id, const float* d_rays, ui
     WR_CUDA(ctx, cudaMemsetAsync(err, 0, sizeof(unsigned int), s));
     const TraceTune tt = trace_tune_of(ctx);
     WR_CUDA(ctx, launch_trace_closest(sc->tree, d_rays, n, d_inside, d_contact, d_hits, counter, err, ctx->num_sms,
-                                      ctx->trace_prune, s, &ctx->last_trace_blocks, &tt));
+                                      ctx->trace_prune, s, &ctx->last_trace_blocks, &tt, ctx->wf_ctas_per_sm));
     ctx->kernel_launches++;
     return WR_OK;
 }
@@ -276,7 +276,8 @@ int wr_trace_closest(wr_ctx* ctx, wr_scene_id id, const float* rays, uint64_t n,
     const TraceTune tt = trace_tune_of(ctx);
     WR_CUDA(ctx, launch_trace_closest(sc->tree, ctx->rays.as<float>(), n, filtered ? ctx->inside.as<int32_t>() : nullptr,
                                       filtered ? ctx->contact.as<int32_t>() : nullptr, ctx->hits.as<wr_hit>(), counter,
-                                      err, ctx->num_sms, ctx->trace_prune, s, &ctx->last_trace_blocks, &tt));
+                                      err, ctx->num_sms, ctx->trace_prune, s, &ctx->last_trace_blocks, &tt,
+                                      ctx->wf_ctas_per_sm));
     ctx->kernel_launches++;
     WR_CUDA(ctx, cudaMemcpyAsync(hits, ctx->hits.p, n * sizeof(wr_hit), cudaMemcpyDeviceToHost, s));
     unsigned int herr = 0;

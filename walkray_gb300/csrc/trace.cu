@@ -7,6 +7,8 @@
 // at k * blockDim.x + t) so a warp's pushes hit 32 distinct banks.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "../../include/walkray.h"
 #include "trace_launch.h"
 #include "wr_warp_trace.cuh"
@@ -44,8 +46,9 @@ struct BatchSrc {
     }
 };
 
-template <bool PRUNE>
-__global__ void __launch_bounds__(128) k_trace_closest(DevTree T, const float* __restrict__ rays, uint64_t n,
+// MINB > 0: compiled for at least MINB resident CTAs per SM (a register cap)
+template <bool PRUNE, int MINB>
+__global__ void __launch_bounds__(128, MINB > 0 ? MINB : 1) k_trace_closest(DevTree T, const float* __restrict__ rays, uint64_t n,
                                                          const int32_t* __restrict__ inside,
                                                          const int32_t* __restrict__ contact, wr_hit* __restrict__ hits,
                                                          unsigned long long* __restrict__ counter, int stack_cap,
@@ -58,7 +61,7 @@ __global__ void __launch_bounds__(128) k_trace_closest(DevTree T, const float* _
 cudaError_t launch_trace_closest(const DevTree& T, const float* d_rays, uint64_t n, const int32_t* d_inside,
                                  const int32_t* d_contact, wr_hit* d_hits, unsigned long long* d_counter,
                                  unsigned int* d_err, int num_sms, bool prune, cudaStream_t stream,
-                                 int* launched_blocks, const TraceTune* tune) {
+                                 int* launched_blocks, const TraceTune* tune, int ctas_per_sm) {
     const int block = 128;
     const int stack_cap = (int)T.max_depth + 3;
     const size_t smem = (size_t)stack_cap * block * sizeof(uint32_t);
@@ -67,14 +70,19 @@ cudaError_t launch_trace_closest(const DevTree& T, const float* d_rays, uint64_t
     if (e != cudaSuccess) return e;
     // blocks per SM from the occupancy calculator for this stack size
     int per_sm = 1;
+    const int variant = ctas_per_sm ? ctas_per_sm : 8;  // default: the 8-CTA variant, fastest on the kd workload
     void (*kern)(DevTree, const float*, uint64_t, const int32_t*, const int32_t*, wr_hit*, unsigned long long*, int,
-                 TraceTune, unsigned int*) = prune ? k_trace_closest<true> : k_trace_closest<false>;
+                 TraceTune, unsigned int*) =
+        variant >= 8   ? (prune ? k_trace_closest<true, 8> : k_trace_closest<false, 8>)
+        : variant >= 6 ? (prune ? k_trace_closest<true, 6> : k_trace_closest<false, 6>)
+                           : (prune ? k_trace_closest<true, 0> : k_trace_closest<false, 0>);
     if (smem > 48 * 1024) {
         e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem);
     if (e != cudaSuccess) return e;
+    if (ctas_per_sm > 0) per_sm = std::min(per_sm, ctas_per_sm);
     if (per_sm < 1) per_sm = 1;
     uint64_t need_blocks = (n + block - 1) / block;
     int grid = num_sms * per_sm;

@@ -15,6 +15,6 @@ namespace wr {
 cudaError_t launch_trace_closest(const DevTree& T, const float* d_rays, uint64_t n, const int32_t* d_inside,
                                  const int32_t* d_contact, wr_hit* d_hits, unsigned long long* d_counter,
                                  unsigned int* d_err, int num_sms, bool prune, cudaStream_t stream,
-                                 int* launched_blocks, const TraceTune* tune = nullptr);
+                                 int* launched_blocks, const TraceTune* tune = nullptr, int ctas_per_sm = 0);
 
 }  // namespace wr

@@ -131,7 +131,7 @@ struct ExtendSrc {
     const WfJob* __restrict__ jobs;
     WfSide X;
     int2* __restrict__ hits;
-    unsigned long long* __restrict__ stats;
+    unsigned long long n_rays, n_box, n_tri;  // this thread's work counts (profiling launches)
 
     __device__ __forceinline__ void load(uint64_t id, TraceLane& L, uint32_t* stack, int stride) {
         const float4 a0 = X.a0[id], a1 = X.a1[id];
@@ -150,24 +150,49 @@ struct ExtendSrc {
     }
     __device__ __forceinline__ void store(uint64_t id, const TraceLane& L) {
         hits[id] = make_int2(L.h.slot, __float_as_int(L.h.t));
-        if (stats) {
-            atomicAdd(stats + 0, 1ull);
-            atomicAdd(stats + 1, (unsigned long long)L.n_box);
-            atomicAdd(stats + 2, (unsigned long long)L.n_tri);
-        }
+        n_rays += 1;
+        n_box += L.n_box;
+        n_tri += L.n_tri;
     }
 };
 
-template <bool STATS>
-__global__ void __launch_bounds__(128) k_wf_extend(const RenderScene* __restrict__ scenes,
+// adds the warp's sum of v to *dst (one atomic per warp)
+__device__ __forceinline__ void warp_add(unsigned long long* dst, unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31u) == 0 && v) atomicAdd(dst, v);
+}
+
+// MINB > 0: compiled for at least MINB resident CTAs of 128 threads per SM
+// (a register cap), chosen by the configuration's ctas_per_sm
+#define WR_EXTEND_BOUNDS(MINB) __launch_bounds__(128, (MINB) > 0 ? (MINB) : 1)
+
+template <bool STATS, int MINB>
+__global__ void WR_EXTEND_BOUNDS(MINB) k_wf_extend(const RenderScene* __restrict__ scenes,
                                                      const WfJob* __restrict__ jobs, WfSide X, int2* __restrict__ hits,
                                                      unsigned long long* __restrict__ work, int stack_cap,
                                                      TraceTune tune, unsigned int* __restrict__ err,
                                                      unsigned long long* __restrict__ stats) {
     extern __shared__ uint32_t s_stack[];
     const uint64_t n = (uint64_t)X.counts[0] + X.counts[1];
-    ExtendSrc src{scenes, jobs, X, hits, STATS ? stats : nullptr};
+    ExtendSrc src{scenes, jobs, X, hits, 0ull, 0ull, 0ull};
     warp_trace<true, STATS>(src, n, work, tune, s_stack + threadIdx.x, blockDim.x, stack_cap, err);
+    if (STATS) {
+        warp_add(stats + 0, src.n_rays);
+        warp_add(stats + 1, src.n_box);
+        warp_add(stats + 2, src.n_tri);
+    }
+}
+
+using ExtendKernel = void (*)(const RenderScene*, const WfJob*, WfSide, int2*, unsigned long long*, int, TraceTune,
+                              unsigned int*, unsigned long long*);
+
+// the extend kernel for a configuration: register cap from ctas_per_sm
+// (0 = the 6-CTA variant, fastest on the mixed-material scene)
+static ExtendKernel extend_kernel(int ctas_per_sm, bool stats) {
+    if (ctas_per_sm == 0) ctas_per_sm = 6;
+    if (ctas_per_sm >= 8) return stats ? k_wf_extend<true, 8> : k_wf_extend<false, 8>;
+    if (ctas_per_sm >= 6) return stats ? k_wf_extend<true, 6> : k_wf_extend<false, 6>;
+    return stats ? k_wf_extend<true, 0> : k_wf_extend<false, 0>;
 }
 
 // shade: one bounce per path; survivors compacted into Y, finished paths to the film
@@ -469,14 +494,14 @@ int wf_update_jobs(wr_ctx* ctx, WfEngine* E, const std::vector<WfSlotUpdate>& up
             E->smem_extend = (size_t)cap * E->cfg.extend_block * sizeof(uint32_t);
             if (E->smem_extend > 200 * 1024) return set_error(ctx, WR_ERR_UNSUPPORTED, "tree too deep for the stack");
             if (E->smem_extend > 48 * 1024) {
-                WR_CUDA(ctx, cudaFuncSetAttribute(k_wf_extend<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  (int)E->smem_extend));
-                WR_CUDA(ctx, cudaFuncSetAttribute(k_wf_extend<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  (int)E->smem_extend));
+                for (bool st : {false, true})
+                    WR_CUDA(ctx, cudaFuncSetAttribute(extend_kernel(E->cfg.ctas_per_sm, st),
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                      (int)E->smem_extend));
             }
             int per_sm = 0;
-            WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_extend<false>,
-                                                                       E->cfg.extend_block, E->smem_extend));
+            WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                             &per_sm, extend_kernel(E->cfg.ctas_per_sm, false), E->cfg.extend_block, E->smem_extend));
             if (E->cfg.ctas_per_sm > 0) per_sm = std::min(per_sm, E->cfg.ctas_per_sm);
             E->grid_extend = ctx->num_sms * std::max(1, per_sm);
             E->smem_shadow = E->smem_extend;
@@ -506,7 +531,7 @@ static void enqueue_iteration(WfEngine* E, int x, cudaStream_t s, cudaEvent_t* e
     WfJobCounters* cnt = E->counters.as<WfJobCounters>();
     k_wf_reset<<<1, 1, 0, s>>>(E->side[y], E->work.as<unsigned long long>(), E->shadow.count);
     if (ev) cudaEventRecord(ev[0], s);
-    (stats ? k_wf_extend<true> : k_wf_extend<false>)<<<E->grid_extend, E->cfg.extend_block, E->smem_extend, s>>>(
+    extend_kernel(E->cfg.ctas_per_sm, stats != nullptr)<<<E->grid_extend, E->cfg.extend_block, E->smem_extend, s>>>(
         scenes, jobs, E->side[x], E->hits.as<int2>(), E->work.as<unsigned long long>(), E->stack_cap, E->cfg.trace,
         E->err_word.as<unsigned int>(), stats);
     if (ev) cudaEventRecord(ev[1], s);

@@ -123,6 +123,24 @@ __host__ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k
 
 __host__ __device__ __forceinline__ float u24_to_float(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
 
+// One Philox block {blk, sample, pixel, 0} under (seed_lo, seed_hi).  Not
+// inlined on the device: a path draws from a dozen call sites, and one copy
+// of the ten rounds keeps the shading kernels' code small.
+#ifdef __CUDA_ARCH__
+static __device__ __noinline__ uint4 philox_block(uint32_t blk, uint32_t sample, uint32_t pixel, uint32_t seed_lo,
+                                           uint32_t seed_hi) {
+    uint32_t c[4] = {blk, sample, pixel, 0u};
+    philox4x32_10(c, seed_lo, seed_hi);
+    return make_uint4(c[0], c[1], c[2], c[3]);
+}
+#else
+inline uint4 philox_block(uint32_t blk, uint32_t sample, uint32_t pixel, uint32_t seed_lo, uint32_t seed_hi) {
+    uint32_t c[4] = {blk, sample, pixel, 0u};
+    philox4x32_10(c, seed_lo, seed_hi);
+    return make_uint4(c[0], c[1], c[2], c[3]);
+}
+#endif
+
 // Sequential draws of one path; keeps the four words of the current block in
 // registers (selected without dynamic indexing).
 struct PathRng {
@@ -140,12 +158,11 @@ struct PathRng {
     __host__ __device__ __forceinline__ float next() {
         uint32_t blk = dim >> 2;
         if (blk != cached_block) {
-            uint32_t c[4] = {blk, sample, pixel, 0u};
-            philox4x32_10(c, seed_lo, seed_hi);
-            w0 = c[0];
-            w1 = c[1];
-            w2 = c[2];
-            w3 = c[3];
+            const uint4 c = philox_block(blk, sample, pixel, seed_lo, seed_hi);
+            w0 = c.x;
+            w1 = c.y;
+            w2 = c.z;
+            w3 = c.w;
             cached_block = blk;
         }
         uint32_t k = dim++ & 3u;
