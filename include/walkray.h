@@ -251,6 +251,11 @@ typedef struct wr_render_profile {
     uint64_t box_tests;        /* AABB predicate evaluations (reference count) */
     uint64_t tri_tests;        /* ray-triangle tests */
     uint64_t paths;
+    double ms_drain;           /* the per-path finish of the last paths (k_wf_drain) */
+    uint64_t drained_paths;    /* paths it finished */
+    uint32_t iter_rays[32];    /* rays in the queue of bounce iteration i (first 32 iterations) */
+    float iter_extend_ms[32];  /* extend stage time of iteration i */
+    float iter_shade_ms[32];   /* shade stage time of iteration i */
 } wr_render_profile;
 int wr_profile_render(wr_ctx* ctx, wr_scene_id scene, const wr_render_desc* desc, float* d_sum,
                       wr_render_profile* out);
@@ -318,6 +323,8 @@ typedef struct wr_wavefront_config {
     int32_t refill_min;      /* traversal: idle lanes of a warp that trigger a ray refill (1..32, 0 = default) */
     int32_t leaf_min;        /* traversal: lanes holding leaves that start a warp's leaf tests (1..32,
                                 0 = default); both also apply to wr_trace_closest */
+    int32_t drain_paths;     /* wr_render: once every path is generated and at most this many remain,
+                                finish them in one per-path kernel (0 = never) */
     double mpaths_per_s;     /* filled by wr_autotune */
 } wr_wavefront_config;
 

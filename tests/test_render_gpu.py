@@ -82,7 +82,7 @@ def test_wavefront_equals_megakernel(ctx):
     try:
         b = ctx.render(sid, 32, 16, seed=3, mode="wavefront")
     finally:
-        ctx.set_wavefront_config(capacity=1 << 22)
+        ctx.set_wavefront_config(capacity=1 << 24)
     assert np.allclose(a, b, rtol=1e-4, atol=1e-5), np.abs(a - b).max()
     ctx.release(sid)
 
@@ -249,8 +249,30 @@ def test_pruning_reduces_traversal_work(ctx):
     sid = ctx.upload(s)
     w, h = s.camera.width, s.camera.height
     film = torch.zeros(w * h * 3, dtype=torch.float32, device="cuda")
-    pr = ctx.profile_render(sid, 1, 16, film.data_ptr(), seed=3)
-    ex = ctx.profile_render(sid, 1, 16, film.data_ptr(), seed=3, exact=True)
+    ctx.set_wavefront_config(capacity=1 << 24, drain_paths=0)  # every ray through the extend stages
+    try:
+        pr = ctx.profile_render(sid, 1, 16, film.data_ptr(), seed=3)
+        ex = ctx.profile_render(sid, 1, 16, film.data_ptr(), seed=3, exact=True)
+    finally:
+        ctx.set_wavefront_config(capacity=1 << 24)
+    assert pr["drained_paths"] == 0 and pr["rays"] > 0
     assert abs(pr["rays"] - ex["rays"]) <= 1e-3 * ex["rays"]
     assert pr["box_tests"] < ex["box_tests"]
+    ctx.release(sid)
+
+
+def test_drain_equals_bounce_loop(ctx):
+    """Finishing the last paths one per thread (k_wf_drain) computes the same
+    paths as running the bounce loop to the end."""
+    s = make_golden.golden_scenes()["mixed_l2"]
+    sid = ctx.upload(s)
+    try:
+        ctx.set_wavefront_config(capacity=1 << 16, drain_paths=0)  # loop to the end
+        a = ctx.render(sid, 32, 16, seed=9, mode="wavefront", nee=True)
+        ctx.set_wavefront_config(capacity=1 << 16, drain_paths=1 << 15)  # drain early
+        b = ctx.render(sid, 32, 16, seed=9, mode="wavefront", nee=True)
+    finally:
+        ctx.set_wavefront_config(capacity=1 << 24)
+    assert np.allclose(a, b, rtol=1e-4, atol=1e-5), np.abs(a - b).max()
+    assert a.mean() > 0
     ctx.release(sid)

@@ -71,11 +71,11 @@ def test_traversal_loop_settings_do_not_change_hits(ctx, refill_min, leaf_min):
     g = np.load(os.path.join(GOLDEN, "trace_filtered.npz"))
     rays, ids = make_golden.filtered_rays(s, 32768, seed=5)
     sid = ctx.upload(s)
-    ctx.set_wavefront_config(capacity=1 << 22, refill_min=refill_min, leaf_min=leaf_min)
+    ctx.set_wavefront_config(capacity=1 << 24, refill_min=refill_min, leaf_min=leaf_min)
     try:
         h = ctx.trace_closest(sid, rays, ids[:, 0], ids[:, 1])
     finally:
-        ctx.set_wavefront_config(capacity=1 << 22)
+        ctx.set_wavefront_config(capacity=1 << 24)
     assert np.array_equal(h["tri"], g["tri"])
     hit = h["tri"] != NO_HIT
     assert np.array_equal(h["t"][hit].view(np.uint32), g["t"][hit].view(np.uint32))

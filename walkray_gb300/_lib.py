@@ -91,7 +91,7 @@ class wr_render_desc(C.Structure):
 
 class wr_wavefront_config(C.Structure):
     _fields_ = [("capacity", C.c_uint32), ("extend_block", C.c_int32), ("shade_block", C.c_int32),
-                ("ctas_per_sm", C.c_int32), ("iters_per_graph", C.c_int32), ("refill_min", C.c_int32), ("leaf_min", C.c_int32), ("mpaths_per_s", C.c_double)]
+                ("ctas_per_sm", C.c_int32), ("iters_per_graph", C.c_int32), ("refill_min", C.c_int32), ("leaf_min", C.c_int32), ("drain_paths", C.c_int32), ("mpaths_per_s", C.c_double)]
 
 
 class wr_serve_desc(C.Structure):
@@ -112,7 +112,9 @@ class wr_req_status(C.Structure):
 class wr_render_profile(C.Structure):
     _fields_ = [("ms_extend", C.c_double), ("ms_shade", C.c_double), ("ms_shadow", C.c_double),
                 ("ms_generate", C.c_double), ("ms_total", C.c_double), ("iterations", C.c_uint64),
-                ("rays", C.c_uint64), ("box_tests", C.c_uint64), ("tri_tests", C.c_uint64), ("paths", C.c_uint64)]
+                ("rays", C.c_uint64), ("box_tests", C.c_uint64), ("tri_tests", C.c_uint64), ("paths", C.c_uint64),
+                ("ms_drain", C.c_double), ("drained_paths", C.c_uint64), ("iter_rays", C.c_uint32 * 32),
+                ("iter_extend_ms", C.c_float * 32), ("iter_shade_ms", C.c_float * 32)]
 
 
 WR_RENDER_NEE = 1

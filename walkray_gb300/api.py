@@ -161,16 +161,17 @@ class Context:
         d = L.wr_render_desc(spp, max_path_len, seed, 1, _flags(nee, exact), 0, 0)
         p = L.wr_render_profile()
         self._check(self.lib.wr_profile_render(self.h, sid, C.byref(d), C.c_void_p(d_sum), C.byref(p)))
-        return {k: getattr(p, k) for k, _ in L.wr_render_profile._fields_}
+        return {k: (list(getattr(p, k)) if k.startswith("iter_") else getattr(p, k))
+                for k, _ in L.wr_render_profile._fields_}
 
     def set_wavefront_config(self, capacity: int, extend_block: int = 128, shade_block: int = 128,
                              ctas_per_sm: int = 0, iters_per_graph: int = 4, refill_min: int = 0,
-                             leaf_min: int = 0) -> None:
+                             leaf_min: int = 0, drain_paths: int = 0) -> None:
         """Queue sizes and block shapes of the wavefront renderer; refill_min and
         leaf_min (0 = defaults) tune the warp traversal loop of both the
         extend stage and trace_closest."""
         c = L.wr_wavefront_config(capacity, extend_block, shade_block, ctas_per_sm, iters_per_graph, refill_min,
-                                  leaf_min, 0.0)
+                                  leaf_min, drain_paths, 0.0)
         self._check(self.lib.wr_set_wavefront_config(self.h, C.byref(c)))
 
     def autotune(self, sid: int, spp_per_trial: int, max_path_len: int) -> dict:

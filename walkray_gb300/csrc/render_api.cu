@@ -280,6 +280,7 @@ WfConfig wf_tuned_config(wr_ctx* ctx) {
     if (ctx->wf_ctas_per_sm) c.ctas_per_sm = ctx->wf_ctas_per_sm;
     if (ctx->wf_iters) c.iters_per_graph = ctx->wf_iters;
     c.trace = trace_tune_of(ctx);
+    c.drain_paths = ctx->wf_drain_paths;
     return c;
 }
 

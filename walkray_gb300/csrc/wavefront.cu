@@ -45,10 +45,10 @@ __device__ __forceinline__ void wf_load(const WfSide& X, uint32_t i, WfPath& p) 
     p.dim = (uint32_t)misc.y;
     p.depth = (uint32_t)misc.z & 0xffffu;
     p.st.n = (int)((uint32_t)misc.z >> 16);
-    p.st.v[0] = stk.x;
-    p.st.v[1] = stk.y;
-    p.st.v[2] = stk.z;
-    p.st.v[3] = stk.w;
+    p.st.v0 = stk.x;
+    p.st.v1 = stk.y;
+    p.st.v2 = stk.z;
+    p.st.v3 = stk.w;
     const float4 a4 = X.a4[i];
     p.prev_d = mk(a4.x, a4.y, a4.z);
 }
@@ -61,7 +61,7 @@ __device__ __forceinline__ void wf_store(const WfSide& Y, uint32_t j, const WfPa
     Y.ids[j] = make_int4(p.cur.inside, p.cur.contact, p.job, (int)p.pixel);
     Y.misc[j] = make_int4((int)p.sample, (int)p.dim, (int)(p.depth | ((uint32_t)p.st.n << 16)),
                           __float_as_int(p.cur.cnorm.z));
-    Y.stk[j] = make_int4(p.st.v[0], p.st.v[1], p.st.v[2], p.st.v[3]);
+    Y.stk[j] = make_int4(p.st.v0, p.st.v1, p.st.v2, p.st.v3);
     Y.a4[j] = make_float4(p.prev_d.x, p.prev_d.y, p.prev_d.z, 0.f);
 }
 
@@ -259,6 +259,61 @@ __global__ void __launch_bounds__(128) k_wf_shade(const RenderScene* __restrict_
     }
 }
 
+// drain: the last paths of a render, each finished by one thread (trace,
+// bounce, NEE connection) without returning to the bounce loop.  Once nothing
+// is left to generate, the loop's iterations each cost about the latency of
+// their slowest ray however few rays remain; here the remaining paths run
+// side by side instead.  Same paths, draws and film additions as the loop.
+__global__ void __launch_bounds__(128) k_wf_drain(const RenderScene* __restrict__ scenes,
+                                                    const WfJob* __restrict__ jobs,
+                                                    WfJobCounters* __restrict__ counters, WfSide X, int stack_cap,
+                                                    unsigned int* __restrict__ err) {
+    extern __shared__ uint32_t s_stack[];
+    uint32_t* stack = s_stack + threadIdx.x;
+    const uint32_t n = X.counts[0] + X.counts[1];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    WfPath p;
+    wf_load(X, i, p);
+    const WfJob& J = jobs[p.job];
+    const RenderScene& S = scenes[J.scene];
+    PathRng g;
+    g.init(J.seed, p.pixel, p.sample, p.dim);
+    const bool nee = (J.flags & WR_RENDER_NEE) != 0;
+    const float pf = prune_factor(J.flags);
+    bool filtered = p.cur.contact != CAMERA_OBJ, nee_here = false;
+    f3 result = mk(0, 0, 0);
+    for (;;) {
+        RayQ q = make_rayq(p.cur.o, p.cur.d, S.tree.scene_mag);
+        q.pf = pf;
+        const Hit h = filtered ? trace_closest<true, true>(S.tree, q, p.cur.inside, p.cur.contact, stack,
+                                                           blockDim.x, stack_cap, err)
+                               : trace_closest<false, true>(S.tree, q, -1, -1, stack, blockDim.x, stack_cap, err);
+        if (h.slot < 0 && filtered) {  // a scattered ray that escapes ends with zero radiance
+            nee_here = nee;
+            break;
+        }
+        set_hit(S, p.cur, h);
+        filtered = true;
+        if (path_advance(S, p.cur, p.color, p.prev_d, p.depth, p.st, g, J.max_path_len, nee, result, nee_here))
+            break;
+    }
+    if (nee_here) {
+        ShadowReq sr;
+        result = mk(0, 0, 0);
+        if (nee_prepare(S, p.cur, p.prev_d, p.color, g, sr)) {
+            RayQ q = make_rayq(sr.o, sr.d, S.tree.scene_mag);
+            q.pf = pf;
+            const Hit h = trace_closest<true, true>(S.tree, q, sr.inside, sr.contact, stack, blockDim.x, stack_cap, err);
+            if (nee_visible(h, sr.dist)) result = sr.contrib;
+        }
+    }
+    if (result.x != 0.f || result.y != 0.f || result.z != 0.f) film_add(J, p.pixel, result);
+    const unsigned same = __match_any_sync(__activemask(), p.job);
+    if ((threadIdx.x & 31u) == (unsigned)(__ffs(same) - 1))
+        atomicAdd(&counters[p.job].finished, (unsigned long long)__popc(same));
+}
+
 // generate: new camera paths into the free slots of Y, from the job slots
 // listed in `order` (admission order); the list lives in device memory so the
 // captured graph does not change when jobs come and go
@@ -373,6 +428,7 @@ int wf_engine_get(wr_ctx* ctx, const WfConfig& cfg, WfEngine** out) {
         cur->cfg.shade_block == cfg.shade_block && cur->cfg.ctas_per_sm == cfg.ctas_per_sm &&
         cur->cfg.iters_per_graph == cfg.iters_per_graph && cur->cfg.trace.refill_min == cfg.trace.refill_min &&
         cur->cfg.trace.leaf_min == cfg.trace.leaf_min) {
+        cur->cfg.drain_paths = cfg.drain_paths;  // host-side only
         *out = cur;
         return WR_OK;
     }
@@ -408,7 +464,8 @@ int wf_engine_get(wr_ctx* ctx, const WfConfig& cfg, WfEngine** out) {
     WR_CUDA(ctx, E->work.reserve(sizeof(unsigned long long)));
     WR_CUDA(ctx, E->err_word.reserve(sizeof(unsigned int)));
     WR_CUDA(ctx, cudaMemset(E->err_word.p, 0, sizeof(unsigned int)));
-    WR_CUDA(ctx, cudaMallocHost(&E->host_counters, sizeof(WfJobCounters) * WF_MAX_JOBS));
+    // the job counters, then one extra record for the queue counts of side 0
+    WR_CUDA(ctx, cudaMallocHost(&E->host_counters, sizeof(WfJobCounters) * (WF_MAX_JOBS + 1)));
     E->job_tab.assign(WF_MAX_JOBS, WfJob{});
     E->order_host.assign(1, 0);
     // persistent grids from the occupancy calculator
@@ -574,6 +631,7 @@ int profile_wavefront(wr_ctx* ctx, RenderData& rd, const RenderParams& P, uint32
     const unsigned long long total = u.jh.job.total;
     cudaEventRecord(t0, s);
     int x = 0;
+    uint32_t queued = 0;  // rays waiting in side x
     for (uint64_t it = 0;; it++) {
         enqueue_iteration(E, x, s, ev, st.as<unsigned long long>());
         ctx->kernel_launches += 5;
@@ -588,9 +646,29 @@ int profile_wavefront(wr_ctx* ctx, RenderData& rd, const RenderParams& P, uint32
         out->ms_shade += b;
         out->ms_shadow += cc;
         out->ms_generate += d;
+        if (it < 32) {
+            out->iter_rays[it] = queued;
+            out->iter_extend_ms[it] = a;
+            out->iter_shade_ms[it] = b;
+        }
         out->iterations++;
-        if ((rc = wf_read_counters(ctx, E, c, s)) != WR_OK) break;
+        uint32_t waiting = 0;
+        if ((rc = wf_read_counters(ctx, E, c, s, &waiting, x)) != WR_OK) break;
+        queued = waiting;
         if (c[0].finished >= total) break;
+        if (c[0].claimed >= total && waiting <= E->cfg.drain_threshold()) {
+            cudaEventRecord(ev[0], s);
+            if ((rc = wf_drain(ctx, E, x, waiting, s)) != WR_OK) break;
+            cudaEventRecord(ev[1], s);
+            WR_CUDA(ctx, cudaEventSynchronize(ev[1]));
+            float dm = 0;
+            cudaEventElapsedTime(&dm, ev[0], ev[1]);
+            out->ms_drain = dm;
+            out->drained_paths = waiting;
+            if ((rc = wf_read_counters(ctx, E, c, s)) != WR_OK) break;
+            if (c[0].finished < total) rc = set_error(ctx, WR_ERR_INTERNAL, "wavefront drain left paths");
+            break;
+        }
         if (it > 100000) {
             rc = set_error(ctx, WR_ERR_TIMEOUT, "wavefront did not drain");
             break;
@@ -646,12 +724,31 @@ int wf_launch(wr_ctx* ctx, WfEngine* E, cudaStream_t s) {
     return WR_OK;
 }
 
-int wf_read_counters(wr_ctx* ctx, WfEngine* E, std::vector<WfJobCounters>& out, cudaStream_t s) {
+int wf_read_counters(wr_ctx* ctx, WfEngine* E, std::vector<WfJobCounters>& out, cudaStream_t s, uint32_t* waiting,
+                     int side) {
     out.resize(WF_MAX_JOBS);
     WR_CUDA(ctx, cudaMemcpyAsync(E->host_counters, E->counters.p, sizeof(WfJobCounters) * WF_MAX_JOBS,
                                  cudaMemcpyDeviceToHost, s));
+    unsigned int* q = reinterpret_cast<unsigned int*>(E->host_counters + WF_MAX_JOBS);
+    if (waiting)
+        WR_CUDA(ctx, cudaMemcpyAsync(q, E->side[side].counts, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
     WR_CUDA(ctx, cudaStreamSynchronize(s));
     std::memcpy(out.data(), E->host_counters, sizeof(WfJobCounters) * WF_MAX_JOBS);
+    if (waiting) *waiting = q[0] + q[1];
+    return WR_OK;
+}
+
+int wf_drain(wr_ctx* ctx, WfEngine* E, int side, uint32_t n, cudaStream_t s) {
+    if (n == 0) return WR_OK;
+    const int block = 128;
+    const size_t smem = (size_t)E->stack_cap * block * sizeof(uint32_t);
+    if (smem > 48 * 1024)
+        WR_CUDA(ctx, cudaFuncSetAttribute(k_wf_drain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_wf_drain<<<(n + block - 1) / block, block, smem, s>>>(E->scenes.as<RenderScene>(), E->jobs.as<WfJob>(),
+                                                           E->counters.as<WfJobCounters>(), E->side[side],
+                                                           E->stack_cap, E->err_word.as<unsigned int>());
+    WR_CUDA(ctx, cudaGetLastError());
+    ctx->kernel_launches++;
     return WR_OK;
 }
 
@@ -705,10 +802,19 @@ int render_wavefront(wr_ctx* ctx, RenderData& rd, const RenderParams& P, uint32_
     const unsigned long long total = u.jh.job.total;
     const uint64_t max_launches =
         1 + (total / std::max<uint32_t>(1, E->cfg.capacity) + 4) * (uint64_t)(P.max_path_len + 4) * 4;
+    const uint32_t drain_at = E->cfg.drain_threshold();
     for (uint64_t l = 0;; l++) {
         if ((rc = wf_launch(ctx, E, s)) != WR_OK) return rc;
-        if ((rc = wf_read_counters(ctx, E, c, s)) != WR_OK) return rc;
+        uint32_t waiting = 0;
+        if ((rc = wf_read_counters(ctx, E, c, s, &waiting)) != WR_OK) return rc;
         if (c[0].finished >= total) break;
+        if (c[0].claimed >= total && waiting <= drain_at) {
+            // every path is generated and few remain: finish them one per thread
+            if ((rc = wf_drain(ctx, E, 0, waiting, s)) != WR_OK) return rc;
+            if ((rc = wf_read_counters(ctx, E, c, s)) != WR_OK) return rc;
+            if (c[0].finished < total) return set_error(ctx, WR_ERR_INTERNAL, "wavefront drain left paths");
+            break;
+        }
         if (l > max_launches) return set_error(ctx, WR_ERR_TIMEOUT, "wavefront did not drain");
     }
     // retire the job so a later render starts from an empty table

@@ -70,12 +70,17 @@ struct WfShadow {
 };
 
 struct WfConfig {
-    uint32_t capacity = 1u << 22;  // paths in flight (4M x 128 B of state per side)
+    uint32_t capacity = 1u << 24;  // paths in flight (16M x 128 B of state per side): a 1024^2 x 16-spp call at once
     int extend_block = 128;
     int shade_block = 128;
     int ctas_per_sm = 0;           // 0 = occupancy calculator
     int iters_per_graph = 4;       // ping-pong pairs per graph launch
     TraceTune trace = default_trace_tune();  // warp traversal loop of the extend stage
+    int drain_paths = 0;           // per-path finish of a render's last paths at most this many (0 = never)
+
+    uint32_t drain_threshold() const {
+        return drain_paths > 0 ? (uint32_t)drain_paths : 0u;
+    }
 };
 
 struct WfEngine;
@@ -103,7 +108,12 @@ struct WfSlotUpdate {
 int wf_update_jobs(wr_ctx* ctx, WfEngine* E, const std::vector<WfSlotUpdate>& updates, const std::vector<int>& order,
                    cudaStream_t s);
 int wf_launch(wr_ctx* ctx, WfEngine* E, cudaStream_t s);  // one graph replay
-int wf_read_counters(wr_ctx* ctx, WfEngine* E, std::vector<WfJobCounters>& out, cudaStream_t s);
+// per-job counters; `waiting` (optional) gets the number of paths waiting in
+// queue side `side` (side 0 after a graph replay)
+int wf_read_counters(wr_ctx* ctx, WfEngine* E, std::vector<WfJobCounters>& out, cudaStream_t s,
+                     uint32_t* waiting = nullptr, int side = 0);
+// finishes the n paths waiting in side `side`, one thread per path (k_wf_drain)
+int wf_drain(wr_ctx* ctx, WfEngine* E, int side, uint32_t n, cudaStream_t s);
 int wf_error_word(wr_ctx* ctx, WfEngine* E, unsigned int* herr, cudaStream_t s);
 int wf_reset_queues(wr_ctx* ctx, WfEngine* E, cudaStream_t s);
 const WfConfig& wf_config(const WfEngine* E);

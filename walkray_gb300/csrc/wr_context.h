@@ -82,6 +82,7 @@ struct wr_ctx {
     uint32_t wf_capacity = 0;
     int wf_extend_block = 0, wf_shade_block = 0, wf_ctas_per_sm = 0, wf_iters = 0;
     int trace_refill_min = 0, trace_leaf_min = 0;  // warp traversal loop (0 = defaults)
+    int wf_drain_paths = 0;                          // drain threshold of wr_render (0 = never)
 };
 
 namespace wr {

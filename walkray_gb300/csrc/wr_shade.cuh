@@ -117,25 +117,37 @@ __device__ __forceinline__ PRay ray_default() {
 }
 
 // per-path stack of enclosing objects; top == current inside object
+// Four named registers rather than an array: a runtime index into an array
+// would put the stack (and the path state around it) in local memory.
 struct InsideStack {
-    int v[INSIDE_STACK];
+    int v0, v1, v2, v3;
     int n;
+    __device__ __forceinline__ int get(int k) const { return k == 0 ? v0 : (k == 1 ? v1 : (k == 2 ? v2 : v3)); }
+    __device__ __forceinline__ void put(int k, int x) {
+        v0 = k == 0 ? x : v0;
+        v1 = k == 1 ? x : v1;
+        v2 = k == 2 ? x : v2;
+        v3 = k == 3 ? x : v3;
+    }
     __device__ __forceinline__ void reset(int top) {
         n = 0;
-        if (top >= 0) v[n++] = top;
+        v0 = v1 = v2 = v3 = -1;
+        if (top >= 0) put(n++, top);
     }
-    __device__ __forceinline__ int top() const { return n > 0 ? v[n - 1] : -1; }
+    __device__ __forceinline__ int top() const { return n > 0 ? get(n - 1) : -1; }
     // object enclosing the exit point of `self` (what findInsideObject(outRay, self) finds for nested meshes)
     __device__ __forceinline__ int below(int self) const {
-        for (int k = n - 1; k >= 0; k--)
-            if (v[k] == self) return k > 0 ? v[k - 1] : -1;
-        return n > 0 && v[n - 1] != self ? v[n - 1] : -1;
+#pragma unroll
+        for (int k = INSIDE_STACK - 1; k >= 0; k--)
+            if (k < n && get(k) == self) return k > 0 ? get(k - 1) : -1;
+        return n > 0 && get(n - 1) != self ? get(n - 1) : -1;
     }
     __device__ __forceinline__ void set_top(int obj) {
         // a ray's inside object changed: entering pushes, leaving pops
         if (obj == top()) return;
-        for (int k = n - 1; k >= 0; k--)
-            if (v[k] == obj) {
+#pragma unroll
+        for (int k = INSIDE_STACK - 1; k >= 0; k--)
+            if (k < n && get(k) == obj) {
                 n = k + 1;
                 return;
             }
@@ -143,8 +155,8 @@ struct InsideStack {
             n = 0;
             return;
         }
-        if (n < INSIDE_STACK) v[n++] = obj;
-        else v[n - 1] = obj;
+        if (n < INSIDE_STACK) put(n++, obj);
+        else put(n - 1, obj);
     }
 };
 
@@ -636,7 +648,7 @@ __device__ __forceinline__ PRay scatter_heterogeneous(const RenderScene& S, int 
 
 // one scatter() call, following delegations (RefractiveObject handing a hit
 // inside it to the hit object; media handing over to the surface hit)
-static __device__ __noinline__ PRay scatter(const RenderScene& S, int self, const PRay& in, PathRng& g,
+static __device__ __forceinline__ PRay scatter(const RenderScene& S, int self, const PRay& in, PathRng& g,
                                             InsideStack& st) {
     PRay cur = in;
     float oP_scale = 1.f;
