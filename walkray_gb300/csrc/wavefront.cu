@@ -81,11 +81,45 @@ __device__ __forceinline__ uint32_t warp_append(unsigned int* counter, bool want
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
-__global__ void k_wf_reset(WfSide Y, unsigned long long* work, unsigned int* shadow_count) {
+__global__ void k_wf_reset(WfSide Y, unsigned long long* work, unsigned int* shadow_count, WfSort B) {
     Y.counts[0] = 0;
     Y.counts[1] = 0;
     *work = 0;
     *shadow_count = 0;
+    for (int k = 0; k < WF_SORT_KEYS; k++) B.counts[k] = 0;
+}
+
+// sort: bucket the queue by shading material (warp-aggregated appends)
+__global__ void __launch_bounds__(256) k_wf_sort(const RenderScene* __restrict__ scenes,
+                                                   const WfJob* __restrict__ jobs, WfSide X,
+                                                   const int2* __restrict__ hits, WfSort B, uint32_t capacity) {
+    const uint32_t n = X.counts[0] + X.counts[1];
+    const uint32_t step = gridDim.x * blockDim.x;
+    const unsigned lane = threadIdx.x & 31u;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += step) {  // warp-uniform trip count
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < n;
+        int key = 0;
+        if (valid) {
+            const int slot = hits[i].x;
+            if (slot >= 0) {
+                const int4 ids = X.ids[i];
+                const RenderScene& S = scenes[jobs[ids.z].scene];
+                const int self = ids.x >= 0 ? ids.x : (int)__float_as_uint(__ldg(&S.tree.tris[slot].v1.w));
+                key = 1 + (int)obj_type(S, self);
+                key = key < WF_SORT_KEYS ? key : WF_SORT_KEYS - 1;
+            }
+        }
+        const unsigned vm = __ballot_sync(0xffffffffu, valid);
+        if (valid) {
+            const unsigned peers = __match_any_sync(vm, key);
+            const int leader = __ffs(peers) - 1;
+            unsigned int b = 0;
+            if ((int)lane == leader) b = atomicAdd(&B.counts[key], (unsigned)__popc(peers));
+            b = __shfl_sync(peers, b, leader);
+            B.idx[(size_t)key * capacity + b + __popc(peers & ((1u << lane) - 1u))] = i;
+        }
+    }
 }
 
 // film update of a finished path: isLegalColor, fixVignetting, FP32 atomics
@@ -199,12 +233,30 @@ static ExtendKernel extend_kernel(int ctas_per_sm, bool stats) {
 __global__ void __launch_bounds__(128) k_wf_shade(const RenderScene* __restrict__ scenes,
                                                     const WfJob* __restrict__ jobs,
                                                     WfJobCounters* __restrict__ counters, WfSide X,
-                                                    const int2* __restrict__ hits, WfSide Y, WfShadow Q) {
-    const uint32_t n = X.counts[0] + X.counts[1];
+                                                    const int2* __restrict__ hits, WfSide Y, WfShadow Q, WfSort B,
+                                                    uint32_t capacity) {
+    __shared__ uint32_t s_first[WF_SORT_KEYS + 1];  // first queue position of each bucket
+    if (threadIdx.x == 0) {
+        uint32_t a = 0;
+        for (int k = 0; k < WF_SORT_KEYS; k++) {
+            s_first[k] = a;
+            a += B.counts[k];
+        }
+        s_first[WF_SORT_KEYS] = a;
+    }
+    __syncthreads();
+    const uint32_t n = s_first[WF_SORT_KEYS];
     const uint32_t step = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += step) {  // warp-uniform trip count
-        const uint32_t i = base + threadIdx.x;
-        const bool valid = i < n;
+        const uint32_t j = base + threadIdx.x;
+        const bool valid = j < n;
+        uint32_t i = 0;
+        if (valid) {  // the j-th path in bucket order
+            int k = 0;
+#pragma unroll
+            for (int kk = 1; kk < WF_SORT_KEYS; kk++) k = j >= s_first[kk] ? kk : k;
+            i = B.idx[(size_t)k * capacity + (j - s_first[k])];
+        }
         WfPath p;
         bool keep = false, done = false, shadow = false;
         f3 result = mk(0, 0, 0);
@@ -254,8 +306,8 @@ __global__ void __launch_bounds__(128) k_wf_shade(const RenderScene* __restrict_
                     atomicAdd(&counters[p.job].finished, (unsigned long long)__popc(same));
             }
         }
-        const uint32_t j = warp_append(&Y.counts[0], keep, 0);
-        if (keep) wf_store(Y, j, p);
+        const uint32_t out = warp_append(&Y.counts[0], keep, 0);
+        if (keep) wf_store(Y, out, p);
     }
 }
 
@@ -379,9 +431,11 @@ __global__ void __launch_bounds__(128) k_wf_generate(const WfJob* __restrict__ j
 // ---------------------------------------------------------------------------
 struct WfEngine {
     WfConfig cfg;
-    DeviceBuffer side_mem[2], hits, scenes, jobs, order, counters, work, err_word, shadow_mem;
+    DeviceBuffer side_mem[2], hits, scenes, jobs, order, counters, work, err_word, shadow_mem, sort_mem;
     WfSide side[2];
     WfShadow shadow{};
+    WfSort sort{};
+    int grid_sort = 0;
     int grid_shadow = 0;
     size_t smem_shadow = 0;
     std::vector<const RenderData*> scene_of;  // host mirror of the scene table
@@ -443,6 +497,11 @@ int wf_engine_get(wr_ctx* ctx, const WfConfig& cfg, WfEngine** out) {
         if (rc != WR_OK) return rc;
     }
     WR_CUDA(ctx, E->hits.reserve(sizeof(int2) * (size_t)cfg.capacity));
+    WR_CUDA(ctx, E->sort_mem.reserve(sizeof(uint32_t) * ((size_t)WF_SORT_KEYS * cfg.capacity + 64)));
+    E->sort.counts = E->sort_mem.as<unsigned int>();
+    E->sort.idx = E->sort.counts + 64;
+    WR_CUDA(ctx, cudaMemset(E->sort.counts, 0, sizeof(unsigned int) * WF_SORT_KEYS));
+    E->grid_sort = ctx->num_sms * 4;
     {
         const size_t Q = cfg.capacity;
         WR_CUDA(ctx, E->shadow_mem.reserve(Q * (3 * sizeof(float4) + sizeof(int4)) + 256));
@@ -586,14 +645,15 @@ static void enqueue_iteration(WfEngine* E, int x, cudaStream_t s, cudaEvent_t* e
     const RenderScene* scenes = E->scenes.as<RenderScene>();
     const WfJob* jobs = E->jobs.as<WfJob>();
     WfJobCounters* cnt = E->counters.as<WfJobCounters>();
-    k_wf_reset<<<1, 1, 0, s>>>(E->side[y], E->work.as<unsigned long long>(), E->shadow.count);
+    k_wf_reset<<<1, 1, 0, s>>>(E->side[y], E->work.as<unsigned long long>(), E->shadow.count, E->sort);
     if (ev) cudaEventRecord(ev[0], s);
     extend_kernel(E->cfg.ctas_per_sm, stats != nullptr)<<<E->grid_extend, E->cfg.extend_block, E->smem_extend, s>>>(
         scenes, jobs, E->side[x], E->hits.as<int2>(), E->work.as<unsigned long long>(), E->stack_cap, E->cfg.trace,
         E->err_word.as<unsigned int>(), stats);
     if (ev) cudaEventRecord(ev[1], s);
+    k_wf_sort<<<E->grid_sort, 256, 0, s>>>(scenes, jobs, E->side[x], E->hits.as<int2>(), E->sort, E->cfg.capacity);
     k_wf_shade<<<E->grid_shade, E->cfg.shade_block, 0, s>>>(scenes, jobs, cnt, E->side[x], E->hits.as<int2>(),
-                                                            E->side[y], E->shadow);
+                                                            E->side[y], E->shadow, E->sort, E->cfg.capacity);
     if (ev) cudaEventRecord(ev[2], s);
     k_wf_shadow<<<E->grid_shadow, E->cfg.extend_block, E->smem_shadow, s>>>(scenes, jobs, E->shadow, E->stack_cap,
                                                                            E->err_word.as<unsigned int>());
@@ -634,7 +694,7 @@ int profile_wavefront(wr_ctx* ctx, RenderData& rd, const RenderParams& P, uint32
     uint32_t queued = 0;  // rays waiting in side x
     for (uint64_t it = 0;; it++) {
         enqueue_iteration(E, x, s, ev, st.as<unsigned long long>());
-        ctx->kernel_launches += 5;
+        ctx->kernel_launches += 6;
         x = 1 - x;
         WR_CUDA(ctx, cudaEventSynchronize(ev[4]));
         float a = 0, b = 0, cc = 0, d = 0;
@@ -720,7 +780,7 @@ int wf_launch(wr_ctx* ctx, WfEngine* E, cudaStream_t s) {
         E->graph_stack = E->stack_cap;
     }
     WR_CUDA(ctx, cudaGraphLaunch(E->graph, s));
-    ctx->kernel_launches += 5ull * 2 * E->cfg.iters_per_graph;  // reset, extend, shade, shadow, generate per iteration
+    ctx->kernel_launches += 6ull * 2 * E->cfg.iters_per_graph;  // reset, extend, sort, shade, shadow, generate
     return WR_OK;
 }
 

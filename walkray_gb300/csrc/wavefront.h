@@ -60,6 +60,15 @@ struct WfSide {
     unsigned int* counts;  // [0] survivors written by shade, [1] paths appended by generate
 };
 
+// the extend stage's queue bucketed by the material that shades each path
+// (0 = no hit, 1 + WR_MAT_* of the inside or hit object), so that the shade
+// stage runs one material's code per warp
+constexpr int WF_SORT_KEYS = 8;
+struct WfSort {
+    unsigned int* counts;  // [WF_SORT_KEYS]
+    uint32_t* idx;         // bucket k at idx + k * capacity
+};
+
 // shadow rays of next-event estimation, written by shade, traced by k_wf_shadow
 struct WfShadow {
     float4* o;    // origin, distance to the light sample
