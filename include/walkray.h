@@ -58,6 +58,7 @@ extern "C" {
 #define WR_MAT_EMISSIVE 4      /* EmissiveObject            emissiveObj.h */
 #define WR_MAT_HOMOGENEOUS 5   /* HomogeneousVolume         homogeneousVolume.h */
 #define WR_MAT_HETEROGENEOUS 6 /* HeterogeneousVolume       HeterogeneousVolume.h */
+#define WR_MAT_REFLECTIVE 7    /* ReflectiveObject (mirror)  reflectiveObj.h; colour in albedo */
 
 /* One scene object: a triangle mesh with world-space vertices (the
  * reference's Mesh with an identity transform) and its material.  Fields a
@@ -69,7 +70,7 @@ typedef struct wr_object_desc {
     uint32_t tri_begin;      /* first triangle of this object in wr_scene_desc.triangles */
     uint32_t tri_count;
     uint32_t grid_index;     /* heterogeneous media: index into wr_scene_desc.grids */
-    float albedo[3];         /* diffuse / glossy reflectanceAlbedo */
+    float albedo[3];         /* diffuse / glossy reflectanceAlbedo, reflective color */
     float emission[3];       /* emissive color */
     float power;             /* isotropic Phong exponent */
     float ior;               /* refractive object / medium index of refraction */

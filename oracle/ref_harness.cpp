@@ -38,6 +38,7 @@
 #include "glossyObj.h"
 #include "anisotropicGlossyObj.h"
 #include "refractiveObj.h"
+#include "reflectiveObj.h"
 #include "emissiveObj.h"
 #include "homogeneousVolume.h"
 #include "HeterogeneousVolume.h"
@@ -97,6 +98,7 @@ static void build_scene(RenderEngine& eng, const wrs_scene& ws, Rng* rng) {
             case WR_MAT_EMISSIVE: obj = new EmissiveObject(&sc); break;
             case WR_MAT_HOMOGENEOUS: obj = new HomogeneousVolume(&sc, d.g); break;
             case WR_MAT_HETEROGENEOUS: obj = new HeterogeneousVolume(&sc, d.g); break;
+            case WR_MAT_REFLECTIVE: obj = new ReflectiveObject(&sc); break;
             default: fprintf(stderr, "unknown object type %u\n", d.type); exit(2);
         }
         obj->setRng(rng);
@@ -121,6 +123,7 @@ static void build_scene(RenderEngine& eng, const wrs_scene& ws, Rng* rng) {
                 static_cast<RefractiveObject*>(obj)->setDecayColor(v3(d.decay));
                 break;
             case WR_MAT_EMISSIVE: static_cast<EmissiveObject*>(obj)->setColor(e); break;
+            case WR_MAT_REFLECTIVE: static_cast<ReflectiveObject*>(obj)->setColor(a); break;
             case WR_MAT_HOMOGENEOUS:
                 static_cast<HomogeneousVolume*>(obj)->setSigma(v3(d.sigma_s), v3(d.sigma_a));
                 static_cast<HomogeneousVolume*>(obj)->setIOR(d.ior);

@@ -12,6 +12,11 @@ from the reference sources) on small seeded scenes and stores its answers:
                       several scenes
   render_cornell.npz  Cornell box 32x32, 8 independent reference renders of
                       256 spp each (PathTracer::renderPixels), as images
+  render_cornell_nee.npz  the same with the NEE branch on
+  render_mirror.npz   the Cornell box with a mirror tall box (ReflectiveObject),
+                      8 reference renders of 256 spp
+  render_dof.npz      the Cornell box through a thin lens (depth of field),
+                      8 reference renders of 2048 spp
 
 Usage: python tests/golden/make_golden.py   (needs the reference tree on this
 machine; the fixtures it writes are what the tests read elsewhere)
@@ -43,6 +48,8 @@ def golden_scenes():
         "ico4": S.icosphere_kd(4, seed=1),
         "mixed_l2": S.mixed_spheres(64, 64, seed=7, level=2),
         "media_small": S.cornell_media(32, 32, grid_n=16, seed=3),
+        "mirror": S.cornell_mirror(32, 32),
+        "dof": S.cornell_dof(32, 32, lens_radius=0.2),
     }
 
 
@@ -58,6 +65,23 @@ def filtered_rays(scene: S.Scene, n: int, seed: int):
 
 def run(args, env=None):
     subprocess.run([REF, *args], check=True, env=env, stdout=subprocess.DEVNULL)
+
+
+def render_set(scene, p, td, name, extra=(), spp=256):
+    """8 single-threaded reference renders (seeds 1..8, depth 8) into `name`."""
+    scene.save(p)
+    env = dict(os.environ, OMP_NUM_THREADS="1", WR_REF_WORKDIR=td)
+    procs, outs = [], []
+    for seed in range(1, 9):
+        out = os.path.join(td, f"{name}.{seed}.bin")
+        procs.append(subprocess.Popen([REF, "render", p, str(spp), "8", str(seed), out, *extra], env=env,
+                                      stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL))
+        outs.append(out)
+    for pr in procs:
+        assert pr.wait() == 0
+    h, w = scene.camera.height, scene.camera.width
+    imgs = np.stack([np.fromfile(o, np.float32).reshape(h, w, 3) for o in outs])
+    np.savez_compressed(os.path.join(HERE, name), images=imgs, spp=spp, max_path_len=8)
 
 
 def main():
@@ -115,6 +139,8 @@ def main():
             assert pr.wait() == 0
         imgs = np.stack([np.fromfile(o, np.float32).reshape(32, 32, 3) for o in outs])
         np.savez_compressed(os.path.join(HERE, "render_cornell_nee.npz"), images=imgs, spp=256, max_path_len=8)
+        render_set(sc["mirror"], p, td, "render_mirror.npz")
+        render_set(sc["dof"], p, td, "render_dof.npz", spp=2048)
     print("golden fixtures written to", HERE)
 
 

@@ -23,7 +23,7 @@ def dropin(built):
     return os.path.join(ROOT, "oracle", "_ref", "wr_ref_dropin")
 
 
-@pytest.mark.parametrize("name", ["cornell", "mixed_l2"])
+@pytest.mark.parametrize("name", ["cornell", "mixed_l2", "mirror"])
 def test_dropin_reads_materials(dropin, tmp_path, name):
     s = make_golden.golden_scenes()[name]
     p = str(tmp_path / "s.wrs")
@@ -44,6 +44,8 @@ def test_dropin_reads_materials(dropin, tmp_path, name):
             assert np.array_equal(g["emission"], w["emission"])
         if t == S.MAT_REFRACTIVE:
             assert g["ior"] == w["ior"] and np.array_equal(g["decay"], w["decay"])
+        if t == S.MAT_REFLECTIVE:
+            assert np.allclose(g["albedo"], w["albedo"], rtol=1e-5)
 
 
 def test_dropin_rejects_media(dropin, tmp_path):

@@ -111,3 +111,43 @@ def test_oracle_render_matches_reference_statistically(built):
     z = (br.mean(0) - bp.mean(0)) / np.sqrt(br.var(0, ddof=1) / 8 + bp.var(0, ddof=1) / 8 + 1e-12)
     assert np.abs(z).max() < 4.5, np.abs(z).max()
     assert abs(port.mean() / ref.mean() - 1) < 0.015
+
+
+def test_oracle_mirror_matches_reference_statistically(built):
+    """ReflectiveObject (reflectiveObj.h:17-43), including the reference's
+    unparenthesised MAX_VEC_COMP: the restated renderer vs 8 reference
+    renders of the mirror Cornell box."""
+    g = np.load(os.path.join(GOLDEN, "render_mirror.npz"))
+    ref = g["images"].astype(np.float64)
+    s = make_golden.golden_scenes()["mirror"]
+    orc = wr_oracle.SceneOracle(s)
+    port = np.stack([(orc.render(256, 8, seed=1100 + k)[0] / 256).reshape(32, 32, 3) for k in range(8)])
+    blk = lambda a: a.reshape(a.shape[0], 8, 4, 8, 4, 3).mean((2, 4))
+    br, bp = blk(ref), blk(port)
+    z = (br.mean(0) - bp.mean(0)) / np.sqrt(br.var(0, ddof=1) / 8 + bp.var(0, ddof=1) / 8 + 1e-12)
+    assert np.abs(z).max() < 4.5, np.abs(z).max()
+    assert abs(port.mean() / ref.mean() - 1) < 0.02
+    # the mirror shows the scene: different from the all-diffuse box
+    plain = np.load(os.path.join(GOLDEN, "render_cornell.npz"))["images"].astype(np.float64)
+    assert abs(plain.mean() / ref.mean() - 1) > 0.01 or np.abs(blk(plain).mean(0) - br.mean(0)).max() > 0.05
+
+
+def test_oracle_thin_lens_matches_reference_statistically(built):
+    """Camera::generateRay with depth of field (camera.cpp:30-47,
+    concentricSampleDisk :207-249) vs 8 reference renders."""
+    g = np.load(os.path.join(GOLDEN, "render_dof.npz"))
+    ref = g["images"].astype(np.float64)
+    s = make_golden.golden_scenes()["dof"]
+    orc = wr_oracle.SceneOracle(s)
+    port = np.stack([(orc.render(2048, 8, seed=1200 + k)[0] / 2048).reshape(32, 32, 3) for k in range(8)])
+    blk = lambda a: a.reshape(a.shape[0], 8, 4, 8, 4, 3).mean((2, 4))
+    br, bp = blk(ref), blk(port)
+    z = (br.mean(0) - bp.mean(0)) / np.sqrt(br.var(0, ddof=1) / 8 + bp.var(0, ddof=1) / 8 + 1e-12)
+    assert np.abs(z).max() < 4.5, np.abs(z).max()
+    assert abs(port.mean() / ref.mean() - 1) < 0.015
+    # and the lens matters at this noise level: the pinhole oracle is told apart
+    pin = wr_oracle.SceneOracle(make_golden.golden_scenes()["cornell"])
+    pim = np.stack([(pin.render(2048, 8, seed=1300 + k)[0] / 2048).reshape(32, 32, 3) for k in range(8)])
+    bq = blk(pim)
+    zp = (br.mean(0) - bq.mean(0)) / np.sqrt(br.var(0, ddof=1) / 8 + bq.var(0, ddof=1) / 8 + 1e-12)
+    assert np.abs(zp).max() > 4.5, np.abs(zp).max()

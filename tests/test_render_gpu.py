@@ -276,3 +276,42 @@ def test_drain_equals_bounce_loop(ctx):
     assert np.allclose(a, b, rtol=1e-4, atol=1e-5), np.abs(a - b).max()
     assert a.mean() > 0
     ctx.release(sid)
+
+
+def test_mirror_matches_reference_and_oracle(ctx):
+    """ReflectiveObject on the GPU: against the reference's renders of the
+    mirror Cornell box (statistically), against the oracle on the same random
+    streams (paired), and wavefront against megakernel (same paths)."""
+    s = make_golden.golden_scenes()["mirror"]
+    sid = ctx.upload(s)
+    ref = np.load(os.path.join(GOLDEN, "render_mirror.npz"))["images"].astype(np.float64)
+    gpu = gpu_images(ctx, sid, range(30, 38), 256, 8)
+    z = block_z(gpu, ref, 4)
+    assert np.abs(z).max() < 4.5, np.abs(z).max()
+    assert abs(gpu.mean() / ref.mean() - 1) < 0.02
+    orc = wr_oracle.SceneOracle(s)
+    for seed in (30, 31):
+        o = orc.render(256, 8, seed=seed)[0].reshape(32, 32, 3) / 256
+        g = ctx.render(sid, 256, 8, seed=seed).astype(np.float64)
+        assert abs(g.mean() / o.mean() - 1) < 2e-3, (g.mean(), o.mean())
+    w = ctx.render(sid, 64, 8, seed=40, mode="wavefront")
+    m = ctx.render(sid, 64, 8, seed=40, mode="megakernel")
+    assert np.allclose(w, m, rtol=1e-4, atol=1e-5), np.abs(w - m).max()
+    ctx.release(sid)
+
+
+def test_thin_lens_matches_oracle_paired(ctx):
+    """Depth of field (camera.cpp:30-47): the GPU's camera rays draw the
+    lens sample as the oracle does, so the same seeds give the same images."""
+    s = make_golden.golden_scenes()["dof"]
+    sid = ctx.upload(s)
+    orc = wr_oracle.SceneOracle(s)
+    for seed in (50, 51):
+        o = orc.render(256, 8, seed=seed)[0].reshape(32, 32, 3) / 256
+        g = ctx.render(sid, 256, 8, seed=seed).astype(np.float64)
+        assert abs(g.mean() / o.mean() - 1) < 2e-3, (g.mean(), o.mean())
+        assert np.median(np.abs(g - o)) < 1e-3
+    ref = np.load(os.path.join(GOLDEN, "render_dof.npz"))["images"].astype(np.float64)
+    gpu = gpu_images(ctx, sid, range(60, 68), 2048, 8)
+    assert np.abs(block_z(gpu, ref, 4)).max() < 4.5
+    ctx.release(sid)

@@ -120,7 +120,7 @@ int wr_scene_upload(wr_ctx* ctx, const wr_scene_desc* d, wr_scene_id* out) {
     uint64_t tri_sum = 0;
     for (uint32_t o = 0; o < d->num_objects; o++) {
         const wr_object_desc& m = d->objects[o];
-        if (m.type > WR_MAT_HETEROGENEOUS) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "unknown object type");
+        if (m.type > WR_MAT_REFLECTIVE) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "unknown object type");
         if ((uint64_t)m.vert_begin + m.vert_count > d->num_vertices ||
             (uint64_t)m.tri_begin + m.tri_count > d->num_triangles)
             return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "object range outside the scene arrays");

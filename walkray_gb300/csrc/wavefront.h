@@ -63,7 +63,7 @@ struct WfSide {
 // the extend stage's queue bucketed by the material that shades each path
 // (0 = no hit, 1 + WR_MAT_* of the inside or hit object), so that the shade
 // stage runs one material's code per warp
-constexpr int WF_SORT_KEYS = 8;
+constexpr int WF_SORT_KEYS = 9;
 struct WfSort {
     unsigned int* counts;  // [WF_SORT_KEYS]
     uint32_t* idx;         // bucket k at idx + k * capacity

@@ -434,6 +434,32 @@ __device__ __forceinline__ PRay scatter_emissive(const RenderScene& S, int self,
     return out;
 }
 
+// ReflectiveObject::scatter (reflectiveObj.h:17-43): mirror direction about
+// the hit face's normal; Russian roulette with p = MAX_VEC_COMP(color); on
+// survival radiance color / cosineTerm, pdf p (a delta direction).  The
+// reference's MAX macro (macros.h:13) has no parentheses, so MAX_VEC_COMP
+// evaluates to x > y ? x : max(y, z), reproduced here.
+__device__ __forceinline__ PRay scatter_reflective(const RenderScene& S, int self, const PRay& in, PathRng& g) {
+    PRay out = ray_default();
+    const f3 N = in.inorm;
+    out.o = in.o + in.d * in.idist;
+    out.inside = in.inside;
+    out.d = mirror_dir(N, in.d);
+    const f3 c = ld3(S.objs[self].albedo);
+    const float p = c.x > c.y ? c.x : (c.y > c.z ? c.y : c.z);
+    if (g.next() < p) {
+        out.contact = self;
+        out.cnorm = self == in.iobj ? N : obj_normal(S, self, in.itri);
+        out.rad = divs(c, cos_term(S, out));
+        out.dP = p;
+    } else {
+        out.rad = mk(0, 0, 0);
+        out.d = mk(0, 0, 0);
+        out.dP = 1.f - p;
+    }
+    return out;
+}
+
 // RefractiveObject::scatter (refractiveObj.h:27-88)
 __device__ __forceinline__ PRay scatter_refractive(const RenderScene& S, int self, const PRay& in, PathRng& g,
                                                    InsideStack& st, bool* delegate) {
@@ -662,6 +688,7 @@ static __device__ __forceinline__ PRay scatter(const RenderScene& S, int self, c
             case WR_MAT_GLOSSY:
             case WR_MAT_ANISO: out = scatter_surface(S, self, cur, g); break;
             case WR_MAT_EMISSIVE: out = scatter_emissive(S, self, cur); break;
+            case WR_MAT_REFLECTIVE: out = scatter_reflective(S, self, cur, g); break;
             case WR_MAT_REFRACTIVE:
                 out = scatter_refractive(S, self, cur, g, st, &del);
                 if (del) {  // `return inRay.intersectObj->scatter(inRay)`
@@ -893,7 +920,8 @@ __device__ __forceinline__ bool nee_prepare(const RenderScene& S, const PRay& en
     if (end.contact >= 0) {
         const uint32_t t = obj_type(S, end.contact);
         if (t == WR_MAT_EMISSIVE) return false;  // isEmissive()
-        if (t == WR_MAT_GLOSSY || t == WR_MAT_ANISO || t == WR_MAT_REFRACTIVE) return false;  // !nonSpecular()
+        if (t == WR_MAT_GLOSSY || t == WR_MAT_ANISO || t == WR_MAT_REFRACTIVE || t == WR_MAT_REFLECTIVE)
+            return false;  // !nonSpecular()
     }
     PRay e = end;
     e.d = normalize(light.o - e.o);

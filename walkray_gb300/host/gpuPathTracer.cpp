@@ -12,6 +12,7 @@
 #include "emissiveObj.h"
 #include "glossyObj.h"
 #include "homogeneousVolume.h"
+#include "reflectiveObj.h"
 #include "refractiveObj.h"
 #include "renderEngine.h"
 #include "scene.h"
@@ -85,6 +86,34 @@ bool wrDefaultDescribe(const AbstractObject* o, wr_object_desc* d) {
         d->ior = r->getIOR();
         Ray ray;
         put3(d->decay, r->randianceDecay(ray, 1.f));  // decayColor^1
+        return true;
+    }
+    if (dynamic_cast<const ReflectiveObject*>(o)) {
+        // the colour is private: scatter a ray that arrives along -N (it leaves
+        // along N, so cosineTerm is 1) with a local Rng until the roulette keeps
+        // it; radiance * cosineTerm is then the colour (reflectiveObj.h:29-35)
+        d->type = WR_MAT_REFLECTIVE;
+        AbstractObject* m = const_cast<AbstractObject*>(o);
+        Rng local(7), *saved = m->rng;
+        m->rng = &local;
+        Ray in;
+        vec3f p = o->getWorldVertexPosition(o->getVertexIndices(0)[0]);
+        vec3f n = o->getWorldNormal(0, p);
+        in.origin = p + n;
+        in.direction = -n;
+        in.intersectObj = m;
+        in.intersectTriangleID = 0;
+        in.intersectDist = 1.f;
+        vec3f c(0, 0, 0);
+        for (int k = 0; k < 256; k++) {
+            Ray out = o->scatter(in);
+            if (out.direction.length() > 0.5f) {
+                c = out.radiance * out.cosineTerm();
+                break;
+            }
+        }
+        m->rng = saved;
+        put3(d->albedo, c);
         return true;
     }
     // media keep their coefficients and grids private; describe them through a

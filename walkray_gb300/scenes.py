@@ -37,6 +37,7 @@ MAT_REFRACTIVE = 3
 MAT_EMISSIVE = 4
 MAT_HOMOGENEOUS = 5
 MAT_HETEROGENEOUS = 6
+MAT_REFLECTIVE = 7
 
 MAT_NAMES = {
     MAT_DIFFUSE: "diffuse",
@@ -46,6 +47,7 @@ MAT_NAMES = {
     MAT_EMISSIVE: "emissive",
     MAT_HOMOGENEOUS: "homogeneous",
     MAT_HETEROGENEOUS: "heterogeneous",
+    MAT_REFLECTIVE: "reflective",
 }
 
 # numpy mirror of wr_object_desc (136 bytes, every field 4 bytes wide)
@@ -152,6 +154,8 @@ class Scene:
             r["decay"] = (1.0, 1.0, 1.0)
             r["density_scale"] = 100.0
             r["step_size"] = 0.002
+            if o.type == MAT_REFLECTIVE:
+                r["albedo"] = (1.0, 1.0, 1.0)  # ReflectiveObject's default color (reflectiveObj.h:10)
             for k, val in o.params.items():
                 r[k] = val
             vb += len(o.verts)
@@ -401,6 +405,29 @@ def cornell(width=256, height=256) -> Scene:
     c = CORNELL_CAMERA
     s.camera = Camera.from_fov(c["position"], c["focus"], c["up"], width, height, c["fov"])
     assert s.num_triangles == 36
+    return s
+
+
+def cornell_mirror(width=256, height=256, color=(0.9, 0.6, 0.95)) -> Scene:
+    """The Cornell box with the tall box a mirror (ReflectiveObject,
+    reflectiveObj.h).  The default colour has x > y but z largest, where the
+    reference's MAX_VEC_COMP (macros.h:13-16) gives x rather than max(x, y, z)."""
+    s = cornell(width, height)
+    s.name = "cornell_mirror"
+    tall = s.objects[6]
+    tall.type = MAT_REFLECTIVE
+    tall.params = {"albedo": tuple(color)}
+    return s
+
+
+def cornell_dof(width=256, height=256, lens_radius=0.05, focal_dist=1.8) -> Scene:
+    """The Cornell box seen through a thin lens (Camera::setDOFParameters,
+    camera.cpp:30-47): lens radius and distance to the plane of focus (the
+    tall box is about 1.9 from the camera, the back wall 2.4)."""
+    s = cornell(width, height)
+    s.name = "cornell_dof"
+    s.camera.lens_radius = float(lens_radius)
+    s.camera.focal_dist = float(focal_dist)
     return s
 
 
