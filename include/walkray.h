@@ -336,6 +336,23 @@ int wr_set_wavefront_config(wr_ctx* ctx, const wr_wavefront_config* cfg);
 int wr_autotune(wr_ctx* ctx, wr_scene_id scene, uint32_t spp_per_trial, uint32_t max_path_len,
                 wr_wavefront_config* best);
 
+/* ---- scene files (no GPU needed) ----------------------------------------- */
+/* WalkRay's scene configuration read into a wr_scene_desc: Config::load
+ * (config.cpp:432-575) with its <Scene>, <Object>, <GroupObject>, <Camera>
+ * and <Material> nodes, and Mesh::loadShape (mesh.cpp:5-130) for .obj and
+ * .shp meshes, including the reference's unitizing of every mesh.  The
+ * description's arrays belong to the wr_scene_file and live until
+ * wr_scene_file_free.  On failure `err` (may be NULL) gets a message. */
+typedef struct wr_scene_file wr_scene_file;
+typedef struct wr_scene_file_settings {
+    char renderer[32];     /* the <renderer> name, e.g. "PathTracer" / "PT" */
+    uint32_t spp;          /* <iter> (0 when absent) */
+    uint32_t max_path_len; /* 20, as Config::load sets for every renderer */
+} wr_scene_file_settings;
+int wr_scene_file_load(const char* config_path, wr_scene_file** out, char* err, size_t err_len);
+int wr_scene_file_get(const wr_scene_file* f, wr_scene_desc* desc, wr_scene_file_settings* settings);
+int wr_scene_file_free(wr_scene_file* f);
+
 /* ---- host-side tree (no GPU needed) ------------------------------------- */
 /* Builds the reference tree on the host only and returns its flattened
  * form, so that host logic can be checked without a device.

@@ -270,6 +270,57 @@ static int cmd_render(int argc, char** argv) {
     return 0;
 }
 
+// mesh file single|group out.bin [16 floats, row-major transform]: meshes as
+// WalkRay loads them for Config::load (config.cpp:456-507, mesh.cpp:5-158).
+// single: Mesh::loadShape(file) (unitized), world positions through the
+// transform; group: the GroupObject flow (transform on the whole mesh, then
+// loadShape(file, true, &shapes)), each shape's world positions.  Output per
+// mesh: name length + name, vertex count + x y z floats, face count + indices.
+static int cmd_mesh(int argc, char** argv) {
+    if (argc < 5) return 2;
+    float v[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    for (int k = 0; k < 16 && 5 + k < argc; k++) v[k] = (float)atof(argv[5 + k]);
+    mat4f T;
+    T.set_value(v);  // readMatrix: set_value, then transpose (config.cpp:610-619)
+    T = transpose(T);
+    std::vector<Mesh*> meshes;
+    Mesh single, group;
+    std::vector<Mesh*> shapes;
+    if (!strcmp(argv[3], "single")) {
+        single.loadShape(argv[2]);
+        single.setTransform(T);
+        meshes.push_back(&single);
+    } else {
+        group.setTransform(T);
+        group.loadShape(argv[2], true, &shapes);
+        meshes = shapes;
+    }
+    FILE* f = fopen(argv[4], "wb");
+    if (!f) return 1;
+    const uint32_t n = (uint32_t)meshes.size();
+    fwrite(&n, 4, 1, f);
+    for (Mesh* m : meshes) {
+        const uint32_t len = (uint32_t)m->name.size();
+        fwrite(&len, 4, 1, f);
+        fwrite(m->name.data(), 1, len, f);
+        const uint32_t nv = m->getVertexNum(), nf = m->getTriangleNum();
+        fwrite(&nv, 4, 1, f);
+        for (uint32_t i = 0; i < nv; i++) {
+            vec3f w = m->getWorldVertexPosition(i);
+            fwrite(&w.x, 4, 3, f);
+        }
+        fwrite(&nf, 4, 1, f);
+        for (uint32_t i = 0; i < nf; i++) {
+            vec3ui t = m->getVertexIndices(i);
+            uint32_t t3[3] = {t.x, t.y, t.z};
+            fwrite(t3, 4, 3, f);
+        }
+    }
+    fclose(f);
+    for (Mesh* s : shapes) delete s;
+    return 0;
+}
+
 #ifdef WR_DROPIN
 #include "gpuPathTracer.h"
 // describe scene.wrs out.bin: the drop-in renderer's reading of every
@@ -303,6 +354,7 @@ int main(int argc, char** argv) {
     if (!strcmp(argv[1], "trace")) return cmd_trace(argc, argv);
     if (!strcmp(argv[1], "dumptree")) return cmd_dumptree(argc, argv);
     if (!strcmp(argv[1], "render")) return cmd_render(argc, argv);
+    if (!strcmp(argv[1], "mesh")) return cmd_mesh(argc, argv);
 #ifdef WR_DROPIN
     if (!strcmp(argv[1], "describe")) return cmd_describe(argc, argv);
 #endif

@@ -17,6 +17,10 @@ from the reference sources) on small seeded scenes and stores its answers:
                       8 reference renders of 256 spp
   render_dof.npz      the Cornell box through a thin lens (depth of field),
                       8 reference renders of 2048 spp
+  xml/                a scene in WalkRay's file layout (config, scene and
+                      material XML, .obj / .shp meshes, a density grid)
+  mesh_ref.npz        the reference's Mesh::loadShape of those meshes
+                      (single objects and a group), world positions
 
 Usage: python tests/golden/make_golden.py   (needs the reference tree on this
 machine; the fixtures it writes are what the tests read elsewhere)
@@ -84,6 +88,126 @@ def render_set(scene, p, td, name, extra=(), spp=256):
     np.savez_compressed(os.path.join(HERE, name), images=imgs, spp=spp, max_path_len=8)
 
 
+# --------------------------------------------------------------------------
+# a WalkRay-format scene on disk: config, scene and material XML files, meshes
+# (.obj with groups and every face form, .shp) and a density grid
+# --------------------------------------------------------------------------
+XML_DIR = os.path.join(HERE, "xml")
+T_QUAD = [0.8, -0.6, 0.0, 0.3, 0.6, 0.8, 0.0, -0.25, 0.0, 0.0, 1.0, 1.2, 0.0, 0.0, 0.0, 1.0]
+T_GROUP = [0.35, 0.0, 0.0, 0.5, 0.0, 0.35, 0.0, 0.3, 0.0, 0.0, 0.35, 0.6, 0.0, 0.0, 0.0, 1.0]
+T_SHP = [0.2, 0.0, 0.0, 0.3, 0.0, 0.2, 0.0, 0.2, 0.0, 0.0, 0.2, 0.4, 0.0, 0.0, 0.0, 1.0]
+T_GRID = [0.15, 0.0, 0.0, 0.7, 0.0, 0.15, 0.0, 0.2, 0.0, 0.0, 0.15, 0.3, 0.0, 0.0, 0.0, 1.0]
+MESH_CASES = [  # file, loadShape flow, transform (row-major)
+    ("quad_forms.obj", "single", T_QUAD),
+    ("two_groups.obj", "group", T_GROUP),
+    ("tri.shp", "single", T_SHP),
+]
+
+
+def _mat(T):
+    return "".join("[" + ", ".join(repr(float(x)) for x in T[4 * r:4 * r + 4]) + "]" for r in range(4))
+
+
+def write_xml_fixtures(d=XML_DIR):
+    """The scene files (all seeded / fixed, small)."""
+    os.makedirs(d, exist_ok=True)
+    with open(os.path.join(d, "quad_forms.obj"), "w") as f:
+        f.write("# faces in every form Mesh::loadShape reads\n"
+                "v -1.0 0.0 -1.0\nv 1.0 0.0 -1.0\nv 1.0 0.0 1.0\nv -1.0 0.0 1.0\nv 0.0 0.5 0.0\n"
+                "vt 0 0\nvt 1 0\nvt 1 1\nvn 0 1 0\n"
+                "f 1 2 3\nf 1/1 3/2 4/3\nf 1/1/1 2/2/1 5/3/1\nf 2//1 3//1 5//1\nf 3 4 5 1\n")
+    with open(os.path.join(d, "two_groups.obj"), "w") as f:
+        f.write("v 9 9 9\n"  # before the first group: counted by unitize, in no shape
+                "g tetra\nv 0 0 0\nv 1 0 0\nv 0 1 0\nv 0 0 1\nf 2 3 4\nf 2 4 3\nf 2 3 5\nf 3 4 5\n"
+                "g slab\nv 2 0 0\nv 3 0 0\nv 3 0.25 2\nv 2 0.25 2\nf 6 7 8\nf 6 8 9\n")
+    # .shp: a count n then n floats, a count m then m unsigned (mesh.cpp:20-25)
+    vdata = np.array([0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1, 1, 1, 1], np.float32)
+    fdata = np.array([0, 1, 2, 0, 1, 3, 1, 2, 4], np.uint32)
+    with open(os.path.join(d, "tri.shp"), "wb") as f:
+        f.write(np.int32(len(vdata)).tobytes() + vdata.tobytes() + np.int32(len(fdata)).tobytes() + fdata.tobytes())
+    rng = np.random.default_rng(11)
+    dens = rng.random((4, 3, 2)).astype(np.float32) * 3
+    with open(os.path.join(d, "density.txt"), "w") as f:
+        f.write("2 3 4\n" + " ".join(repr(float(x)) for x in dens.ravel()) + "\n")
+    with open(os.path.join(d, "materials.xml"), "w") as f:
+        f.write("""<Material Name="white"><type>Diffuse</type><color>(0.73, 0.73, 0.73)</color></Material>
+<Material Name="red"><type>Diffuse</type><color>(0.63, 0.065, 0.05)</color></Material>
+<Material Name="phong"><type>Glossy</type><color>(0.5, 0.4, 0.3)</color><power>40</power></Material>
+<Material Name="glass"><type>Refractive</type><IOR>1.33</IOR><decayColor>(0.9, 0.95, 1.0)</decayColor></Material>
+<Material Name="mirror"><type>Reflective</type><color>(0.9, 0.6, 0.95)</color></Material>
+<Material Name="light"><type>Emissive</type><color>(17, 12, 4)</color></Material>
+<Material Name="aniso"><type>AnisotropicGlossy</type><Rs>(0.3, 0.3, 0.3)</Rs><Rd>(0.2, 0.1, 0.05)</Rd><Nu>10</Nu><Nv>100</Nv></Material>
+<Material Name="fog"><type>GridVolume</type><g>0.3</g><IOR>1.0</IOR><sigma_s>(0.8, 0.8, 0.8)</sigma_s><sigma_a>(0.2, 0.2, 0.2)</sigma_a><density_scale>1</density_scale><density_file>density.txt</density_file></Material>
+""")
+    with open(os.path.join(d, "scene.xml"), "w") as f:
+        f.write(f"""<?xml version="1.0"?>
+<!-- a WalkRay scene in the reference's layout -->
+<Scene Name="test">
+  <GroupObject>
+    <filePath>two_groups.obj</filePath>
+    <transform>{_mat(T_GROUP)}</transform>
+    <Object Name="tetra"><Material><path>materials.xml</path><name>phong</name></Material></Object>
+    <Object Name="slab"><Material><path>materials.xml</path><name>mirror</name></Material></Object>
+  </GroupObject>
+  <Object>
+    <filePath>quad_forms.obj</filePath>
+    <Material><path>materials.xml</path><name>aniso</name></Material>
+    <transform>{_mat(T_QUAD)}</transform>
+  </Object>
+  <Object>
+    <filePath>tri.shp</filePath>
+    <Material><path>materials.xml</path><name>glass</name></Material>
+    <transform>{_mat(T_SHP)}</transform>
+  </Object>
+  <Object>
+    <filePath>quad_forms.obj</filePath>
+    <Material><path>materials.xml</path><name>fog</name></Material>
+    <transform>{_mat(T_GRID)}</transform>
+  </Object>
+  <Object>
+    <filePath>quad_forms.obj</filePath>
+    <Material><path>materials.xml</path><name>light</name></Material>
+    <transform>[0.2, 0.0, 0.0, 0.5][0.0, -0.2, 0.0, 1.0][0.0, 0.0, 0.2, 0.5][0.0, 0.0, 0.0, 1.0]</transform>
+  </Object>
+  <Camera Name="main">
+    <position>(0.5, 0.5, -1.4)</position><focus>(0.5, 0.5, 0.0)</focus><up>(0.0, 1.0, 0.0)</up>
+    <width>48</width><height>32</height><sightDist>43.95</sightDist>
+    <lensRadius>0.01</lensRadius><focalDist>1.9</focalDist>
+  </Camera>
+</Scene>
+""")
+    with open(os.path.join(d, "config.xml"), "w") as f:
+        f.write("""<Config>
+  <Scene><path>scene.xml</path><name>test</name><camera>main</camera></Scene>
+  <renderer>PathTracer</renderer>
+  <iter>64</iter>
+</Config>
+""")
+
+
+def mesh_fixtures(td):
+    """The reference's own Mesh::loadShape of MESH_CASES (harness `mesh`)."""
+    out = {}
+    for k, (fname, mode, T) in enumerate(MESH_CASES):
+        o = os.path.join(td, f"m{k}.bin")
+        run(["mesh", os.path.join(XML_DIR, fname), mode, o, *[repr(float(x)) for x in T]])
+        b = open(o, "rb").read()
+        off, n = 4, int(np.frombuffer(b[:4], np.uint32)[0])
+        for j in range(n):
+            ln = int(np.frombuffer(b[off:off + 4], np.uint32)[0])
+            name = b[off + 4:off + 4 + ln].decode()
+            off += 4 + ln
+            nv = int(np.frombuffer(b[off:off + 4], np.uint32)[0])
+            v = np.frombuffer(b[off + 4:off + 4 + 12 * nv], np.float32).reshape(nv, 3)
+            off += 4 + 12 * nv
+            nf = int(np.frombuffer(b[off:off + 4], np.uint32)[0])
+            f = np.frombuffer(b[off + 4:off + 4 + 12 * nf], np.uint32).reshape(nf, 3)
+            off += 4 + 12 * nf
+            out[f"{k}_{j}_v"], out[f"{k}_{j}_f"] = v, f
+            out[f"{k}_{j}_name"] = np.array(name)
+    np.savez_compressed(os.path.join(HERE, "mesh_ref.npz"), **out)
+
+
 def main():
     if not os.path.exists(REF):
         sys.exit("build the reference harness first: make -C oracle ref")
@@ -141,6 +265,8 @@ def main():
         np.savez_compressed(os.path.join(HERE, "render_cornell_nee.npz"), images=imgs, spp=256, max_path_len=8)
         render_set(sc["mirror"], p, td, "render_mirror.npz")
         render_set(sc["dof"], p, td, "render_dof.npz", spp=2048)
+        write_xml_fixtures()
+        mesh_fixtures(td)
     print("golden fixtures written to", HERE)
 
 

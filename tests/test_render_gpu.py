@@ -315,3 +315,21 @@ def test_thin_lens_matches_oracle_paired(ctx):
     gpu = gpu_images(ctx, sid, range(60, 68), 2048, 8)
     assert np.abs(block_z(gpu, ref, 4)).max() < 4.5
     ctx.release(sid)
+
+
+def test_scene_file_renders_through_both_renderers(ctx):
+    """A scene read from WalkRay's XML / .obj / .shp files (wr_scene_file_load)
+    uploads and renders: wavefront equal to megakernel, and the same paths as
+    the oracle on the same random streams (delta tracking for its grid)."""
+    from walkray_gb300 import api
+
+    s, st = api.load_scene_file(os.path.join(GOLDEN, "xml", "config.xml"))
+    sid = ctx.upload(s)
+    n = st["max_path_len"]
+    w = ctx.render(sid, 64, n, seed=70, mode="wavefront")
+    m = ctx.render(sid, 64, n, seed=70, mode="megakernel")
+    assert np.allclose(w, m, rtol=1e-4, atol=1e-5), np.abs(w - m).max()
+    h_, w_ = s.camera.height, s.camera.width
+    o = wr_oracle.SceneOracle(s).render(64, n, seed=70, flags=wr_oracle.DELTA)[0].reshape(h_, w_, 3) / 64
+    assert m.mean() > 0 and abs(m.mean() / o.mean() - 1) < 5e-3, (m.mean(), o.mean())
+    ctx.release(sid)

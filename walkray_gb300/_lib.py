@@ -64,6 +64,10 @@ class wr_scene_desc(C.Structure):
     ]
 
 
+class wr_scene_file_settings(C.Structure):
+    _fields_ = [("renderer", C.c_char * 32), ("spp", C.c_uint32), ("max_path_len", C.c_uint32)]
+
+
 class wr_hit(C.Structure):
     _fields_ = [("tri", C.c_uint32), ("t", C.c_float), ("b1", C.c_float), ("b2", C.c_float)]
 
@@ -151,6 +155,9 @@ _SIGS = {
     "wr_poll": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(wr_req_status)]),
     "wr_fetch": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p]),
     "wr_cancel": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "wr_scene_file_load": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p), C.c_char_p, C.c_size_t]),
+    "wr_scene_file_get": (C.c_int, [C.c_void_p, C.POINTER(wr_scene_desc), C.POINTER(wr_scene_file_settings)]),
+    "wr_scene_file_free": (C.c_int, [C.c_void_p]),
     "wr_kdtree_build_host": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_int,
                                        C.POINTER(C.c_void_p)]),
     "wr_kdtree_host_sizes": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),

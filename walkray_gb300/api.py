@@ -8,6 +8,7 @@
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -249,6 +250,50 @@ class Server:
                     raise TimeoutError(f"{len(left)} requests unfinished")
                 time.sleep(poll_s)
         return status
+
+
+def load_scene_file(path: str):
+    """WalkRay's XML scene configuration (and the .obj / .shp meshes and
+    density files it names) read by the library (wr_scene_file_load), as a
+    scenes.Scene with world-space vertices, plus the render settings
+    {renderer, spp, max_path_len}.  No GPU is needed."""
+    from .scenes import OBJECT_DTYPE, Camera, Grid
+
+    lib = L.load()
+    h = C.c_void_p()
+    err = C.create_string_buffer(512)
+    rc = lib.wr_scene_file_load(path.encode(), C.byref(h), err, len(err))
+    if rc != L.WR_OK:
+        raise L.WRError(rc, err.value.decode(errors="replace") or "wr_scene_file_load failed")
+    try:
+        d, st = L.wr_scene_desc(), L.wr_scene_file_settings()
+        lib.wr_scene_file_get(h, C.byref(d), C.byref(st))
+        objs = np.frombuffer((C.c_char * (d.num_objects * OBJECT_DTYPE.itemsize)).from_address(d.objects),
+                             OBJECT_DTYPE).copy() if d.num_objects else np.zeros(0, OBJECT_DTYPE)
+        verts = np.ctypeslib.as_array((C.c_float * (3 * d.num_vertices)).from_address(d.vertices)).reshape(-1, 3).copy() \
+            if d.num_vertices else np.zeros((0, 3), np.float32)
+        tris = np.ctypeslib.as_array((C.c_uint32 * (3 * d.num_triangles)).from_address(d.triangles)).reshape(-1, 3).copy() \
+            if d.num_triangles else np.zeros((0, 3), np.uint32)
+        grids = []
+        gds = (L.wr_grid_desc * d.num_grids).from_address(d.grids) if d.num_grids else []
+        for g in gds:
+            dens = np.ctypeslib.as_array(g.density, shape=(g.nz * g.ny * g.nx,)).reshape(g.nz, g.ny, g.nx).copy()
+            grids.append(Grid(dens, tuple(g.p0), tuple(g.p1)))
+        s = Scene(os.path.basename(path))
+        s.grids = grids
+        skip = {"type", "vert_begin", "vert_count", "tri_begin", "tri_count"}
+        for o in objs:
+            vb, vc, tb, tc = int(o["vert_begin"]), int(o["vert_count"]), int(o["tri_begin"]), int(o["tri_count"])
+            params = {k: (tuple(float(x) for x in o[k]) if o[k].shape else o[k].item())
+                      for k in OBJECT_DTYPE.names if k not in skip}
+            s.add(int(o["type"]), verts[vb:vb + vc], tris[tb:tb + tc], **params)
+        c = d.camera
+        s.camera = Camera(tuple(c.position), tuple(c.focus), tuple(c.up), int(c.width), int(c.height),
+                          float(c.image_plane_dist), float(c.lens_radius), float(c.focal_dist))
+        settings = {"renderer": st.renderer.decode(), "spp": int(st.spp), "max_path_len": int(st.max_path_len)}
+        return s, settings
+    finally:
+        lib.wr_scene_file_free(h)
 
 
 def build_tree_host(verts: np.ndarray, tris: np.ndarray, threads: int = 0) -> dict:
