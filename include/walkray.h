@@ -192,6 +192,10 @@ int wr_trace_closest_device(wr_ctx* ctx, wr_scene_id scene, const float* d_rays,
 /* ---- rendering ---------------------------------------------------------- */
 #define WR_MODE_MEGAKERNEL 0u /* one thread per pixel runs whole paths */
 #define WR_MODE_WAVEFRONT 1u  /* generate / extend / shade queues, persistent kernels, graph bounce loop */
+#define WR_MODE_BIDIRECTIONAL 2u /* BidirectionalPathTracer (bidirPathTracer.cpp:10-313): eye and light
+                                    sub-paths, all connections, balance-heuristic MIS, light tracing;
+                                    surfaces only (participating media: WR_ERR_UNSUPPORTED),
+                                    max_path_len <= 30 */
 
 #define WR_RENDER_NEE 1u      /* PathTracer's next-event-estimation branch (pathTracer.cpp:39-66) */
 /* Rendering traverses front to back and skips a box whose entry distance is

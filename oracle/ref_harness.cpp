@@ -15,9 +15,10 @@
  *   dumptree scene.wrs out.bin
  *            the reference tree in depth-first pre-order:
  *            per node {u32 is_leaf, f32 min[3], f32 max[3], u32 ntri, u32 tris[ntri]}
- *   render   scene.wrs spp maxlen seed out.bin [nee]
+ *   render   scene.wrs spp maxlen seed out.bin [nee|bpt]
  *            PathTracer::renderPixels (pathTracer.cpp:7-76) as it is: the
- *            per-spp tree rebuild and PFM write included.  out: W*H*3 f32
+ *            per-spp tree rebuild and PFM write included; with `bpt`
+ *            BidirectionalPathTracer::renderPixels (bidirPathTracer.cpp:10-56).  out: W*H*3 f32
  *            (row 0 = top, p = y*W + x).  Elapsed seconds on stderr.
  */
 #include "wr_ref_prelude.h"
@@ -47,6 +48,7 @@
 #define class struct
 #include "pathTracer.h"
 #undef class
+#include "bidirPathTracer.h"
 
 extern "C" {
 #include "wrs_io.h"
@@ -243,6 +245,7 @@ static int cmd_render(int argc, char** argv) {
     unsigned spp = (unsigned)atoi(argv[3]), maxlen = (unsigned)atoi(argv[4]);
     int seed = atoi(argv[5]);
     bool nee = argc > 7 && strcmp(argv[7], "nee") == 0;
+    bool bpt = argc > 7 && strcmp(argv[7], "bpt") == 0;
     RenderEngine* eng = new RenderEngine();
     delete eng->rng;
     eng->rng = new Rng(seed);
@@ -252,9 +255,15 @@ static int cmd_render(int argc, char** argv) {
     // per-object trees (config.cpp:519, renderEngine.cpp:27-30)
     eng->scene.buildKDTree(true);
     eng->scene.buildObjKDTrees(true);
-    PathTracer* pt = new PathTracer(eng, spp, maxlen);
-    pt->name = "PathTracer";
-    pt->useNextEventEstimation = nee;
+    MCRenderer* pt;
+    if (bpt) {
+        pt = new BidirectionalPathTracer(eng, spp, maxlen);
+    } else {
+        PathTracer* p = new PathTracer(eng, spp, maxlen);
+        p->name = "PathTracer";
+        p->useNextEventEstimation = nee;
+        pt = p;
+    }
     eng->renderer = pt;
     const char* wd = getenv("WR_REF_WORKDIR");
     if (chdir(wd ? wd : "/tmp") != 0) return 1;

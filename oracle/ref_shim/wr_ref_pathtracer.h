@@ -1,6 +1,7 @@
-/* Extra forced include for pathTracer.cpp only.  Line 23 of that file passes
- * the temporary returned by Camera::generateRay to MCRenderer::samplePath,
- * which takes Ray& — MSVC binds it, g++ does not.  The macro routes that one
+/* Extra forced include for pathTracer.cpp and bidirPathTracer.cpp only.
+ * pathTracer.cpp:23 and bidirPathTracer.cpp:32 pass the temporary returned by
+ * Camera::generateRay to MCRenderer::samplePath, which takes Ray& — MSVC
+ * binds it, g++ does not.  The macro routes that one
  * call through an identity function that yields an lvalue; the reference
  * source file itself is compiled as it lies. */
 #pragma once

@@ -73,6 +73,17 @@ void wro_scene_free(wro_scene* s);
 void wro_render(const wro_scene* s, uint32_t max_path_len, uint64_t seed, uint32_t flags, uint32_t p0, uint32_t p1,
                 uint32_t s0, uint32_t s1, double* sum, double* sumsq, int nthreads, uint64_t* rays_traced);
 
+/* ---- bidirectional path tracer ----------------------------------------- */
+/* BidirectionalPathTracer::renderPixels (bidirPathTracer.cpp:10-56) for
+ * samples [s0, s1) of every pixel: eye and light sub-paths, all their
+ * connections with balance-heuristic MIS weights and light-tracing splats;
+ * each sample's image after isLegalColor and fixVignetting is added to sum
+ * (and its square to sumsq).  Returns 1 (nothing rendered) for scenes with
+ * participating media, which this restatement does not cover. */
+int wro_render_bpt(const wro_scene* s, uint32_t max_path_len, uint64_t seed, uint32_t s0, uint32_t s1, double* sum,
+                   double* sumsq, int nthreads, uint64_t* rays_traced);
+int wro_scene_has_media(const wro_scene* s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -47,6 +47,9 @@ def load():
         lib.wro_scene_free.argtypes = [C.c_void_p]
         lib.wro_render.argtypes = [C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
                                    C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_uint64)]
+        lib.wro_render_bpt.restype = C.c_int
+        lib.wro_render_bpt.argtypes = [C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p,
+                                       C.c_void_p, C.c_int, C.POINTER(C.c_uint64)]
         _lib = lib
     return _lib
 
@@ -130,4 +133,20 @@ class SceneOracle:
         rays = C.c_uint64()
         self.lib.wro_render(self.h, max_path_len, seed, flags, p0, p1, s0, s0 + spp, _p(s), _p(s2), threads,
                             C.byref(rays))
+        return s, s2, rays.value
+
+    def render_bpt(self, spp: int, max_path_len: int, seed: int, s0: int = 0, threads: int = 0,
+                   want_sumsq: bool = False):
+        """The restated BidirectionalPathTracer: per-pixel sums over samples
+        [s0, s0 + spp) of each sample's image (after isLegalColor and
+        fixVignetting), like render()."""
+        c = self.scene.camera
+        npx = c.width * c.height
+        s = np.zeros((npx, 3), np.float64)
+        s2 = np.zeros((npx, 3), np.float64) if want_sumsq else None
+        rays = C.c_uint64()
+        rc = self.lib.wro_render_bpt(self.h, max_path_len, seed, s0, s0 + spp, _p(s), _p(s2), threads,
+                                     C.byref(rays))
+        if rc:
+            raise ValueError("the bidirectional restatement does not cover participating media")
         return s, s2, rays.value

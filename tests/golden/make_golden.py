@@ -21,9 +21,13 @@ from the reference sources) on small seeded scenes and stores its answers:
                       material XML, .obj / .shp meshes, a density grid)
   mesh_ref.npz        the reference's Mesh::loadShape of those meshes
                       (single objects and a group), world positions
+  render_bpt_*.npz    BidirectionalPathTracer::renderPixels on the Cornell,
+                      mirror, thin-lens and mixed-material scenes, 8
+                      reference renders of 64 spp each
 
-Usage: python tests/golden/make_golden.py   (needs the reference tree on this
-machine; the fixtures it writes are what the tests read elsewhere)
+Usage: python tests/golden/make_golden.py [bpt]   (needs the reference tree on
+this machine; `bpt` remakes only the bidirectional renders; the fixtures it
+writes are what the tests read elsewhere)
 """
 from __future__ import annotations
 
@@ -208,9 +212,25 @@ def mesh_fixtures(td):
     np.savez_compressed(os.path.join(HERE, "mesh_ref.npz"), **out)
 
 
+BPT_SCENES = ("cornell", "mirror", "dof", "mixed_l2")
+
+
+def bpt_fixtures(td):
+    """BidirectionalPathTracer::renderPixels (bidirPathTracer.cpp:10-56), 8
+    reference renders of 64 spp per scene, depth 8."""
+    sc = golden_scenes()
+    p = os.path.join(td, "s.wrs")
+    for name in BPT_SCENES:
+        render_set(sc[name], p, td, f"render_bpt_{name}.npz", extra=("bpt",), spp=64)
+
+
 def main():
     if not os.path.exists(REF):
         sys.exit("build the reference harness first: make -C oracle ref")
+    if sys.argv[1:] == ["bpt"]:  # only the bidirectional renders
+        with tempfile.TemporaryDirectory() as td:
+            bpt_fixtures(td)
+        return
     sc = golden_scenes()
     with tempfile.TemporaryDirectory() as td:
         # plain traversal
@@ -267,6 +287,7 @@ def main():
         render_set(sc["dof"], p, td, "render_dof.npz", spp=2048)
         write_xml_fixtures()
         mesh_fixtures(td)
+        bpt_fixtures(td)
     print("golden fixtures written to", HERE)
 
 

@@ -1,0 +1,99 @@
+"""The bidirectional renderer (WR_MODE_BIDIRECTIONAL) on the GPU through the
+C ABI: paired with the oracle's restatement of BidirectionalPathTracer on the
+same counter-based random streams (the sub-paths draw the same numbers, the
+connections draw none, so the images differ only by FP32 rounding and the
+order of the film's additions), and statistical against the reference's own
+renders (golden fixtures from bidirPathTracer.cpp through the reference
+harness)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+import make_golden
+import wr_oracle
+from walkray_gb300 import _lib as L
+from walkray_gb300 import scenes as S
+
+pytestmark = pytest.mark.gpu
+
+SCENES = ["cornell", "mirror", "dof", "mixed_l2"]
+
+
+def block_z(a, b, k):
+    def blk(x):
+        n, h, w, c = x.shape
+        return x.reshape(n, h // k, k, w // k, k, c).mean((2, 4))
+    ba, bb = blk(a), blk(b)
+    return (ba.mean(0) - bb.mean(0)) / np.sqrt(ba.var(0, ddof=1) / len(a) + bb.var(0, ddof=1) / len(b) + 1e-12)
+
+
+@pytest.mark.parametrize("name", SCENES)
+def test_bidirectional_paired_with_oracle(ctx, name):
+    s = make_golden.golden_scenes()[name]
+    h, w = s.camera.height, s.camera.width
+    sid = ctx.upload(s)
+    orc = wr_oracle.SceneOracle(s)
+    for seed in (41, 42):
+        o = orc.render_bpt(16, 8, seed=seed)[0].reshape(h, w, 3) / 16
+        g = ctx.render(sid, 16, 8, seed=seed, mode="bidirectional").astype(np.float64)
+        assert abs(g.mean() / o.mean() - 1) < 2e-3, (g.mean(), o.mean())
+        close = np.isclose(g, o, rtol=1e-3, atol=1e-5)
+        assert close.mean() > 0.99, close.mean()
+    ctx.release(sid)
+
+
+@pytest.mark.parametrize("name", SCENES)
+def test_bidirectional_matches_reference_renders(ctx, name):
+    ref = np.load(os.path.join(GOLDEN, f"render_bpt_{name}.npz"))["images"].astype(np.float64)
+    s = make_golden.golden_scenes()[name]
+    sid = ctx.upload(s)
+    gpu = np.stack([ctx.render(sid, 64, 8, seed=900 + k, mode="bidirectional").astype(np.float64)
+                    for k in range(8)])
+    assert np.abs(block_z(gpu, ref, 4)).max() < 4.8
+    assert abs(gpu.mean() / ref.mean() - 1) < 0.015
+    ctx.release(sid)
+
+
+def test_bidirectional_sums_match_mean_and_batches(ctx):
+    """wr_render_device adds per-sample images: the sum over 24 samples is
+    the mean of wr_render times 24, and samples [0, 24) rendered as 10 + 14
+    (spp_offset) are the same samples."""
+    s = make_golden.golden_scenes()["cornell"]
+    sid = ctx.upload(s)
+    m = ctx.render(sid, 24, 8, seed=5, mode="bidirectional").astype(np.float64)
+    s1, s2 = ctx.render_stats(sid, 24, 8, seed=5, mode="bidirectional")
+    assert np.allclose(s1 / 24, m, rtol=1e-5, atol=1e-7)
+    assert (s2 >= s1 * s1 / 24 * (1 - 1e-4) - 1e-6).all()  # sum of squares >= (sum)^2 / n
+    a = ctx.render(sid, 10, 8, seed=5, mode="bidirectional").astype(np.float64) * 10
+    b = ctx.render(sid, 14, 8, seed=5, mode="bidirectional", spp_offset=10).astype(np.float64) * 14
+    assert np.allclose((a + b) / 24, m, rtol=1e-4, atol=1e-6)
+    ctx.release(sid)
+
+
+def test_bidirectional_refuses_media_and_long_paths(ctx):
+    sid = ctx.upload(make_golden.golden_scenes()["media_small"])
+    with pytest.raises(L.WRError) as e:
+        ctx.render(sid, 1, 8, mode="bidirectional")
+    assert "media" in str(e.value)
+    ctx.release(sid)
+    sid = ctx.upload(make_golden.golden_scenes()["cornell"])
+    with pytest.raises(L.WRError):
+        ctx.render(sid, 1, 31, mode="bidirectional")
+    with pytest.raises(L.WRError):
+        ctx.render(sid, 1, 8, mode="bidirectional", nee=True)
+    ctx.render(sid, 1, 30, mode="bidirectional")
+    ctx.release(sid)
+
+
+def test_bidirectional_without_lights_is_black(ctx):
+    s = make_golden.golden_scenes()["cornell"]
+    for o in s.objects:
+        if o.type == S.MAT_EMISSIVE:
+            o.type = S.MAT_DIFFUSE
+            o.params = {"albedo": (0.5, 0.5, 0.5)}
+    sid = ctx.upload(s)
+    img = ctx.render(sid, 4, 8, mode="bidirectional")
+    assert not img.any()
+    ctx.release(sid)

@@ -187,7 +187,7 @@ class Context:
         return cam
 
 
-MODES = {"megakernel": 0, "wavefront": 1}
+MODES = {"megakernel": 0, "wavefront": 1, "bidirectional": 2}
 
 
 def _flags(nee: bool, exact: bool) -> int:

@@ -1,0 +1,562 @@
+// bpt.cu — WR_MODE_BIDIRECTIONAL: WalkRay's bidirectional path tracer
+// (BidirectionalPathTracer, bidirPathTracer.cpp:10-313) on the GPU.
+//
+// One render call runs in batches of samples-per-pixel; a batch of B samples
+// of every pixel is three kernels:
+//
+//   k_bpt_subpaths  one thread per (pixel, sample): the eye sub-path
+//                   (Camera::generateRay + MCRenderer::samplePath) and the
+//                   light sub-path (Scene::genLightSample + samplePath), every
+//                   ray record written to HBM (64 B per vertex, vertex-major so
+//                   that a warp's stores of vertex k are contiguous);
+//   k_bpt_connect   one thread per (pixel, sample): every (light length,
+//                   eye length) pair of throughputByConnecting — connectEdge,
+//                   the visibility ray (traced inline), connectingColorProb
+//                   and the balance-heuristic weight of connectingMisWeight
+//                   (FP64 products, as the reference) — adding to the sample's
+//                   image: its own pixel, or, for one-vertex eye sub-paths, the
+//                   pixel the light vertex projects to (light tracing);
+//   k_bpt_resolve   per pixel: each sample's image through isLegalColor and
+//                   fixVignetting into the caller's sum (and sum of squares).
+//
+// The connection step never builds the connected path: vertex i of it is
+// light vertex i (i < l) or eye vertex l + e - 1 - i, read from HBM, except
+// the two connection vertices, which connectEdge changes and which live in
+// registers.  Draws: the eye sub-path takes the Philox stream of (pixel,
+// sample) from draw 0, the light sub-path the same stream from draw 2^30;
+// the connections draw nothing.  Participating media are not covered (their
+// densities in the MIS weight); such scenes are refused by the caller.
+#include <algorithm>
+#include <memory>
+
+#include "render_launch.h"
+#include "wr_context.h"
+#include "wr_shade.cuh"
+
+namespace wr {
+
+constexpr uint32_t BPT_LIGHT_DIM0 = 0x40000000u;
+constexpr int BPT_MAX_RECORDS = 32;  // records per sub-path: max_path_len + 2
+constexpr double INV_PI_D = 0.31830988618379067153776752674503;
+constexpr double EPS_D = 1e-5;
+
+// ---------------------------------------------------------------------------
+// vertex records: {o, oP}, {d, dP}, {rad, inside}, {contact normal, contact + 2 | delta << 31}
+// ---------------------------------------------------------------------------
+struct VtxStore {
+    float4* base;
+    uint32_t nsamp;  // samples in the batch (the stride between vertex k and k + 1)
+    __device__ __forceinline__ float4* at(uint32_t sid, int k) const {
+        return base + 4 * ((size_t)k * nsamp + sid);
+    }
+    __device__ __forceinline__ void put(uint32_t sid, int k, const PRay& r) const {
+        float4* v = at(sid, k);
+        v[0] = make_float4(r.o.x, r.o.y, r.o.z, r.oP);
+        v[1] = make_float4(r.d.x, r.d.y, r.d.z, r.dP);
+        v[2] = make_float4(r.rad.x, r.rad.y, r.rad.z, __int_as_float(r.inside));
+        v[3] = make_float4(r.cnorm.x, r.cnorm.y, r.cnorm.z,
+                           __uint_as_float((uint32_t)(r.contact + 2) | (r.delta ? 0x80000000u : 0u)));
+    }
+    __device__ __forceinline__ PRay get(uint32_t sid, int k) const {
+        const float4* v = at(sid, k);
+        const float4 a = __ldg(v), b = __ldg(v + 1), c = __ldg(v + 2), n = __ldg(v + 3);
+        PRay r = ray_default();
+        r.o = mk(a.x, a.y, a.z);
+        r.oP = a.w;
+        r.d = mk(b.x, b.y, b.z);
+        r.dP = b.w;
+        r.rad = mk(c.x, c.y, c.z);
+        r.inside = __float_as_int(c.w);
+        r.cnorm = mk(n.x, n.y, n.z);
+        const uint32_t w = __float_as_uint(n.w);
+        r.contact = (int)(w & 0x7fffffffu) - 2;
+        r.delta = (w >> 31) != 0;
+        return r;
+    }
+};
+
+struct BptParams {
+    uint64_t seed;
+    uint32_t s0;          // first sample index of the batch
+    uint32_t nsamp;       // batch samples: npix * spp_in_batch
+    uint32_t npix;
+    uint32_t max_path_len;
+    float pf;             // traversal prune factor
+    int stack_cap;
+    VtxStore eye, light;
+    uint32_t* counts;     // per sample: eye records | light records << 8
+    float* film;          // per sample slot of the batch: npix * 3 floats
+};
+
+// MCRenderer::samplePath (mcRenderer.cpp:16-57) from `prev` (its hit set),
+// every record stored; returns the record count (at most max_path_len + 2)
+__device__ int bpt_sample_path(const RenderScene& S, const BptParams& P, const VtxStore& out, uint32_t sid, PRay prev,
+                               PathRng& g, uint32_t* stack, int stride, unsigned int* err) {
+    InsideStack st;
+    st.reset(prev.inside);
+    int n = 0;
+    for (uint32_t depth = 0;; depth++) {
+        out.put(sid, n++, prev);
+        PRay term = ray_default();
+        term.o = prev.o;
+        term.rad = mk(0, 0, 0);
+        term.delta = true;
+        const int self = prev.inside >= 0 ? prev.inside : prev.iobj;
+        if (self < 0) {
+            out.put(sid, n++, term);
+            break;
+        }
+        PRay next = scatter(S, self, prev, g, st);
+        if (length(next.d) < 0.5f) {
+            out.put(sid, n++, next);
+            break;
+        }
+        if (depth + 1 > P.max_path_len) {
+            out.put(sid, n++, term);
+            break;
+        }
+        st.set_top(next.inside);
+        RayQ q = make_rayq(next.o, next.d, S.tree.scene_mag);
+        q.pf = P.pf;
+        const Hit h = trace_closest<true, true>(S.tree, q, next.inside, next.contact, stack, stride, P.stack_cap, err);
+        if (h.slot < 0) {
+            out.put(sid, n++, next);
+            out.put(sid, n++, term);
+            break;
+        }
+        set_hit(S, next, h);
+        prev = next;
+    }
+    return n;
+}
+
+__global__ void __launch_bounds__(128) k_bpt_subpaths(RenderScene S, BptParams P, unsigned int* __restrict__ err) {
+    extern __shared__ uint32_t s_stack[];
+    uint32_t* stack = s_stack + threadIdx.x;
+    const int stride = blockDim.x;
+    const uint32_t sid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sid >= P.nsamp) return;
+    const uint32_t pixel = sid % P.npix, sample = P.s0 + sid / P.npix;
+    // eye sub-path: the camera ray is traced without a condition (camera.cpp:52)
+    PathRng g;
+    g.init(P.seed, pixel, sample, 0);
+    PRay cam = camera_ray(S.cam, pixel, g);
+    {
+        RayQ q = make_rayq(cam.o, cam.d, S.tree.scene_mag);
+        q.pf = P.pf;
+        const Hit h = trace_closest<false, true>(S.tree, q, -1, -1, stack, stride, P.stack_cap, err);
+        set_hit(S, cam, h);
+    }
+    const int ne = bpt_sample_path(S, P, P.eye, sid, cam, g, stack, stride, err);
+    // light sub-path (Scene::genLightSample -> AbstractObject::genSurfaceSample,
+    // abstractObj.cpp:18-52): the emitted ray is traced with NoSelfCondition
+    int nl = 0;
+    if (S.nlights) {
+        PathRng gl;
+        gl.init(P.seed, pixel, sample, BPT_LIGHT_DIM0);
+        PRay lr = light_sample(S, gl);
+        lr.iobj = -1;
+        if (lr.contact >= 0) {
+            lr.inside = __ldg(&S.light_inside[lr.contact]);
+            RayQ q = make_rayq(lr.o, lr.d, S.tree.scene_mag);
+            q.pf = P.pf;
+            const Hit h = trace_closest<true, true>(S.tree, q, lr.inside, lr.contact, stack, stride, P.stack_cap, err);
+            if (h.slot >= 0 && h.t > 0.f) set_hit(S, lr, h);  // `if(dist > 0)`
+            else lr.iobj = -1;
+        }
+        nl = bpt_sample_path(S, P, P.light, sid, lr, gl, stack, stride, err);
+    }
+    P.counts[sid] = (uint32_t)ne | ((uint32_t)nl << 8);
+}
+
+// ---------------------------------------------------------------------------
+// the connection step
+// ---------------------------------------------------------------------------
+// Camera::getPixelSolidAngle (camera.cpp:125-131)
+__device__ __forceinline__ float pixel_solid_angle(const CamParams& C, uint32_t pid) {
+    const uint32_t x = pid % C.width, y = pid / C.width;
+    const float xc = (float)((double)x + 0.5 - (C.width / 2.0)), yc = (float)((C.height / 2.0) - 0.5 - (double)y);
+    const float dist = sqrtf(xc * xc + yc * yc + C.ipd * C.ipd);
+    return C.ipd / powf(dist, 3.f);
+}
+
+// Ray::evalDirectionProbability (ray.cpp:32-38) with the objects' overrides;
+// `same` is the reference's `&inRay == &outRay` (an emitted ray)
+__device__ float bpt_dir_prob(const RenderScene& S, f3 in_d, const PRay& out, bool same, uint32_t cam_pixel) {
+    if (out.contact == CAMERA_OBJ) return (float)(1.0 / (double)pixel_solid_angle(S.cam, cam_pixel));
+    const int o = out.contact >= 0 ? out.contact : out.inside;
+    if (o < 0) return 0.f;
+    const wr_object_desc* m = &S.objs[o];
+    const uint32_t t = __ldg(&m->type);
+    if (t == WR_MAT_DIFFUSE || t == WR_MAT_GLOSSY) {  // diffuseObj.h:22-27, glossyObj.h:25-31
+        if (out.contact < 0) return 0.f;
+        const f3 al = ld3(m->albedo);
+        float p = al.x;
+        if (al.y > p) p = al.y;
+        if (al.z > p) p = al.z;
+        const float dn = dot(out.cnorm, out.d);
+        if (t == WR_MAT_DIFFUSE) return p * (dn > 0.f ? (float)((double)dn * INV_PI_D) : 0.f);
+        const float ct = (double)dn > EPS_D ? dn : (float)EPS_D;
+        const float power = __ldg(&m->power);
+        return p * (float)(((double)power + 1.0) * (double)powf(ct, power) * (INV_PI_D * 0.5));
+    }
+    if (t == WR_MAT_ANISO) {  // anisotropicGlossyObj.h:47-52, anisotropicPhong.h:19-33
+        if (out.contact < 0) return 0.f;
+        const f3 N = out.cnorm;
+        if (!(dot(in_d, N) <= 0.f && dot(out.d, N) >= 0.f)) return 0.f;
+        const f3 h = normalize(out.d - in_d);
+        float pdf = aniso_half_pdf(__ldg(&m->nu), __ldg(&m->nv), N, h);
+        pdf /= 4.f * fabsf(dot(in_d, h));
+        return pdf;
+    }
+    if (t == WR_MAT_REFLECTIVE) {  // reflectiveObj.h:44-46 with the unparenthesised MAX_VEC_COMP
+        const f3 c = ld3(m->albedo);
+        return c.x > c.y ? c.x : (c.y > c.z ? c.y : c.z);
+    }
+    // AbstractObject::evalDirectionProbability (abstractObj.cpp:61-68)
+    return same ? (float)(INV_PI_D * 0.25f) * 2.f : 0.f;
+}
+
+// Ray::evalBSDF (ray.cpp:15-22); the camera's evaluateBSDF is AbstractObject's (1, 1, 1)
+__device__ __forceinline__ f3 bpt_eval_bsdf(const RenderScene& S, f3 in_d, const PRay& out) {
+    if (out.contact == CAMERA_OBJ) return mk(1, 1, 1);
+    return eval_bsdf(S, in_d, out);
+}
+
+__device__ __forceinline__ bool emissive(const RenderScene& S, int o) {
+    return o >= 0 && obj_type(S, o) == WR_MAT_EMISSIVE;
+}
+
+__device__ __forceinline__ float max_eps(float a) { return (double)a > EPS_D ? a : (float)EPS_D; }
+
+// PdfWtoA (util.h:100-106) with aPdfW = 1
+__device__ __forceinline__ float pdf_w_to_a(float dist, float cos_there) { return fabsf(cos_there) / (dist * dist); }
+
+// the connected path y0..y(l-1) x(e-1)..x0 of one (l, e) pair
+struct Conn {
+    VtxStore eye, light;
+    uint32_t sid;
+    int l, e, n, c;
+    bool mod;
+    PRay lc, ec;  // the connection vertices after connectEdge (when mod)
+    __device__ __forceinline__ PRay v(int i) const {
+        if (mod && i == c) return lc;
+        if (mod && i == c + 1) return ec;
+        return i < l ? light.get(sid, i) : eye.get(sid, e - 1 - (i - l));
+    }
+};
+
+// BidirectionalPathTracer::linkVertex (bidirPathTracer.cpp:226-243) for
+// start in [0, n): the record, pointed at its neighbour on the connecting side
+__device__ __forceinline__ PRay link(const Conn& C, int start, bool reverse, const PRay& vs, const PRay& ve) {
+    PRay r = vs;
+    if ((reverse && start > C.c) || (!reverse && start <= C.c)) return r;
+    r.d = normalize(ve.o - vs.o);
+    r.inside = ve.inside;
+    return r;
+}
+
+// BidirectionalPathTracer::connectingMisWeight (bidirPathTracer.cpp:142-220),
+// expTerm = 1; the origin densities of surface vertices are 1
+// (AbstractObject::evalOriginProbability, abstractObj.cpp:54-59)
+__device__ float bpt_mis_weight(const RenderScene& S, const Conn& C, uint32_t pixel, double* rev) {
+    const int n = C.n, c = C.c;
+    // reverse densities, eye end first
+    rev[n - 1] = C.v(n - 1).oP;
+    for (int i = n - 2; i >= 0; i--) {
+        const PRay vi = C.v(i), v1 = C.v(i + 1);
+        const float dist = max_eps(length(v1.o - vi.o));
+        const PRay lr = link(C, i, false, vi, v1);
+        rev[i] = rev[i + 1] * (double)pdf_w_to_a(dist, cos_term(S, lr));
+        if (v1.delta) continue;
+        float dirp;
+        if (i < n - 2) {
+            const PRay v2 = C.v(i + 2);
+            const PRay a = link(C, i + 2, true, v2, v1), b = link(C, i + 1, true, v1, vi);
+            dirp = bpt_dir_prob(S, a.d, b, false, pixel);
+        } else {
+            dirp = bpt_dir_prob(S, v1.d, v1, true, pixel);  // vertex n-1 is the camera, never re-pointed
+        }
+        rev[i] *= (double)dirp;
+    }
+    // direct densities, light end first, with the sum over techniques
+    double dir = C.v(0).oP, all = 0.0, self = c == -1 ? rev[0] : 0.0;
+    bool can_connect = false;
+    PRay pm2 = C.v(0), pm1 = pm2;
+    {
+        const PRay v1 = C.v(1);
+        if (!pm1.delta && !v1.delta) {
+            all += dir * rev[1];
+            can_connect = true;
+        }
+        if (c == 0) self = dir * rev[1];
+    }
+    for (int i = 1; i < n; i++) {
+        const PRay vi = C.v(i);
+        const float dist = max_eps(length(vi.o - pm1.o));
+        const PRay lr = link(C, i, true, vi, pm1);
+        dir = dir * (double)pdf_w_to_a(dist, cos_term(S, lr));
+        if (!pm1.delta) {
+            float dirp;
+            if (i > 1) {
+                const PRay a = link(C, i - 2, false, pm2, pm1), b = link(C, i - 1, false, pm1, vi);
+                dirp = bpt_dir_prob(S, a.d, b, false, pixel);
+            } else {
+                const PRay r = link(C, 0, false, pm1, vi);
+                dirp = bpt_dir_prob(S, r.d, r, true, pixel);
+            }
+            dir *= (double)dirp;
+        }
+        if (i < n - 1) {
+            const PRay vn = C.v(i + 1);
+            if (!vi.delta && !vn.delta) {
+                all += dir * rev[i + 1];
+                can_connect = true;
+            }
+            if (i == c) self = dir * rev[i + 1];
+        }
+        pm2 = pm1;
+        pm1 = vi;
+    }
+    if (!can_connect) all += rev[0];
+    const double w = self / all;
+    return (float)(w > 0.0 ? w : 0.0);
+}
+
+// BidirectionalPathTracer::connectingColorProb (bidirPathTracer.cpp:267-290)
+__device__ void bpt_color_prob(const RenderScene& S, const Conn& C, f3& color, float& prob) {
+    const int n = C.n, c = C.c;
+    f3 col = mk(1, 1, 1);
+    float pr = 1.f;
+    PRay prev = C.v(0), cur = prev;
+    for (int i = 0; i < n; i++) {
+        cur = i == 0 ? prev : C.v(i);
+        col = vmul(col, cur.rad);
+        float dist = 0.f;
+        if (i <= c) {
+            const PRay nx = C.v(i + 1);
+            dist = max_eps(length(cur.o - nx.o));
+            col = vmul(col, radiance_decay(S, cur, dist));
+            if (i == c) col = col * (cos_term(S, cur) * cos_term(S, nx) / (dist * dist));
+        } else if (i > c + 1) {
+            dist = max_eps(length(prev.o - cur.o));
+            col = vmul(col, radiance_decay(S, cur, dist));
+        }
+        if (i != c && i != c + 1) col = col * cos_term(S, cur);
+        pr *= cur.dP * cur.oP;
+        prev = cur;
+    }
+    color = col;
+    prob = pr;
+}
+
+// Camera::convToRaster / convToRaster2 and checkPixelBound (camera.cpp:148-180);
+// a non-finite coordinate (a point in the camera's plane) counts as outside
+__device__ bool bpt_raster(const CamParams& C, f3 p, f3 lens_o, uint32_t* pid) {
+    if (C.lens_radius > 0.f) {
+        const f3 dir = normalize(p - lens_o);
+        const float ft = C.focal_dist / fabsf(dot(C.front, dir));
+        p = lens_o + dir * ft;
+    }
+    const f3 v = p - C.pos;
+    const float scale = C.ipd / dot(v, C.front);
+    const float rx = (float)(C.width / 2.0 + (double)(dot(v, C.right) * scale));
+    const float ry = (float)(C.height / 2.0 - (double)(dot(v, C.top) * scale));
+    if (!(fabsf(rx) < 2.0e9f) || !(fabsf(ry) < 2.0e9f)) return false;
+    const int px = (int)rx, py = (int)ry;
+    if (px < 0 || py < 0 || px >= (int)C.width || py >= (int)C.height) return false;
+    *pid = (uint32_t)py * C.width + (uint32_t)px;
+    return true;
+}
+
+__device__ __forceinline__ void film_add(float* f, uint32_t pid, f3 c) {
+    atomicAdd(f + 3 * (size_t)pid, c.x);
+    atomicAdd(f + 3 * (size_t)pid + 1, c.y);
+    atomicAdd(f + 3 * (size_t)pid + 2, c.z);
+}
+
+__global__ void __launch_bounds__(128) k_bpt_connect(RenderScene S, BptParams P, unsigned int* __restrict__ err) {
+    extern __shared__ uint32_t s_stack[];
+    uint32_t* stack = s_stack + threadIdx.x;
+    const int stride = blockDim.x;
+    const uint32_t sid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sid >= P.nsamp) return;
+    const uint32_t pixel = sid % P.npix;
+    float* film = P.film + 3 * (size_t)P.npix * (sid / P.npix);
+    const uint32_t cnt = P.counts[sid];
+    const int ne = (int)(cnt & 0xffu), nl = (int)(cnt >> 8);
+    double rev[2 * BPT_MAX_RECORDS];
+    f3 own = mk(0, 0, 0);
+    Conn C;
+    C.eye = P.eye;
+    C.light = P.light;
+    C.sid = sid;
+    for (int W = 2; W <= ne + nl; W++) {
+        const int lmin = W - ne > 0 ? W - ne : 0;
+        const int lmax = W - 1 >= nl ? nl : W - 1;
+        for (int l = lmin; l <= lmax; l++) {
+            const int e = W - l;
+            C.l = l;
+            C.e = e;
+            C.n = W;
+            C.c = l - 1;
+            C.mod = false;
+            const PRay first = C.v(0);
+            if (!emissive(S, first.contact)) continue;
+            if (l == 0) {  // a whole eye path: used only if no two neighbours are both non-delta
+                bool can = false;
+                PRay a = first;
+                for (int i = 1; i < W && !can; i++) {
+                    const PRay b = C.v(i);
+                    can = !a.delta && !b.delta;
+                    a = b;
+                }
+                if (can) continue;
+            } else {
+                // connectEdge (bidirPathTracer.cpp:293-312)
+                PRay lc = P.light.get(sid, l - 1), ec = P.eye.get(sid, e - 1);
+                if (l > 1 && emissive(S, lc.contact)) continue;
+                if (emissive(S, ec.contact)) continue;
+                if (lc.delta || ec.delta) continue;
+                const PRay pl = l - 1 > 0 ? P.light.get(sid, l - 2) : lc;
+                const PRay pe = e >= 2 ? P.eye.get(sid, e - 2) : ec;
+                lc.d = normalize(ec.o - lc.o);
+                ec.d = -lc.d;
+                lc.dP = 1.f;
+                lc.delta = false;
+                lc.rad = bpt_eval_bsdf(S, l - 1 > 0 ? pl.d : lc.d, lc);
+                if (lc.contact != -1 && l - 1 > 0) lc.inside = dot(lc.cnorm, lc.d) > 0.f ? pl.inside : lc.contact;
+                ec.dP = 1.f;
+                ec.delta = false;
+                ec.rad = bpt_eval_bsdf(S, e >= 2 ? pe.d : ec.d, ec);
+                if (ec.contact != -1 && e >= 2) ec.inside = dot(ec.cnorm, ec.d) > 0.f ? pe.inside : ec.contact;
+                C.lc = lc;
+                C.ec = ec;
+                C.mod = true;
+                // MCRenderer::visibilityTest (mcRenderer.cpp:59-65)
+                RayQ q = make_rayq(ec.o, ec.d, S.tree.scene_mag);
+                q.pf = P.pf;
+                const Hit h = trace_closest<true, true>(S.tree, q, ec.inside, ec.contact, stack, stride, P.stack_cap, err);
+                if (!(h.slot < 0 || (double)(h.t - length(ec.o - lc.o)) >= -EPS_D)) continue;
+            }
+            f3 col;
+            float prob;
+            bpt_color_prob(S, C, col, prob);
+            if (prob == 0.f) continue;
+            if (length(col) == 0.f) continue;
+            const float w = bpt_mis_weight(S, C, pixel, rev);
+            f3 contrib = divs(col, prob) * w;
+            if (e > 1) {
+                own = own + contrib;
+            } else {  // the light vertex seen by the camera: splat where it projects
+                const PRay cr = C.v(W - 1), lv = C.v(W - 2);
+                uint32_t pid;
+                if (bpt_raster(S.cam, lv.o, cr.o, &pid)) {
+                    float sa;
+                    if (S.cam.lens_radius > 0.f) {  // Camera::computeSolidAngle (camera.cpp:133-142)
+                        const float ct = dot(normalize(lv.o - cr.o), S.cam.front);
+                        sa = S.cam.ipd / powf(S.cam.ipd / ct, 3.f);
+                    } else {
+                        sa = pixel_solid_angle(S.cam, pid);
+                    }
+                    const float f = (float)(1.0 / (double)sa);
+                    contrib = contrib * (f / (float)P.npix);
+                    film_add(film, pid, contrib);
+                }
+            }
+        }
+    }
+    if (own.x != 0.f || own.y != 0.f || own.z != 0.f) film_add(film, pixel, own);
+}
+
+// each sample's image: isLegalColor, fixVignetting, into the caller's film
+__global__ void k_bpt_resolve(CamParams cam, float* __restrict__ film, uint32_t npix, uint32_t slots,
+                              float* __restrict__ sum, float* __restrict__ sumsq) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    f3 acc = mk(0, 0, 0), acc2 = mk(0, 0, 0);
+    for (uint32_t b = 0; b < slots; b++) {
+        float* f = film + 3 * ((size_t)b * npix + p);
+        f3 c = mk(f[0], f[1], f[2]);
+        f[0] = f[1] = f[2] = 0.f;
+        if (!legal(c)) c = mk(0, 0, 0);
+        c = fix_vignetting(cam, c, p);
+        acc = acc + c;
+        acc2 = acc2 + vmul(c, c);
+    }
+    float* s = sum + 3 * (size_t)p;
+    s[0] += acc.x;
+    s[1] += acc.y;
+    s[2] += acc.z;
+    if (sumsq) {
+        float* s2 = sumsq + 3 * (size_t)p;
+        s2[0] += acc2.x;
+        s2[1] += acc2.y;
+        s2[2] += acc2.z;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+struct BptState {
+    DeviceBuffer eye, light, counts, film;
+};
+
+int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& RP, uint32_t spp_offset,
+                         uint32_t spp, float* d_sum, float* d_sumsq, unsigned int* err, cudaStream_t stream) {
+    if (RP.max_path_len + 2 > (uint32_t)BPT_MAX_RECORDS)
+        return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "bidirectional mode: max_path_len is limited to 30");
+    if (!ctx->bidir) ctx->bidir = std::make_shared<BptState>();
+    BptState& st = *static_cast<BptState*>(ctx->bidir.get());
+    const uint32_t npix = S.cam.width * S.cam.height;
+    const uint32_t nrec = RP.max_path_len + 2;
+    // a batch of whole samples-per-pixel: vertex records of both sub-paths
+    // (64 B each), the counts and the batch's images in about 1 GiB
+    const size_t per_sample = 2ull * nrec * 64 + 4 + 12;
+    const uint64_t max_samples = std::max<uint64_t>(npix, (1ull << 30) / per_sample);
+    const uint32_t per_batch = (uint32_t)std::min<uint64_t>(spp, std::max<uint64_t>(1, max_samples / npix));
+    const uint64_t nsamp = (uint64_t)npix * per_batch;
+    if (nsamp > 0xffffffffull) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "image too large");
+    WR_CUDA(ctx, st.eye.reserve(64ull * nrec * nsamp));
+    WR_CUDA(ctx, st.light.reserve(64ull * nrec * nsamp));
+    WR_CUDA(ctx, st.counts.reserve(4ull * nsamp));
+    const size_t film_bytes = 12ull * nsamp;
+    if (st.film.bytes < film_bytes) {
+        WR_CUDA(ctx, st.film.reserve(film_bytes));
+        WR_CUDA(ctx, cudaMemsetAsync(st.film.p, 0, st.film.bytes, stream));
+    }
+    BptParams P{};
+    P.seed = RP.seed;
+    P.npix = npix;
+    P.max_path_len = RP.max_path_len;
+    P.pf = prune_factor(RP.flags);
+    P.stack_cap = RP.stack_cap;
+    P.eye.base = st.eye.as<float4>();
+    P.light.base = st.light.as<float4>();
+    P.counts = st.counts.as<uint32_t>();
+    P.film = st.film.as<float>();
+    const int block = 128;
+    const size_t smem = (size_t)RP.stack_cap * block * sizeof(uint32_t);
+    if (smem > 48 * 1024) {
+        WR_CUDA(ctx, cudaFuncSetAttribute(k_bpt_subpaths, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        WR_CUDA(ctx, cudaFuncSetAttribute(k_bpt_connect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    }
+    for (uint32_t done = 0; done < spp; done += per_batch) {
+        const uint32_t b = std::min(per_batch, spp - done);
+        P.s0 = spp_offset + done;
+        P.nsamp = npix * b;
+        P.eye.nsamp = P.light.nsamp = P.nsamp;
+        const int grid = (int)((P.nsamp + block - 1) / block);
+        k_bpt_subpaths<<<grid, block, smem, stream>>>(S, P, err);
+        WR_CUDA(ctx, cudaGetLastError());
+        k_bpt_connect<<<grid, block, smem, stream>>>(S, P, err);
+        WR_CUDA(ctx, cudaGetLastError());
+        k_bpt_resolve<<<(npix + 255) / 256, 256, 0, stream>>>(S.cam, P.film, npix, b, d_sum, d_sumsq);
+        WR_CUDA(ctx, cudaGetLastError());
+        ctx->kernel_launches += 3;
+    }
+    return WR_OK;
+}
+
+}  // namespace wr

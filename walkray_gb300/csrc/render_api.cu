@@ -13,9 +13,10 @@ namespace wr {
 
 struct RenderData {
     RenderScene S{};
-    DeviceBuffer objs, tri_slot, light_obj, light_thresh, obj_area, pick_prob, tri_thresh, grids;
+    DeviceBuffer objs, tri_slot, light_obj, light_thresh, obj_area, pick_prob, tri_thresh, grids, light_inside;
     std::vector<std::unique_ptr<DeviceBuffer>> grid_data;
     std::string unsupported;  // non-empty: this scene cannot be rendered (why)
+    bool has_media = false;
 };
 
 namespace {
@@ -33,9 +34,9 @@ float host_tri(f3 v0, f3 v1, f3 v2, f3 o, f3 d) {
     return t >= 0.f ? t : -1.f;
 }
 
-// Scene::findInsideObject (scene.cpp:115-144) for one ray, each object's
-// closest hit found by brute force over its triangles
-int host_find_inside(const SceneGPU& sc, f3 o, f3 d) {
+// Scene::findInsideObject (scene.cpp:115-144) for one ray, skipping object
+// `skip`, each object's closest hit found by brute force over its triangles
+int host_find_inside(const SceneGPU& sc, f3 o, f3 d, int skip = -1) {
     auto closest = [&](int obj, f3 dir, f3* nrm) -> bool {
         const wr_object_desc& m = sc.objects[obj];
         float best = -1.f;
@@ -54,6 +55,7 @@ int host_find_inside(const SceneGPU& sc, f3 o, f3 d) {
         return best >= 0;
     };
     for (int i = (int)sc.objects.size() - 1; i >= 0; i--) {
+        if (i == skip) continue;
         f3 n;
         if (!closest(i, -d, &n) || dot(n, -d) < 0) continue;
         if (!closest(i, d, &n) || dot(n, d) < 0) continue;
@@ -145,6 +147,22 @@ int prepare_render(wr_ctx* ctx, SceneGPU* sc, RenderData** out) {
         light_thresh.push_back(bound);
     }
     for (int o : light_obj) pick[o] = obj_area[o] / bound;
+    // the object enclosing each emitter (the inside object of its emitted rays,
+    // abstractObj.cpp:39), taken on its first triangle's centroid along the
+    // face normal: for closed, properly nested meshes it does not depend on the point
+    std::vector<int> light_inside(sc->objects.size() + 1, -1);
+    for (int o : light_obj) {
+        const wr_object_desc& m = sc->objects[o];
+        if (!m.tri_count) continue;
+        const uint32_t* lt = &sc->triangles[3 * (size_t)m.tri_begin];
+        const float* V = &sc->vertices[3 * (size_t)m.vert_begin];
+        f3 v0 = mk(V[3 * lt[0]], V[3 * lt[0] + 1], V[3 * lt[0] + 2]);
+        f3 v1 = mk(V[3 * lt[1]], V[3 * lt[1] + 1], V[3 * lt[1] + 2]);
+        f3 v2 = mk(V[3 * lt[2]], V[3 * lt[2] + 1], V[3 * lt[2] + 2]);
+        light_inside[o] = host_find_inside(*sc, (v0 + v1 + v2) * (1.f / 3.f), normalize(cross(v1 - v0, v2 - v0)), o);
+    }
+    WR_CUDA(ctx, upload(rd->light_inside, light_inside));
+    S.light_inside = rd->light_inside.as<int>();
     S.nlights = (uint32_t)light_obj.size();
     S.light_area = bound;
     WR_CUDA(ctx, upload(rd->light_obj, light_obj));
@@ -179,6 +197,8 @@ int prepare_render(wr_ctx* ctx, SceneGPU* sc, RenderData** out) {
     WR_CUDA(ctx, upload(rd->grids, gd));
     S.grids = rd->grids.as<GridDev>();
     for (const wr_object_desc& m : sc->objects)
+        if (m.type == WR_MAT_HOMOGENEOUS || m.type == WR_MAT_HETEROGENEOUS) rd->has_media = true;
+    for (const wr_object_desc& m : sc->objects)
         if (m.type == WR_MAT_HETEROGENEOUS &&
             !(m.sigma_s[0] + m.sigma_a[0] == m.sigma_s[1] + m.sigma_a[1] &&
               m.sigma_s[0] + m.sigma_a[0] == m.sigma_s[2] + m.sigma_a[2]))
@@ -199,7 +219,7 @@ int wr_render_device(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, fl
     if (!ctx || !desc || !d_sum) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "null argument");
     SceneGPU* sc = find_scene(ctx, id);
     if (!sc) return set_error(ctx, WR_ERR_NOT_FOUND, "no such scene");
-    if (desc->mode != WR_MODE_MEGAKERNEL && desc->mode != WR_MODE_WAVEFRONT)
+    if (desc->mode != WR_MODE_MEGAKERNEL && desc->mode != WR_MODE_WAVEFRONT && desc->mode != WR_MODE_BIDIRECTIONAL)
         return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "unknown render mode");
     if (desc->flags & ~RENDER_KNOWN_FLAGS) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "unknown render flags");
     if ((uint64_t)desc->spp_offset + desc->spp > 0xffffffffull)
@@ -219,6 +239,14 @@ int wr_render_device(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, fl
         P.flags = desc->flags;
         P.stack_cap = (int)sc->tree.max_depth + 3;
         const uint64_t npix = (uint64_t)rd->S.cam.width * rd->S.cam.height;
+        if (desc->mode == WR_MODE_BIDIRECTIONAL) {
+            if (rd->has_media)
+                return set_error(ctx, WR_ERR_UNSUPPORTED,
+                                 "bidirectional mode: participating media are not supported");
+            if (desc->flags & WR_RENDER_NEE)
+                return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "bidirectional mode has no NEE switch");
+            return render_bidirectional(ctx, rd->S, P, desc->spp_offset, desc->spp, d_sum, d_sumsq, err, s);
+        }
         if (desc->mode == WR_MODE_WAVEFRONT) {
             rc = render_wavefront(ctx, *rd, P, desc->spp_offset, desc->spp, d_sum, d_sumsq, s);
             if (rc != WR_OK) return rc;

@@ -5,6 +5,8 @@
 
 #include "wr_shade.cuh"
 
+struct wr_ctx;
+
 namespace wr {
 
 constexpr uint32_t RENDER_KNOWN_FLAGS = WR_RENDER_NEE | WR_RENDER_EXACT_TRAVERSAL;
@@ -26,5 +28,10 @@ struct RenderParams {
 // (film2 != NULL: also the sum of squares)
 cudaError_t launch_megakernel(const RenderScene& S, const RenderParams& P, float* film, float* film2,
                               unsigned int* err, cudaStream_t stream);
+
+// WR_MODE_BIDIRECTIONAL (bpt.cu): adds samples [spp_offset, spp_offset + spp)
+// of every pixel to d_sum (and their squares to d_sumsq, may be NULL)
+int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& P, uint32_t spp_offset, uint32_t spp,
+                         float* d_sum, float* d_sumsq, unsigned int* err, cudaStream_t stream);
 
 }  // namespace wr

@@ -78,6 +78,7 @@ struct wr_ctx {
     uint64_t kernel_launches = 0;  // kernels this library has launched on the context
     std::shared_ptr<void> serving;    // serving loop state (serve.cpp)
     std::shared_ptr<void> wavefront;  // wavefront engine (wavefront.cu)
+    std::shared_ptr<void> bidir;      // bidirectional renderer's sub-path buffers (bpt.cu)
     // wavefront configuration chosen by wr_autotune (0 = defaults)
     uint32_t wf_capacity = 0;
     int wf_extend_block = 0, wf_shade_block = 0, wf_ctas_per_sm = 0, wf_iters = 0;

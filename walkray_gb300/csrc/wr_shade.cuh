@@ -60,6 +60,7 @@ struct RenderScene {
     const float* pick_prob;
     const float* tri_thresh;  // cumulative triangle areas, indexed by global triangle id
     const GridDev* grids;
+    const int* light_inside;  // per object: the object enclosing an emitter (-1 none; lights only)
 };
 
 // ---------------------------------------------------------------------------
@@ -98,6 +99,7 @@ struct PRay {
     int inside;
     int contact;    // object, CAMERA_OBJ or -1
     f3 cnorm;       // contact normal (valid when contact != -1)
+    bool delta;     // isDeltaDirection (read by the bidirectional renderer only)
 };
 
 __device__ __forceinline__ PRay ray_default() {
@@ -113,6 +115,7 @@ __device__ __forceinline__ PRay ray_default() {
     r.inside = -1;
     r.contact = -1;
     r.cnorm = mk(0, 0, 0);
+    r.delta = false;
     return r;
 }
 
@@ -452,6 +455,7 @@ __device__ __forceinline__ PRay scatter_reflective(const RenderScene& S, int sel
         out.cnorm = self == in.iobj ? N : obj_normal(S, self, in.itri);
         out.rad = divs(c, cos_term(S, out));
         out.dP = p;
+        out.delta = true;
     } else {
         out.rad = mk(0, 0, 0);
         out.d = mk(0, 0, 0);
@@ -492,6 +496,7 @@ __device__ __forceinline__ PRay scatter_refractive(const RenderScene& S, int sel
         }
     }
     out.d = normalize(out.d);
+    out.delta = true;
     return out;
 }
 
@@ -826,6 +831,11 @@ __device__ __forceinline__ PRay light_sample(const RenderScene& S, PathRng& g) {
     if (li == S.nlights) li--;
     const int o = __ldg(&S.light_obj[li]);
     const uint32_t tb = __ldg(&S.objs[o].tri_begin), tc = __ldg(&S.objs[o].tri_count);
+    if (tc == 0) {  // an emitter without triangles: a dead sample (abstractObj.cpp:20-24)
+        r.d = mk(0, 0, 0);
+        r.rad = mk(0, 0, 0);
+        return r;
+    }
     const float ra = g.next() * __ldg(&S.obj_area[o]);
     uint32_t ti = lower_bound_dev(S.tri_thresh, tb, tc, ra);
     if (ti == tc) ti--;
