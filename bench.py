@@ -13,6 +13,11 @@ Prints ONE JSON line (rank 0).  Workloads:
       Mpaths/s and the time to relMSE 1e-3 of both are reported beside it).
   kd  closest-hit microbenchmark: level-8 displaced icosphere (1,310,720
       triangles), 2^24 rays; one step = all rays.  Metric: Mrays/s.
+  bpt bidirectional path tracing (WR_MODE_BIDIRECTIONAL) of the Cornell box,
+      256x256, max path length 8; one step = one render call of 16 samples
+      per pixel (1,048,576 eye + light sub-path pairs, all connections).
+      Metric: Msamples/s (the unidirectional megakernel on the same scene
+      beside it).
 
 `value` is device-timed with CUDA events per step on the launching stream,
 with the L2 flushed (a 512 MiB write) before every step and inputs resident
@@ -337,6 +342,107 @@ def reference_pt(args):
 
 
 # ---------------------------------------------------------------------------
+# bpt: the bidirectional renderer on the Cornell box
+# ---------------------------------------------------------------------------
+BPT_SIZE, BPT_DEPTH, BPT_SPP = 256, 8, 16
+METRIC_BPT = "Msamples/s (bidirectional path tracing: eye + light sub-path pairs, all connections; Cornell 256^2)"
+
+
+def bpt_scene():
+    from walkray_gb300 import scenes as S
+
+    return S.cornell(BPT_SIZE, BPT_SIZE)
+
+
+def cpu_baseline_bpt(scene, spp: int, threads: int):
+    import wr_oracle
+
+    orc = wr_oracle.SceneOracle(scene)
+    t0 = time.perf_counter()
+    orc.render_bpt(spp, BPT_DEPTH, seed=1, threads=threads)
+    dt = time.perf_counter() - t0
+    n = BPT_SIZE * BPT_SIZE * spp
+    return {"value": n / dt / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
+            "sample": f"{spp} spp of the {BPT_SIZE}^2 Cornell box ({n} samples), WalkRay's "
+                      f"BidirectionalPathTracer restated in C (oracle), {threads} OpenMP threads, tree build excluded"}
+
+
+def run_bpt(args, world, rank, local):
+    import torch
+
+    from walkray_gb300.api import Context
+
+    torch.cuda.set_device(local)
+    scene = bpt_scene()
+    npix = BPT_SIZE * BPT_SIZE
+    ctx = Context(device=local)
+    sid = ctx.upload(scene)
+    stream = torch.cuda.Stream()
+    film = torch.zeros(npix * 3, dtype=torch.float32, device="cuda")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    seed = 2000 + rank
+
+    def step_mode(mode):
+        return lambda i: ctx.render_device(sid, BPT_SPP, BPT_DEPTH, film.data_ptr(), seed=seed, mode=mode,
+                                           spp_offset=i * BPT_SPP, stream=stream.cuda_stream)
+
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup):
+            step_mode("bidirectional")(i)
+            step_mode("megakernel")(i)
+    torch.cuda.synchronize()
+    barrier(world)
+    with ClockSampler(local) as clk:
+        l0 = launches(ctx)
+        ms = timed_steps(step_mode("bidirectional"), args.steps, stream, flush)
+        n_launch = launches(ctx) - l0
+        ms_pt = timed_steps(step_mode("megakernel"), args.steps, stream, flush)
+    ms_max = allreduce(world, ms, "max")
+    samples = float(npix * BPT_SPP * args.steps)
+    value = allreduce(world, samples, "sum") / (ms_max / 1e3) / 1e6
+    pt_value = allreduce(world, samples, "sum") / (allreduce(world, ms_pt, "max") / 1e3) / 1e6
+    barrier(world)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        ctx.render(sid, BPT_SPP, BPT_DEPTH, seed=seed + 1, mode="bidirectional", spp_offset=i * BPT_SPP)
+    e2e_s = allreduce(world, time.perf_counter() - t0, "max")
+    e2e = allreduce(world, samples, "sum") / e2e_s / 1e6
+    line = {
+        "metric": METRIC_BPT, "value": round(value, 3), "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (MIS products f64, as the reference)",
+        "data": "synthetic (seeded scene generator)",
+        "config": {"workload": f"bpt: Cornell box {BPT_SIZE}x{BPT_SIZE}, max depth {BPT_DEPTH}, {BPT_SPP} spp per step "
+                               "(one render call), BidirectionalPathTracer semantics",
+                   "l2": "flushed (512 MiB write) before every step", "parallelism": f"replicas x{world}"},
+        "e2e": {"value": round(e2e, 3), "unit": "Msamples/s", "h2d_bytes_per_step": 256 + 4 * 257,
+                "d2h_bytes_per_step": npix * 12},
+        "unidirectional_megakernel": {"value": round(pt_value, 2), "unit": "Mpaths/s",
+                                      "ms_per_step": round(ms_pt / args.steps, 3)},
+        "samples_per_step": npix * BPT_SPP, "gpu_launches": int(n_launch), "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline_bpt(scene, args.cpu_rows or 2, os.cpu_count() or 1)
+    ctx.close()
+    return line
+
+
+def reference_bpt(args):
+    scene = bpt_scene()
+    threads = os.cpu_count() or 1
+    spp = args.cpu_rows or 1
+    vals = [cpu_baseline_bpt(scene, spp, threads) for _ in range(args.steps)]
+    v = statistics.median(x["value"] for x in vals)
+    return {"metric": METRIC_BPT, "value": round(v, 4), "unit": "Msamples/s", "impl": "reference", "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+            "config": {"workload": f"bpt: Cornell box {BPT_SIZE}x{BPT_SIZE}, max depth {BPT_DEPTH}",
+                       "samples_per_step": BPT_SIZE * BPT_SIZE * spp},
+            "cpu_baseline": dict(vals[0], value=round(v, 4)),
+            "e2e": {"value": round(v, 4), "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+# ---------------------------------------------------------------------------
 # serve: a seeded Poisson stream of render requests through the serving loop
 # ---------------------------------------------------------------------------
 SERVE_RATE = 20.0                       # requests per second
@@ -649,7 +755,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["pt", "kd", "serve", "relmse"], default=os.environ.get("WR_BENCH_WORKLOAD", "pt"))
+    ap.add_argument("--workload", choices=["pt", "kd", "serve", "relmse", "bpt"], default=os.environ.get("WR_BENCH_WORKLOAD", "pt"))
     ap.add_argument("--tune", action="store_true", help="run the wavefront autotuner first (pt)")
     ap.add_argument("--quick", action="store_true", help="skip the roofline profile, relMSE and CPU legs (pt)")
     ap.add_argument("--cpu-sample", type=int, default=0)
@@ -668,7 +774,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        line = reference_pt(args) if args.workload == "pt" else reference_kd(args)
+        line = {"pt": reference_pt, "kd": reference_kd, "bpt": reference_bpt}.get(args.workload, reference_pt)(args)
         print(json.dumps(line), flush=True)
         return
     if world > 1:
@@ -678,7 +784,7 @@ def main():
     from walkray_gb300 import build
 
     build.build_lib()
-    run = {"pt": run_pt, "kd": run_kd, "serve": run_serve, "relmse": run_relmse}[args.workload]
+    run = {"pt": run_pt, "kd": run_kd, "serve": run_serve, "relmse": run_relmse, "bpt": run_bpt}[args.workload]
     line = run(args, world, rank, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
