@@ -2,16 +2,21 @@
 // (BidirectionalPathTracer, bidirPathTracer.cpp:10-313) on the GPU.
 //
 // One render call runs in batches of samples-per-pixel; a batch of B samples
-// of every pixel is three kernels:
+// of every pixel is five kernels:
 //
 //   k_bpt_subpaths  one thread per (pixel, sample): the eye sub-path
 //                   (Camera::generateRay + MCRenderer::samplePath) and the
 //                   light sub-path (Scene::genLightSample + samplePath), every
 //                   ray record written to HBM (64 B per vertex, vertex-major so
 //                   that a warp's stores of vertex k are contiguous);
-//   k_bpt_connect   one thread per (pixel, sample): every (light length,
-//                   eye length) pair of throughputByConnecting — connectEdge,
-//                   the visibility ray (traced inline), connectingColorProb
+//   k_bpt_enum      one thread per (pixel, sample): the (light length, eye
+//                   length) pairs that pass throughputByConnecting's path-shape
+//                   tests, appended to a candidate list in runs of one pair;
+//   k_bpt_visible   persistent, one candidate per thread and step: connectEdge
+//                   and the visibility ray (MCRenderer::visibilityTest); the
+//                   visible ones are appended to the contributing list;
+//   k_bpt_connect   persistent, one contributing connection per thread and
+//                   step: connectEdge again, connectingColorProb
 //                   and the balance-heuristic weight of connectingMisWeight
 //                   (FP64 products, as the reference) — adding to the sample's
 //                   image: its own pixel, or, for one-vertex eye sub-paths, the
@@ -84,9 +89,26 @@ struct BptParams {
     float pf;             // traversal prune factor
     int stack_cap;
     VtxStore eye, light;
-    uint32_t* counts;     // per sample: eye records | light records << 8
+    uint32_t* counts;     // per sample: eye records | light records << 8 (bytes 0 and 1, little-endian)
     float* film;          // per sample slot of the batch: npix * 3 floats
+    uint2* cand;          // connection candidates with a light sub-path (l >= 1): {sample, l | e << 8}
+    uint2* vis;           // connections that contribute: visible candidates and whole eye paths
+    unsigned long long* ncand;  // [0]: entries of cand, [1]: entries of vis
 };
+
+// appends `item` for the lanes with `ok` at consecutive places of list[*count++]
+// (one atomic per warp); every lane of the warp must call it
+__device__ __forceinline__ void warp_append(bool ok, uint2 item, uint2* list, unsigned long long* count) {
+    constexpr unsigned FULL = 0xffffffffu;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned want = __ballot_sync(FULL, ok);
+    if (!want) return;
+    const int leader = __ffs(want) - 1;
+    unsigned long long base = 0;
+    if ((int)lane == leader) base = atomicAdd(count, (unsigned long long)__popc(want));
+    base = __shfl_sync(FULL, base, leader);
+    if (ok) list[base + __popc(want & ((1u << lane) - 1u))] = item;
+}
 
 // MCRenderer::samplePath (mcRenderer.cpp:16-57) from `prev` (its hit set),
 // every record stored; returns the record count (at most max_path_len + 2)
@@ -130,6 +152,7 @@ __device__ int bpt_sample_path(const RenderScene& S, const BptParams& P, const V
     return n;
 }
 
+// blockIdx.y = 0: eye sub-paths, 1: light sub-paths (one kind per warp)
 __global__ void __launch_bounds__(128) k_bpt_subpaths(RenderScene S, BptParams P, unsigned int* __restrict__ err) {
     extern __shared__ uint32_t s_stack[];
     uint32_t* stack = s_stack + threadIdx.x;
@@ -137,17 +160,19 @@ __global__ void __launch_bounds__(128) k_bpt_subpaths(RenderScene S, BptParams P
     const uint32_t sid = blockIdx.x * blockDim.x + threadIdx.x;
     if (sid >= P.nsamp) return;
     const uint32_t pixel = sid % P.npix, sample = P.s0 + sid / P.npix;
-    // eye sub-path: the camera ray is traced without a condition (camera.cpp:52)
-    PathRng g;
-    g.init(P.seed, pixel, sample, 0);
-    PRay cam = camera_ray(S.cam, pixel, g);
-    {
+    if (blockIdx.y == 0) {
+        // eye sub-path: the camera ray is traced without a condition (camera.cpp:52)
+        PathRng g;
+        g.init(P.seed, pixel, sample, 0);
+        PRay cam = camera_ray(S.cam, pixel, g);
         RayQ q = make_rayq(cam.o, cam.d, S.tree.scene_mag);
         q.pf = P.pf;
         const Hit h = trace_closest<false, true>(S.tree, q, -1, -1, stack, stride, P.stack_cap, err);
         set_hit(S, cam, h);
+        const int ne = bpt_sample_path(S, P, P.eye, sid, cam, g, stack, stride, err);
+        reinterpret_cast<uint8_t*>(P.counts + sid)[0] = (uint8_t)ne;
+        return;
     }
-    const int ne = bpt_sample_path(S, P, P.eye, sid, cam, g, stack, stride, err);
     // light sub-path (Scene::genLightSample -> AbstractObject::genSurfaceSample,
     // abstractObj.cpp:18-52): the emitted ray is traced with NoSelfCondition
     int nl = 0;
@@ -166,7 +191,7 @@ __global__ void __launch_bounds__(128) k_bpt_subpaths(RenderScene S, BptParams P
         }
         nl = bpt_sample_path(S, P, P.light, sid, lr, gl, stack, stride, err);
     }
-    P.counts[sid] = (uint32_t)ne | ((uint32_t)nl << 8);
+    reinterpret_cast<uint8_t*>(P.counts + sid)[1] = (uint8_t)nl;
 }
 
 // ---------------------------------------------------------------------------
@@ -261,38 +286,39 @@ __device__ __forceinline__ PRay link(const Conn& C, int start, bool reverse, con
 // (AbstractObject::evalOriginProbability, abstractObj.cpp:54-59)
 __device__ float bpt_mis_weight(const RenderScene& S, const Conn& C, uint32_t pixel, double* rev) {
     const int n = C.n, c = C.c;
-    // reverse densities, eye end first
-    rev[n - 1] = C.v(n - 1).oP;
+    // reverse densities, eye end first (each record read once: a window
+    // v2 = v(i + 2), v1 = v(i + 1), vi = v(i) slides towards the light)
+    PRay v1 = C.v(n - 1), v2 = v1;
+    rev[n - 1] = v1.oP;
     for (int i = n - 2; i >= 0; i--) {
-        const PRay vi = C.v(i), v1 = C.v(i + 1);
+        const PRay vi = C.v(i);
         const float dist = max_eps(length(v1.o - vi.o));
         const PRay lr = link(C, i, false, vi, v1);
         rev[i] = rev[i + 1] * (double)pdf_w_to_a(dist, cos_term(S, lr));
-        if (v1.delta) continue;
-        float dirp;
-        if (i < n - 2) {
-            const PRay v2 = C.v(i + 2);
-            const PRay a = link(C, i + 2, true, v2, v1), b = link(C, i + 1, true, v1, vi);
-            dirp = bpt_dir_prob(S, a.d, b, false, pixel);
-        } else {
-            dirp = bpt_dir_prob(S, v1.d, v1, true, pixel);  // vertex n-1 is the camera, never re-pointed
+        if (!v1.delta) {
+            float dirp;
+            if (i < n - 2) {
+                const PRay a = link(C, i + 2, true, v2, v1), b = link(C, i + 1, true, v1, vi);
+                dirp = bpt_dir_prob(S, a.d, b, false, pixel);
+            } else {
+                dirp = bpt_dir_prob(S, v1.d, v1, true, pixel);  // vertex n-1 is the camera, never re-pointed
+            }
+            rev[i] *= (double)dirp;
         }
-        rev[i] *= (double)dirp;
+        v2 = v1;
+        v1 = vi;
     }
     // direct densities, light end first, with the sum over techniques
-    double dir = C.v(0).oP, all = 0.0, self = c == -1 ? rev[0] : 0.0;
+    // (window pm2 = v(i - 2), pm1 = v(i - 1), vi = v(i), vn = v(i + 1))
+    PRay pm1 = v1, pm2 = v1, vi = C.v(1);
+    double dir = pm1.oP, all = 0.0, self = c == -1 ? rev[0] : 0.0;
     bool can_connect = false;
-    PRay pm2 = C.v(0), pm1 = pm2;
-    {
-        const PRay v1 = C.v(1);
-        if (!pm1.delta && !v1.delta) {
-            all += dir * rev[1];
-            can_connect = true;
-        }
-        if (c == 0) self = dir * rev[1];
+    if (!pm1.delta && !vi.delta) {
+        all += dir * rev[1];
+        can_connect = true;
     }
+    if (c == 0) self = dir * rev[1];
     for (int i = 1; i < n; i++) {
-        const PRay vi = C.v(i);
         const float dist = max_eps(length(vi.o - pm1.o));
         const PRay lr = link(C, i, true, vi, pm1);
         dir = dir * (double)pdf_w_to_a(dist, cos_term(S, lr));
@@ -307,8 +333,9 @@ __device__ float bpt_mis_weight(const RenderScene& S, const Conn& C, uint32_t pi
             }
             dir *= (double)dirp;
         }
+        PRay vn = vi;
         if (i < n - 1) {
-            const PRay vn = C.v(i + 1);
+            vn = C.v(i + 1);
             if (!vi.delta && !vn.delta) {
                 all += dir * rev[i + 1];
                 can_connect = true;
@@ -317,24 +344,25 @@ __device__ float bpt_mis_weight(const RenderScene& S, const Conn& C, uint32_t pi
         }
         pm2 = pm1;
         pm1 = vi;
+        vi = vn;
     }
     if (!can_connect) all += rev[0];
     const double w = self / all;
     return (float)(w > 0.0 ? w : 0.0);
 }
 
-// BidirectionalPathTracer::connectingColorProb (bidirPathTracer.cpp:267-290)
+// BidirectionalPathTracer::connectingColorProb (bidirPathTracer.cpp:267-290),
+// each record read once (prev = v(i - 1), cur = v(i), nx = v(i + 1))
 __device__ void bpt_color_prob(const RenderScene& S, const Conn& C, f3& color, float& prob) {
     const int n = C.n, c = C.c;
     f3 col = mk(1, 1, 1);
     float pr = 1.f;
-    PRay prev = C.v(0), cur = prev;
+    PRay cur = C.v(0), prev = cur;
     for (int i = 0; i < n; i++) {
-        cur = i == 0 ? prev : C.v(i);
+        const PRay nx = i + 1 < n ? C.v(i + 1) : cur;
         col = vmul(col, cur.rad);
         float dist = 0.f;
         if (i <= c) {
-            const PRay nx = C.v(i + 1);
             dist = max_eps(length(cur.o - nx.o));
             col = vmul(col, radiance_decay(S, cur, dist));
             if (i == c) col = col * (cos_term(S, cur) * cos_term(S, nx) / (dist * dist));
@@ -345,6 +373,7 @@ __device__ void bpt_color_prob(const RenderScene& S, const Conn& C, f3& color, f
         if (i != c && i != c + 1) col = col * cos_term(S, cur);
         pr *= cur.dP * cur.oP;
         prev = cur;
+        cur = nx;
     }
     color = col;
     prob = pr;
@@ -375,98 +404,163 @@ __device__ __forceinline__ void film_add(float* f, uint32_t pid, f3 c) {
     atomicAdd(f + 3 * (size_t)pid + 2, c.z);
 }
 
-__global__ void __launch_bounds__(128) k_bpt_connect(RenderScene S, BptParams P, unsigned int* __restrict__ err) {
+// The path-shape tests of throughputByConnecting (bidirPathTracer.cpp:74-103)
+// for every (light length l, eye length e) pair of a sample, from one word
+// per record: the connected path must start at an emitter; a whole eye path
+// (l = 0) counts only if no two neighbours are both non-delta; no emitter
+// may sit at a connection vertex; connectEdge needs both connection vertices
+// non-delta.  Passing pairs with a light sub-path go to the candidate list
+// (their visibility is tested next), whole eye paths straight to the list of
+// contributing connections; e outer and l inner with the same loop bounds in
+// every lane, so that each warp appends runs of one (l, e) pair and the later
+// kernels' warps get uniform work.
+__global__ void __launch_bounds__(128) k_bpt_enum(RenderScene S, BptParams P) {
+    constexpr unsigned FULL = 0xffffffffu;
+    const uint32_t sid = blockIdx.x * blockDim.x + threadIdx.x;
+    int ne = 0, nl = 0;
+    uint32_t emE = 0, dE = 0, emL = 0, dL = 0;  // bit k: record k is an emitter / delta
+    if (sid < P.nsamp) {
+        const uint32_t cnt = __ldg(&P.counts[sid]);
+        ne = (int)(cnt & 0xffu);
+        nl = (int)((cnt >> 8) & 0xffu);
+        for (int k = 0; k < ne; k++) {
+            const uint32_t w = __float_as_uint(__ldg(&P.eye.at(sid, k)[3].w));
+            emE |= (uint32_t)emissive(S, (int)(w & 0x7fffffffu) - 2) << k;
+            dE |= (w >> 31) << k;
+        }
+        for (int k = 0; k < nl; k++) {
+            const uint32_t w = __float_as_uint(__ldg(&P.light.at(sid, k)[3].w));
+            emL |= (uint32_t)emissive(S, (int)(w & 0x7fffffffu) - 2) << k;
+            dL |= (w >> 31) << k;
+        }
+    }
+    const int nrec = (int)P.max_path_len + 2;
+    for (int e = 1; e <= nrec; e++) {
+        for (int l = 0; l <= nrec; l++) {
+            bool ok = e <= ne && l <= nl && l + e >= 2;
+            if (ok) {
+                if (l == 0) {
+                    const uint32_t m = ~dE & (e < 32 ? (1u << e) - 1u : FULL);
+                    ok = ((emE >> (e - 1)) & 1u) && (m & (m >> 1)) == 0;
+                } else {
+                    ok = (emL & 1u) && !(l > 1 && ((emL >> (l - 1)) & 1u)) && !((emE >> (e - 1)) & 1u) &&
+                         !((dL >> (l - 1)) & 1u) && !((dE >> (e - 1)) & 1u);
+                }
+            }
+            const uint2 item = make_uint2(sid, (uint32_t)l | ((uint32_t)e << 8));
+            if (l == 0) warp_append(ok, item, P.vis, P.ncand + 1);
+            else warp_append(ok, item, P.cand, P.ncand);
+        }
+    }
+}
+
+// connectEdge (bidirPathTracer.cpp:293-312): the connection vertices of the
+// (l >= 1, e) connection, pointed at each other, with their new radiance,
+// direction probability and inside objects
+__device__ __forceinline__ void bpt_connect_edge(const RenderScene& S, const BptParams& P, uint32_t sid, int l, int e,
+                                                 PRay& lc, PRay& ec) {
+    lc = P.light.get(sid, l - 1);
+    ec = P.eye.get(sid, e - 1);
+    const PRay pl = l - 1 > 0 ? P.light.get(sid, l - 2) : lc;
+    const PRay pe = e >= 2 ? P.eye.get(sid, e - 2) : ec;
+    lc.d = normalize(ec.o - lc.o);
+    ec.d = -lc.d;
+    lc.dP = 1.f;
+    lc.delta = false;
+    lc.rad = bpt_eval_bsdf(S, l - 1 > 0 ? pl.d : lc.d, lc);
+    if (lc.contact != -1 && l - 1 > 0) lc.inside = dot(lc.cnorm, lc.d) > 0.f ? pl.inside : lc.contact;
+    ec.dP = 1.f;
+    ec.delta = false;
+    ec.rad = bpt_eval_bsdf(S, e >= 2 ? pe.d : ec.d, ec);
+    if (ec.contact != -1 && e >= 2) ec.inside = dot(ec.cnorm, ec.d) > 0.f ? pe.inside : ec.contact;
+}
+
+// MCRenderer::visibilityTest (mcRenderer.cpp:59-65) of every candidate, from
+// the eye vertex towards the light vertex; the visible ones join the list of
+// contributing connections.  Persistent: the grid strides over the list.
+__global__ void __launch_bounds__(128) k_bpt_visible(RenderScene S, BptParams P, unsigned int* __restrict__ err) {
     extern __shared__ uint32_t s_stack[];
     uint32_t* stack = s_stack + threadIdx.x;
     const int stride = blockDim.x;
-    const uint32_t sid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sid >= P.nsamp) return;
+    const unsigned long long total = P.ncand[0];
+    const unsigned long long step = (unsigned long long)gridDim.x * blockDim.x;
+    // every lane runs the same number of turns (warp_append needs the whole warp)
+    const unsigned long long turns = (total + step - 1) / step;
+    for (unsigned long long t = 0; t < turns; t++) {
+        const unsigned long long i = t * step + (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+        bool ok = false;
+        uint2 c = make_uint2(0, 0);
+        if (i < total) {
+            c = P.cand[i];
+            PRay lc, ec;
+            bpt_connect_edge(S, P, c.x, (int)(c.y & 0xffu), (int)(c.y >> 8), lc, ec);
+            RayQ q = make_rayq(ec.o, ec.d, S.tree.scene_mag);
+            q.pf = P.pf;
+            const Hit h = trace_closest<true, true>(S.tree, q, ec.inside, ec.contact, stack, stride, P.stack_cap, err);
+            ok = h.slot < 0 || (double)(h.t - length(ec.o - lc.o)) >= -EPS_D;
+        }
+        warp_append(ok, c, P.vis, P.ncand + 1);
+    }
+}
+
+// One contributing connection (sample sid, light length l, eye length e) of
+// throughputByConnecting: connectEdge, the colour / probability product and
+// the MIS weight, added to the sample's image.
+__device__ void bpt_connect_one(const RenderScene& S, const BptParams& P, uint32_t sid, int l, int e) {
+    const int W = l + e;
     const uint32_t pixel = sid % P.npix;
     float* film = P.film + 3 * (size_t)P.npix * (sid / P.npix);
-    const uint32_t cnt = P.counts[sid];
-    const int ne = (int)(cnt & 0xffu), nl = (int)(cnt >> 8);
-    double rev[2 * BPT_MAX_RECORDS];
-    f3 own = mk(0, 0, 0);
     Conn C;
     C.eye = P.eye;
     C.light = P.light;
     C.sid = sid;
-    for (int W = 2; W <= ne + nl; W++) {
-        const int lmin = W - ne > 0 ? W - ne : 0;
-        const int lmax = W - 1 >= nl ? nl : W - 1;
-        for (int l = lmin; l <= lmax; l++) {
-            const int e = W - l;
-            C.l = l;
-            C.e = e;
-            C.n = W;
-            C.c = l - 1;
-            C.mod = false;
-            const PRay first = C.v(0);
-            if (!emissive(S, first.contact)) continue;
-            if (l == 0) {  // a whole eye path: used only if no two neighbours are both non-delta
-                bool can = false;
-                PRay a = first;
-                for (int i = 1; i < W && !can; i++) {
-                    const PRay b = C.v(i);
-                    can = !a.delta && !b.delta;
-                    a = b;
-                }
-                if (can) continue;
-            } else {
-                // connectEdge (bidirPathTracer.cpp:293-312)
-                PRay lc = P.light.get(sid, l - 1), ec = P.eye.get(sid, e - 1);
-                if (l > 1 && emissive(S, lc.contact)) continue;
-                if (emissive(S, ec.contact)) continue;
-                if (lc.delta || ec.delta) continue;
-                const PRay pl = l - 1 > 0 ? P.light.get(sid, l - 2) : lc;
-                const PRay pe = e >= 2 ? P.eye.get(sid, e - 2) : ec;
-                lc.d = normalize(ec.o - lc.o);
-                ec.d = -lc.d;
-                lc.dP = 1.f;
-                lc.delta = false;
-                lc.rad = bpt_eval_bsdf(S, l - 1 > 0 ? pl.d : lc.d, lc);
-                if (lc.contact != -1 && l - 1 > 0) lc.inside = dot(lc.cnorm, lc.d) > 0.f ? pl.inside : lc.contact;
-                ec.dP = 1.f;
-                ec.delta = false;
-                ec.rad = bpt_eval_bsdf(S, e >= 2 ? pe.d : ec.d, ec);
-                if (ec.contact != -1 && e >= 2) ec.inside = dot(ec.cnorm, ec.d) > 0.f ? pe.inside : ec.contact;
-                C.lc = lc;
-                C.ec = ec;
-                C.mod = true;
-                // MCRenderer::visibilityTest (mcRenderer.cpp:59-65)
-                RayQ q = make_rayq(ec.o, ec.d, S.tree.scene_mag);
-                q.pf = P.pf;
-                const Hit h = trace_closest<true, true>(S.tree, q, ec.inside, ec.contact, stack, stride, P.stack_cap, err);
-                if (!(h.slot < 0 || (double)(h.t - length(ec.o - lc.o)) >= -EPS_D)) continue;
-            }
-            f3 col;
-            float prob;
-            bpt_color_prob(S, C, col, prob);
-            if (prob == 0.f) continue;
-            if (length(col) == 0.f) continue;
-            const float w = bpt_mis_weight(S, C, pixel, rev);
-            f3 contrib = divs(col, prob) * w;
-            if (e > 1) {
-                own = own + contrib;
-            } else {  // the light vertex seen by the camera: splat where it projects
-                const PRay cr = C.v(W - 1), lv = C.v(W - 2);
-                uint32_t pid;
-                if (bpt_raster(S.cam, lv.o, cr.o, &pid)) {
-                    float sa;
-                    if (S.cam.lens_radius > 0.f) {  // Camera::computeSolidAngle (camera.cpp:133-142)
-                        const float ct = dot(normalize(lv.o - cr.o), S.cam.front);
-                        sa = S.cam.ipd / powf(S.cam.ipd / ct, 3.f);
-                    } else {
-                        sa = pixel_solid_angle(S.cam, pid);
-                    }
-                    const float f = (float)(1.0 / (double)sa);
-                    contrib = contrib * (f / (float)P.npix);
-                    film_add(film, pid, contrib);
-                }
-            }
-        }
+    C.l = l;
+    C.e = e;
+    C.n = W;
+    C.c = l - 1;
+    C.mod = false;
+    if (l > 0) {
+        bpt_connect_edge(S, P, sid, l, e, C.lc, C.ec);
+        C.mod = true;
     }
-    if (own.x != 0.f || own.y != 0.f || own.z != 0.f) film_add(film, pixel, own);
+    f3 col;
+    float prob;
+    bpt_color_prob(S, C, col, prob);
+    if (prob == 0.f) return;
+    if (length(col) == 0.f) return;
+    double rev[2 * BPT_MAX_RECORDS];
+    const float w = bpt_mis_weight(S, C, pixel, rev);
+    f3 contrib = divs(col, prob) * w;
+    if (contrib.x == 0.f && contrib.y == 0.f && contrib.z == 0.f) return;
+    if (e > 1) {
+        film_add(film, pixel, contrib);
+        return;
+    }
+    // the light vertex seen by the camera: splat where it projects
+    const PRay cr = C.v(W - 1), lv = C.v(W - 2);
+    uint32_t pid;
+    if (!bpt_raster(S.cam, lv.o, cr.o, &pid)) return;
+    float sa;
+    if (S.cam.lens_radius > 0.f) {  // Camera::computeSolidAngle (camera.cpp:133-142)
+        const float ct = dot(normalize(lv.o - cr.o), S.cam.front);
+        sa = S.cam.ipd / powf(S.cam.ipd / ct, 3.f);
+    } else {
+        sa = pixel_solid_angle(S.cam, pid);
+    }
+    const float f = (float)(1.0 / (double)sa);
+    contrib = contrib * (f / (float)P.npix);
+    film_add(film, pid, contrib);
+}
+
+// persistent: the grid strides over the contributing connections, 32
+// consecutive ones (mostly one (l, e) pair) per warp
+__global__ void __launch_bounds__(128) k_bpt_connect(RenderScene S, BptParams P) {
+    const unsigned long long total = P.ncand[1];
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint2 c = P.vis[i];
+        bpt_connect_one(S, P, c.x, (int)(c.y & 0xffu), (int)(c.y >> 8));
+    }
 }
 
 // each sample's image: isLegalColor, fixVignetting, into the caller's film
@@ -500,7 +594,7 @@ __global__ void k_bpt_resolve(CamParams cam, float* __restrict__ film, uint32_t 
 // host side
 // ---------------------------------------------------------------------------
 struct BptState {
-    DeviceBuffer eye, light, counts, film;
+    DeviceBuffer eye, light, counts, film, cand, vis;
 };
 
 int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& RP, uint32_t spp_offset,
@@ -513,14 +607,16 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
     const uint32_t nrec = RP.max_path_len + 2;
     // a batch of whole samples-per-pixel: vertex records of both sub-paths
     // (64 B each), the counts and the batch's images in about 1 GiB
-    const size_t per_sample = 2ull * nrec * 64 + 4 + 12;
+    const size_t per_sample = 2ull * nrec * 64 + 4 + 12 + 16ull * nrec * (nrec + 1);
     const uint64_t max_samples = std::max<uint64_t>(npix, (1ull << 30) / per_sample);
     const uint32_t per_batch = (uint32_t)std::min<uint64_t>(spp, std::max<uint64_t>(1, max_samples / npix));
     const uint64_t nsamp = (uint64_t)npix * per_batch;
     if (nsamp > 0xffffffffull) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "image too large");
     WR_CUDA(ctx, st.eye.reserve(64ull * nrec * nsamp));
     WR_CUDA(ctx, st.light.reserve(64ull * nrec * nsamp));
-    WR_CUDA(ctx, st.counts.reserve(4ull * nsamp));
+    WR_CUDA(ctx, st.counts.reserve(4ull * nsamp + 24));
+    WR_CUDA(ctx, st.cand.reserve(8ull * nrec * (nrec + 1) * nsamp));
+    WR_CUDA(ctx, st.vis.reserve(8ull * nrec * (nrec + 1) * nsamp));
     const size_t film_bytes = 12ull * nsamp;
     if (st.film.bytes < film_bytes) {
         WR_CUDA(ctx, st.film.reserve(film_bytes));
@@ -536,25 +632,39 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
     P.light.base = st.light.as<float4>();
     P.counts = st.counts.as<uint32_t>();
     P.film = st.film.as<float>();
+    P.cand = st.cand.as<uint2>();
+    P.vis = st.vis.as<uint2>();
+    // the two list counters live after the per-sample counts (8-byte aligned)
+    P.ncand = reinterpret_cast<unsigned long long*>(st.counts.as<char>() + ((4ull * nsamp + 7) & ~7ull));
     const int block = 128;
     const size_t smem = (size_t)RP.stack_cap * block * sizeof(uint32_t);
     if (smem > 48 * 1024) {
         WR_CUDA(ctx, cudaFuncSetAttribute(k_bpt_subpaths, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        WR_CUDA(ctx, cudaFuncSetAttribute(k_bpt_connect, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        WR_CUDA(ctx, cudaFuncSetAttribute(k_bpt_visible, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     }
+    int per_sm = 0, per_sm_v = 0;
+    WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bpt_connect, block, 0));
+    WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_v, k_bpt_visible, block, smem));
+    const int connect_grid = std::max(1, per_sm) * std::max(1, ctx->num_sms);
+    const int visible_grid = std::max(1, per_sm_v) * std::max(1, ctx->num_sms);
     for (uint32_t done = 0; done < spp; done += per_batch) {
         const uint32_t b = std::min(per_batch, spp - done);
         P.s0 = spp_offset + done;
         P.nsamp = npix * b;
         P.eye.nsamp = P.light.nsamp = P.nsamp;
         const int grid = (int)((P.nsamp + block - 1) / block);
-        k_bpt_subpaths<<<grid, block, smem, stream>>>(S, P, err);
+        k_bpt_subpaths<<<dim3(grid, 2), block, smem, stream>>>(S, P, err);
         WR_CUDA(ctx, cudaGetLastError());
-        k_bpt_connect<<<grid, block, smem, stream>>>(S, P, err);
+        WR_CUDA(ctx, cudaMemsetAsync(P.ncand, 0, 2 * sizeof(unsigned long long), stream));
+        k_bpt_enum<<<grid, block, 0, stream>>>(S, P);
+        WR_CUDA(ctx, cudaGetLastError());
+        k_bpt_visible<<<visible_grid, block, smem, stream>>>(S, P, err);
+        WR_CUDA(ctx, cudaGetLastError());
+        k_bpt_connect<<<connect_grid, block, 0, stream>>>(S, P);
         WR_CUDA(ctx, cudaGetLastError());
         k_bpt_resolve<<<(npix + 255) / 256, 256, 0, stream>>>(S.cam, P.film, npix, b, d_sum, d_sumsq);
         WR_CUDA(ctx, cudaGetLastError());
-        ctx->kernel_launches += 3;
+        ctx->kernel_launches += 5;
     }
     return WR_OK;
 }
