@@ -196,6 +196,11 @@ int wr_trace_closest_device(wr_ctx* ctx, wr_scene_id scene, const float* d_rays,
                                     sub-paths, all connections, balance-heuristic MIS, light tracing;
                                     surfaces only (participating media: WR_ERR_UNSUPPORTED),
                                     max_path_len <= 30 */
+#define WR_MODE_VCM 3u           /* VCMTracer (vcmTracer.cpp:6-446): the bidirectional connections with
+                                    VCM weights plus vertex merging of every eye vertex with the light
+                                    points within the iteration's radius (the reference's hash grid);
+                                    wr_render_desc.radius is the base radius (VCMTracer::setRadius;
+                                    0 = the reference's default 0.01); surfaces only, max_path_len <= 30 */
 
 #define WR_RENDER_NEE 1u      /* PathTracer's next-event-estimation branch (pathTracer.cpp:39-66) */
 /* Rendering traverses front to back and skips a box whose entry distance is
@@ -213,7 +218,7 @@ typedef struct wr_render_desc {
     uint32_t mode;         /* WR_MODE_* */
     uint32_t flags;        /* WR_RENDER_* */
     uint32_t spp_offset;   /* index of the first sample (progressive rendering / resume) */
-    uint32_t pad;
+    float radius;          /* WR_MODE_VCM: base merge radius (0 = 0.01); ignored otherwise */
 } wr_render_desc;
 
 /* PathTracer::renderPixels (pathTracer.cpp:7-76) on the GPU: rgb_out gets

@@ -50,6 +50,11 @@ def load():
         lib.wro_render_bpt.restype = C.c_int
         lib.wro_render_bpt.argtypes = [C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p,
                                        C.c_void_p, C.c_int, C.POINTER(C.c_uint64)]
+        lib.wro_render_vcm.restype = C.c_int
+        lib.wro_render_vcm.argtypes = [C.c_void_p, C.c_uint32, C.c_uint64, C.c_float, C.c_uint32, C.c_uint32,
+                                       C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_uint64)]
+        lib.wro_vcm_radius.restype = C.c_float
+        lib.wro_vcm_radius.argtypes = [C.c_float, C.c_uint32]
         _lib = lib
     return _lib
 
@@ -149,4 +154,19 @@ class SceneOracle:
                                      C.byref(rays))
         if rc:
             raise ValueError("the bidirectional restatement does not cover participating media")
+        return s, s2, rays.value
+
+    def render_vcm(self, spp: int, max_path_len: int, seed: int, radius: float = 0.01, s0: int = 0,
+                   threads: int = 0, want_sumsq: bool = False):
+        """The restated VCMTracer with base merge radius `radius`: per-pixel
+        sums over samples [s0, s0 + spp), like render()."""
+        c = self.scene.camera
+        npx = c.width * c.height
+        s = np.zeros((npx, 3), np.float64)
+        s2 = np.zeros((npx, 3), np.float64) if want_sumsq else None
+        rays = C.c_uint64()
+        rc = self.lib.wro_render_vcm(self.h, max_path_len, seed, radius, s0, s0 + spp, _p(s), _p(s2), threads,
+                                     C.byref(rays))
+        if rc:
+            raise ValueError("the VCM restatement does not cover participating media")
         return s, s2, rays.value

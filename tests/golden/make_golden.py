@@ -24,10 +24,13 @@ from the reference sources) on small seeded scenes and stores its answers:
   render_bpt_*.npz    BidirectionalPathTracer::renderPixels on the Cornell,
                       mirror, thin-lens and mixed-material scenes, 8
                       reference renders of 64 spp each
+  render_vcm_*.npz    VCMTracer::renderPixels (base radius 0.02) on the
+                      Cornell, mirror and thin-lens scenes, 8 reference
+                      renders of 64 spp each
 
-Usage: python tests/golden/make_golden.py [bpt]   (needs the reference tree on
-this machine; `bpt` remakes only the bidirectional renders; the fixtures it
-writes are what the tests read elsewhere)
+Usage: python tests/golden/make_golden.py [bpt|vcm]   (needs the reference
+tree on this machine; `bpt` / `vcm` remake only those renders; the fixtures
+it writes are what the tests read elsewhere)
 """
 from __future__ import annotations
 
@@ -224,12 +227,25 @@ def bpt_fixtures(td):
         render_set(sc[name], p, td, f"render_bpt_{name}.npz", extra=("bpt",), spp=64)
 
 
+VCM_SCENES = ("cornell", "mirror", "dof")
+VCM_RADIUS = 0.02
+
+
+def vcm_fixtures(td):
+    """VCMTracer::renderPixels (vcmTracer.cpp:6-92), base radius 0.02, 8
+    reference renders of 64 spp per scene, depth 8."""
+    sc = golden_scenes()
+    p = os.path.join(td, "s.wrs")
+    for name in VCM_SCENES:
+        render_set(sc[name], p, td, f"render_vcm_{name}.npz", extra=("vcm", str(VCM_RADIUS)), spp=64)
+
+
 def main():
     if not os.path.exists(REF):
         sys.exit("build the reference harness first: make -C oracle ref")
-    if sys.argv[1:] == ["bpt"]:  # only the bidirectional renders
+    if sys.argv[1:] in (["bpt"], ["vcm"]):  # only the bidirectional / VCM renders
         with tempfile.TemporaryDirectory() as td:
-            bpt_fixtures(td)
+            (bpt_fixtures if sys.argv[1] == "bpt" else vcm_fixtures)(td)
         return
     sc = golden_scenes()
     with tempfile.TemporaryDirectory() as td:
@@ -288,6 +304,7 @@ def main():
         write_xml_fixtures()
         mesh_fixtures(td)
         bpt_fixtures(td)
+        vcm_fixtures(td)
     print("golden fixtures written to", HERE)
 
 

@@ -175,3 +175,31 @@ def test_oracle_bidirectional_refuses_media(built):
     orc = wr_oracle.SceneOracle(make_golden.golden_scenes()["media_small"])
     with pytest.raises(ValueError):
         orc.render_bpt(1, 8, seed=1)
+
+
+@pytest.mark.parametrize("name", ["cornell", "mirror", "dof"])
+def test_oracle_vcm_matches_reference_statistically(built, name):
+    """VCMTracer (vcmTracer.cpp:6-446), base radius 0.02: the restated
+    connections with VCM weights and merges through the reference's hash grid
+    vs 8 reference renders of 64 spp."""
+    g = np.load(os.path.join(GOLDEN, f"render_vcm_{name}.npz"))
+    ref = g["images"].astype(np.float64)
+    s = make_golden.golden_scenes()[name]
+    h, w = s.camera.height, s.camera.width
+    orc = wr_oracle.SceneOracle(s)
+    port = np.stack([(orc.render_vcm(64, 8, seed=600 + k, radius=make_golden.VCM_RADIUS)[0] / 64).reshape(h, w, 3)
+                     for k in range(8)])
+    blk = lambda a: a.reshape(a.shape[0], h // 4, 4, w // 4, 4, 3).mean((2, 4))
+    br, bp = blk(ref), blk(port)
+    z = (br.mean(0) - bp.mean(0)) / np.sqrt(br.var(0, ddof=1) / 8 + bp.var(0, ddof=1) / 8 + 1e-12)
+    assert np.abs(z).max() < 5.0, np.abs(z).max()
+    assert abs(port.mean() / ref.mean() - 1) < 0.015
+
+
+def test_oracle_vcm_radius_schedule(built):
+    """r_s = max(r0 sqrt((s+1)^(alpha-1)), 1e-5) with alpha = 2/3 (vcmTracer.cpp:27)."""
+    lib = wr_oracle.load()
+    for s in (0, 1, 7, 1000):
+        want = np.float32(0.02) * np.sqrt(np.float32(s + 1) ** (np.float32(2.0 / 3) - np.float32(1)))
+        assert abs(lib.wro_vcm_radius(0.02, s) / want - 1) < 1e-6
+    assert lib.wro_vcm_radius(1e-9, 5) == np.float32(1e-5)

@@ -90,7 +90,7 @@ class wr_trace_filter(C.Structure):
 
 class wr_render_desc(C.Structure):
     _fields_ = [("spp", C.c_uint32), ("max_path_len", C.c_uint32), ("seed", C.c_uint64), ("mode", C.c_uint32),
-                ("flags", C.c_uint32), ("spp_offset", C.c_uint32), ("pad", C.c_uint32)]
+                ("flags", C.c_uint32), ("spp_offset", C.c_uint32), ("radius", C.c_float)]
 
 
 class wr_wavefront_config(C.Structure):

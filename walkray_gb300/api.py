@@ -126,24 +126,25 @@ class Context:
 
     # ---- rendering ------------------------------------------------------
     def render(self, sid: int, spp: int, max_path_len: int, seed: int = 1, mode: str = "megakernel",
-               nee: bool = False, spp_offset: int = 0, exact: bool = False) -> np.ndarray:
-        """Mean image (H, W, 3) float32, row 0 at the top (wr_render)."""
+               nee: bool = False, spp_offset: int = 0, exact: bool = False, radius: float = 0.0) -> np.ndarray:
+        """Mean image (H, W, 3) float32, row 0 at the top (wr_render); `radius`
+        is the base merge radius of mode "vcm" (0 = 0.01)."""
         w, h = self._camera_size(sid)
         out = np.empty((h, w, 3), np.float32)
-        d = L.wr_render_desc(spp, max_path_len, seed, MODES[mode], _flags(nee, exact), spp_offset, 0)
+        d = L.wr_render_desc(spp, max_path_len, seed, MODES[mode], _flags(nee, exact), spp_offset, radius)
         self._check(self.lib.wr_render(self.h, sid, C.byref(d), L.ptr(out)))
         return out
 
     def render_device(self, sid: int, spp: int, max_path_len: int, d_sum: int, d_sumsq: int = 0, seed: int = 1,
                       mode: str = "megakernel", nee: bool = False, spp_offset: int = 0, stream: int = 0,
-                      exact: bool = False) -> None:
+                      exact: bool = False, radius: float = 0.0) -> None:
         """Adds spp samples to a device film (wr_render_device), asynchronous on `stream`."""
-        d = L.wr_render_desc(spp, max_path_len, seed, MODES[mode], _flags(nee, exact), spp_offset, 0)
+        d = L.wr_render_desc(spp, max_path_len, seed, MODES[mode], _flags(nee, exact), spp_offset, radius)
         self._check(self.lib.wr_render_device(self.h, sid, C.byref(d), C.c_void_p(d_sum), C.c_void_p(d_sumsq or None),
                                               C.c_void_p(stream or None)))
 
     def render_stats(self, sid: int, spp: int, max_path_len: int, seed: int = 1, mode: str = "megakernel",
-                     nee: bool = False, exact: bool = False):
+                     nee: bool = False, exact: bool = False, radius: float = 0.0):
         """Per-pixel sum and sum of squares (H, W, 3) over spp samples, via torch device buffers."""
         import torch
 
@@ -152,7 +153,7 @@ class Context:
         s2 = torch.zeros((h, w, 3), dtype=torch.float32, device="cuda")
         torch.cuda.synchronize()
         self.render_device(sid, spp, max_path_len, s.data_ptr(), s2.data_ptr(), seed, mode, nee,
-                           stream=torch.cuda.current_stream().cuda_stream, exact=exact)
+                           stream=torch.cuda.current_stream().cuda_stream, exact=exact, radius=radius)
         torch.cuda.synchronize()
         return s.cpu().numpy().astype(np.float64), s2.cpu().numpy().astype(np.float64)
 
@@ -187,7 +188,7 @@ class Context:
         return cam
 
 
-MODES = {"megakernel": 0, "wavefront": 1, "bidirectional": 2}
+MODES = {"megakernel": 0, "wavefront": 1, "bidirectional": 2, "vcm": 3}
 
 
 def _flags(nee: bool, exact: bool) -> int:

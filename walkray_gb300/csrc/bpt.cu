@@ -43,6 +43,7 @@ namespace wr {
 constexpr uint32_t BPT_LIGHT_DIM0 = 0x40000000u;
 constexpr int BPT_MAX_RECORDS = 32;  // records per sub-path: max_path_len + 2
 constexpr double INV_PI_D = 0.31830988618379067153776752674503;
+constexpr double PI_D = 3.1415926535897932384626433832795;
 constexpr double EPS_D = 1e-5;
 
 // ---------------------------------------------------------------------------
@@ -80,6 +81,15 @@ struct VtxStore {
     }
 };
 
+// The weight's technique set: BidirectionalPathTracer's connections only, or
+// VCMTracer's connections and merges (vcmTracer.cpp:225-330) with merge
+// radius `radius` and nVM = pixel count; `merge`: the path was made by a merge.
+struct MisKind {
+    bool vcm, merge;
+    float radius;
+    double nvm;
+};
+
 struct BptParams {
     uint64_t seed;
     uint32_t s0;          // first sample index of the batch
@@ -93,8 +103,25 @@ struct BptParams {
     float* film;          // per sample slot of the batch: npix * 3 floats
     uint2* cand;          // connection candidates with a light sub-path (l >= 1): {sample, l | e << 8}
     uint2* vis;           // connections that contribute: visible candidates and whole eye paths
-    unsigned long long* ncand;  // [0]: entries of cand, [1]: entries of vis
+    unsigned long long* ncand;  // [0]: entries of cand, [1]: entries of vis, [2]: light points
+    // vertex merging (WR_MODE_VCM); per sample slot s of the batch, the hash grid of hashgrid.hxx
+    bool vcm;
+    const float* radii;   // merge radius of each slot's iteration
+    uint2* pts;           // light points {sample, record}
+    int* bbox;            // per slot: ordered-int keys of min x, y, z, max x, y, z
+    int* head;            // per slot: npix buckets, first point or -1
+    int* next;            // per point: next point of its bucket or -1
 };
+
+// the weight's technique set for a sample of this batch
+__device__ __forceinline__ MisKind mis_kind(const BptParams& P, uint32_t sid, bool merge) {
+    MisKind K;
+    K.vcm = P.vcm;
+    K.merge = merge;
+    K.radius = P.vcm ? __ldg(&P.radii[sid / P.npix]) : 0.f;
+    K.nvm = (double)P.npix;
+    return K;
+}
 
 // appends `item` for the lanes with `ok` at consecutive places of list[*count++]
 // (one atomic per warp); every lane of the warp must call it
@@ -260,16 +287,18 @@ __device__ __forceinline__ float pdf_w_to_a(float dist, float cos_there) { retur
 // the connected path y0..y(l-1) x(e-1)..x0 of one (l, e) pair
 struct Conn {
     VtxStore eye, light;
-    uint32_t sid;
+    uint32_t sid, lsid;  // samples of the eye and of the light sub-path (different for a merge)
     int l, e, n, c;
     bool mod;
     PRay lc, ec;  // the connection vertices after connectEdge (when mod)
     __device__ __forceinline__ PRay v(int i) const {
         if (mod && i == c) return lc;
         if (mod && i == c + 1) return ec;
-        return i < l ? light.get(sid, i) : eye.get(sid, e - 1 - (i - l));
+        return i < l ? light.get(lsid, i) : eye.get(sid, e - 1 - (i - l));
     }
 };
+
+
 
 // BidirectionalPathTracer::linkVertex (bidirPathTracer.cpp:226-243) for
 // start in [0, n): the record, pointed at its neighbour on the connecting side
@@ -284,7 +313,7 @@ __device__ __forceinline__ PRay link(const Conn& C, int start, bool reverse, con
 // BidirectionalPathTracer::connectingMisWeight (bidirPathTracer.cpp:142-220),
 // expTerm = 1; the origin densities of surface vertices are 1
 // (AbstractObject::evalOriginProbability, abstractObj.cpp:54-59)
-__device__ float bpt_mis_weight(const RenderScene& S, const Conn& C, uint32_t pixel, double* rev) {
+__device__ float bpt_mis_weight(const RenderScene& S, const Conn& C, uint32_t pixel, double* rev, const MisKind& K) {
     const int n = C.n, c = C.c;
     // reverse densities, eye end first (each record read once: a window
     // v2 = v(i + 2), v1 = v(i + 1), vi = v(i) slides towards the light)
@@ -308,7 +337,8 @@ __device__ float bpt_mis_weight(const RenderScene& S, const Conn& C, uint32_t pi
         v2 = v1;
         v1 = vi;
     }
-    // direct densities, light end first, with the sum over techniques
+    // direct densities, light end first, with the sum over techniques in the
+    // reference's order: connection of (i, i+1), then merge at i+1
     // (window pm2 = v(i - 2), pm1 = v(i - 1), vi = v(i), vn = v(i + 1))
     PRay pm1 = v1, pm2 = v1, vi = C.v(1);
     double dir = pm1.oP, all = 0.0, self = c == -1 ? rev[0] : 0.0;
@@ -321,9 +351,11 @@ __device__ float bpt_mis_weight(const RenderScene& S, const Conn& C, uint32_t pi
     for (int i = 1; i < n; i++) {
         const float dist = max_eps(length(vi.o - pm1.o));
         const PRay lr = link(C, i, true, vi, pm1);
-        dir = dir * (double)pdf_w_to_a(dist, cos_term(S, lr));
+        const float g = pdf_w_to_a(dist, cos_term(S, lr));
+        const double dir_prev = dir;
+        dir = dir * (double)g;
+        float dirp = 1.f;
         if (!pm1.delta) {
-            float dirp;
             if (i > 1) {
                 const PRay a = link(C, i - 2, false, pm2, pm1), b = link(C, i - 1, false, pm1, vi);
                 dirp = bpt_dir_prob(S, a.d, b, false, pixel);
@@ -332,6 +364,16 @@ __device__ float bpt_mis_weight(const RenderScene& S, const Conn& C, uint32_t pi
                 dirp = bpt_dir_prob(S, r.d, r, true, pixel);
             }
             dir *= (double)dirp;
+        }
+        if (K.vcm && i - 1 < n - 2 && !vi.delta) {  // merging at vertex i (vcmTracer.cpp:298-318)
+            double p = dir_prev * rev[i];
+            if (!pm1.delta) p *= (double)dirp;
+            p *= 1.0;  // link(i-1).evalOriginProbability(link(i)): 1 for surfaces
+            p *= (double)g;
+            p *= PI_D * K.radius * K.radius;
+            if (vi.inside >= 0 && vi.contact == -1) p *= 4.0 / 3 * K.radius;
+            if (K.merge && i - 1 == c) self = p;
+            all += p * K.nvm;
         }
         PRay vn = vi;
         if (i < n - 1) {
@@ -347,13 +389,17 @@ __device__ float bpt_mis_weight(const RenderScene& S, const Conn& C, uint32_t pi
         vi = vn;
     }
     if (!can_connect) all += rev[0];
+    if (K.merge) self *= K.nvm;
     const double w = self / all;
-    return (float)(w > 0.0 ? w : 0.0);
+    return (float)(w > 0.0 ? w : 0.0);  // also VCMTracer's `!(w >= 0) -> 0`
 }
 
 // BidirectionalPathTracer::connectingColorProb (bidirPathTracer.cpp:267-290),
 // each record read once (prev = v(i - 1), cur = v(i), nx = v(i + 1))
-__device__ void bpt_color_prob(const RenderScene& S, const Conn& C, f3& color, float& prob) {
+// For a merge (VCMTracer::connectingColorProb, vcmTracer.cpp:357-366) the
+// light vertex's density of landing within `radius` is multiplied in.
+__device__ void bpt_color_prob(const RenderScene& S, const Conn& C, f3& color, float& prob, bool merge = false,
+                               float radius = 0.f) {
     const int n = C.n, c = C.c;
     f3 col = mk(1, 1, 1);
     float pr = 1.f;
@@ -372,6 +418,11 @@ __device__ void bpt_color_prob(const RenderScene& S, const Conn& C, f3& color, f
         }
         if (i != c && i != c + 1) col = col * cos_term(S, cur);
         pr *= cur.dP * cur.oP;
+        if (merge && i == c) {
+            pr = (float)((double)pr * (PI_D * radius * radius));
+            pr *= pdf_w_to_a(dist, cos_term(S, nx));  // link(c + 1, reverse): the eye vertex as connected
+            if (nx.inside >= 0 && nx.contact == -1) pr = (float)((double)pr * (4.0 / 3 * radius));
+        }
         prev = cur;
         cur = nx;
     }
@@ -514,6 +565,7 @@ __device__ void bpt_connect_one(const RenderScene& S, const BptParams& P, uint32
     C.eye = P.eye;
     C.light = P.light;
     C.sid = sid;
+    C.lsid = sid;
     C.l = l;
     C.e = e;
     C.n = W;
@@ -529,7 +581,7 @@ __device__ void bpt_connect_one(const RenderScene& S, const BptParams& P, uint32
     if (prob == 0.f) return;
     if (length(col) == 0.f) return;
     double rev[2 * BPT_MAX_RECORDS];
-    const float w = bpt_mis_weight(S, C, pixel, rev);
+    const float w = bpt_mis_weight(S, C, pixel, rev, mis_kind(P, sid, false));
     f3 contrib = divs(col, prob) * w;
     if (contrib.x == 0.f && contrib.y == 0.f && contrib.z == 0.f) return;
     if (e > 1) {
@@ -561,6 +613,180 @@ __global__ void __launch_bounds__(128) k_bpt_connect(RenderScene S, BptParams P)
         const uint2 c = P.vis[i];
         bpt_connect_one(S, P, c.x, (int)(c.y & 0xffu), (int)(c.y >> 8));
     }
+}
+
+// ---------------------------------------------------------------------------
+// vertex merging (VCMTracer::throughputByMerging, vcmTracer.cpp:175-223) and
+// the reference's hash grid (hashgrid.hxx): npix buckets per iteration, cell
+// size 2 r, the spatial hash of GetCellIndex, the 8 cells nearest a query and
+// a bounding box over every particle — including the npix placeholder points
+// at the origin that VCMTracer's point vector starts with (they never
+// contribute, so only their place in the box is kept: the box starts at the
+// origin).  The buckets are linked lists; a bucket reached through two of the
+// 8 cells is walked twice, as in the reference.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int fkey(float f) {
+    const int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float fkey_inv(int k) { return __int_as_float(k >= 0 ? k : k ^ 0x7fffffff); }
+
+struct GridView {
+    f3 bmin, bmax;
+    float radius, inv_cell;
+    const int* head;  // this slot's buckets
+    uint32_t nb;
+};
+
+__device__ __forceinline__ GridView grid_view(const BptParams& P, uint32_t slot) {
+    GridView G;
+    const int* k = P.bbox + 6 * slot;
+    G.bmin = mk(fkey_inv(k[0]), fkey_inv(k[1]), fkey_inv(k[2]));
+    G.bmax = mk(fkey_inv(k[3]), fkey_inv(k[4]), fkey_inv(k[5]));
+    G.radius = __ldg(&P.radii[slot]);
+    G.inv_cell = 1.f / (G.radius * 2.f);
+    G.head = P.head + (size_t)slot * P.npix;
+    G.nb = P.npix;
+    return G;
+}
+
+// HashGrid::GetCellIndex (hashgrid.hxx:185-202)
+__device__ __forceinline__ uint32_t grid_bucket(const GridView& G, int cx, int cy, int cz) {
+    const uint32_t x = (uint32_t)cx, y = (uint32_t)cy, z = (uint32_t)cz;
+    return ((x * 73856093u) ^ (y * 19349663u) ^ (z * 83492791u)) % G.nb;
+}
+__device__ __forceinline__ uint32_t grid_bucket(const GridView& G, f3 p) {
+    const f3 d = p - G.bmin;
+    return grid_bucket(G, (int)floorf(G.inv_cell * d.x), (int)floorf(G.inv_cell * d.y), (int)floorf(G.inv_cell * d.z));
+}
+
+// The light points of each sample (vcmTracer.cpp:40-54): light records 1..
+// before the first emitter, delta records skipped; their bounding box per slot.
+__global__ void __launch_bounds__(128) k_vcm_points(RenderScene S, BptParams P) {
+    const uint32_t sid = blockIdx.x * blockDim.x + threadIdx.x;
+    int nl = 0;
+    if (sid < P.nsamp) nl = (int)((__ldg(&P.counts[sid]) >> 8) & 0xffu);
+    const int nrec = (int)P.max_path_len + 2;
+    f3 lo = mk(0, 0, 0), hi = mk(0, 0, 0);
+    bool any = false, alive = true;
+    for (int i = 1; i < nrec; i++) {  // equal loop bounds in every lane: warp_append needs the whole warp
+        bool ok = false;
+        uint2 item = make_uint2(sid, (uint32_t)i);
+        if (alive && i < nl) {
+            const PRay r = P.light.get(sid, i);
+            if (emissive(S, r.contact)) alive = false;
+            else if (!r.delta) {
+                ok = true;
+                lo = mk(fminf(lo.x, r.o.x), fminf(lo.y, r.o.y), fminf(lo.z, r.o.z));
+                hi = mk(fmaxf(hi.x, r.o.x), fmaxf(hi.y, r.o.y), fmaxf(hi.z, r.o.z));
+                any = true;
+            }
+        }
+        warp_append(ok, item, P.pts, P.ncand + 2);
+    }
+    if (any) {
+        int* k = P.bbox + 6 * (sid / P.npix);
+        atomicMin(k + 0, fkey(lo.x));
+        atomicMin(k + 1, fkey(lo.y));
+        atomicMin(k + 2, fkey(lo.z));
+        atomicMax(k + 3, fkey(hi.x));
+        atomicMax(k + 4, fkey(hi.y));
+        atomicMax(k + 5, fkey(hi.z));
+    }
+}
+
+// HashGrid::Build: every point into its bucket's list
+__global__ void __launch_bounds__(256) k_vcm_link(BptParams P) {
+    const unsigned long long total = P.ncand[2];
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint2 pt = P.pts[i];
+        const GridView G = grid_view(P, pt.x / P.npix);
+        const f3 pos = xyz(__ldg(P.light.at(pt.x, (int)pt.y)));
+        const uint32_t b = grid_bucket(G, pos);
+        P.next[i] = atomicExch(P.head + (size_t)(pt.x / P.npix) * P.npix + b, (int)i);
+    }
+}
+
+// One merge: light records [0, idx) of sample lsid, then eye records i..0 of
+// sample sid (Query::Process, vcmTracer.cpp:188-201).  Adds w * colour / prob.
+__device__ void vcm_merge_one(const RenderScene& S, const BptParams& P, uint32_t sid, int i, uint32_t lsid, int idx,
+                              double* rev, f3& contrib) {
+    Conn C;
+    C.eye = P.eye;
+    C.light = P.light;
+    C.sid = sid;
+    C.lsid = lsid;
+    C.l = idx;
+    C.e = i + 1;
+    C.n = idx + i + 1;
+    C.c = idx - 1;
+    // connectEdge for a merge (vcmTracer.cpp:375-409): the light record is only
+    // re-pointed, the eye vertex evaluated towards it
+    PRay lc = P.light.get(lsid, idx - 1), ec = P.eye.get(sid, i);
+    const PRay pe = P.eye.get(sid, i - 1);
+    lc.d = normalize(ec.o - lc.o);
+    ec.d = -lc.d;
+    ec.dP = 1.f;
+    ec.delta = false;
+    ec.rad = bpt_eval_bsdf(S, pe.d, ec);
+    if (ec.contact != -1) ec.inside = dot(ec.cnorm, ec.d) > 0.f ? pe.inside : ec.contact;
+    C.lc = lc;
+    C.ec = ec;
+    C.mod = true;
+    const MisKind K = mis_kind(P, sid, true);
+    f3 col;
+    float prob;
+    bpt_color_prob(S, C, col, prob, true, K.radius);
+    if (length(col) == 0.f || prob == 0.f) return;
+    const float w = bpt_mis_weight(S, C, sid % P.npix, rev, K);
+    contrib = contrib + divs(col * w, prob);
+}
+
+// One thread per sample: every non-delta eye vertex (before an emitter) is a
+// query of the hash grid (HashGrid::Process, hashgrid.hxx:97-161); each query's
+// sum over its merges / nVM goes to the sample's pixel.
+__global__ void __launch_bounds__(128) k_vcm_merge(RenderScene S, BptParams P) {
+    const uint32_t sid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sid >= P.nsamp) return;
+    const int ne = (int)(__ldg(&P.counts[sid]) & 0xffu);
+    const uint32_t slot = sid / P.npix;
+    const GridView G = grid_view(P, slot);
+    const float rr = G.radius * G.radius;
+    const unsigned long long npts = P.ncand[2];
+    double rev[2 * BPT_MAX_RECORDS];
+    f3 own = mk(0, 0, 0);
+    for (int i = 1; i < ne; i++) {
+        const PRay q = P.eye.get(sid, i);
+        if (emissive(S, q.contact)) break;
+        if (q.delta) continue;
+        f3 contrib = mk(0, 0, 0);
+        const f3 dmin = q.o - G.bmin, dmax = G.bmax - q.o;
+        if (!(dmin.x < 0.f || dmin.y < 0.f || dmin.z < 0.f || dmax.x < 0.f || dmax.y < 0.f || dmax.z < 0.f)) {
+            const f3 cp = mk(G.inv_cell * dmin.x, G.inv_cell * dmin.y, G.inv_cell * dmin.z);
+            const f3 cf = mk(floorf(cp.x), floorf(cp.y), floorf(cp.z));
+            const int px = (int)cf.x, py = (int)cf.y, pz = (int)cf.z;
+            const f3 fr = cp - cf;
+            const int pxo = px + (fr.x < 0.5f ? -1 : 1), pyo = py + (fr.y < 0.5f ? -1 : 1),
+                      pzo = pz + (fr.z < 0.5f ? -1 : 1);
+            for (int j = 0; j < 8; j++) {
+                const int cx = (j & 4) ? pxo : px, cy = (j & 2) ? pyo : py, cz = (j & 1) ? pzo : pz;
+                // a list is at most every point of the batch long (bounded walk)
+                unsigned long long guard = 0;
+                for (int k = __ldg(&G.head[grid_bucket(G, cx, cy, cz)]); k >= 0 && guard++ < npts;
+                     k = __ldg(&P.next[k])) {
+                    const uint2 pt = P.pts[k];
+                    const f3 pos = xyz(__ldg(P.light.at(pt.x, (int)pt.y)));
+                    const float dist = length(q.o - pos);
+                    if (!(dist * dist <= rr)) continue;
+                    vcm_merge_one(S, P, sid, i, pt.x, (int)pt.y, rev, contrib);
+                }
+            }
+        }
+        own = own + divs(contrib, (float)P.npix);
+    }
+    if (own.x != 0.f || own.y != 0.f || own.z != 0.f)
+        film_add(P.film + 3 * (size_t)P.npix * slot, sid % P.npix, own);
 }
 
 // each sample's image: isLegalColor, fixVignetting, into the caller's film
@@ -595,10 +821,21 @@ __global__ void k_bpt_resolve(CamParams cam, float* __restrict__ film, uint32_t 
 // ---------------------------------------------------------------------------
 struct BptState {
     DeviceBuffer eye, light, counts, film, cand, vis;
+    DeviceBuffer pts, next, head, bbox, radii;  // vertex merging
+    std::vector<float> h_radii;
 };
 
+// VCMTracer's merge radius of iteration s (vcmTracer.cpp:27), alpha = 2/3,
+// computed on the host with the C library's powf and sqrtf
+float vcm_radius(float base, uint32_t s) {
+    const float alpha = (float)(2.0 / 3);
+    const float r = base * sqrtf(powf((float)(s + 1), alpha - 1.f));
+    return (double)r > EPS_D ? r : (float)EPS_D;
+}
+
 int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& RP, uint32_t spp_offset,
-                         uint32_t spp, float* d_sum, float* d_sumsq, unsigned int* err, cudaStream_t stream) {
+                         uint32_t spp, float* d_sum, float* d_sumsq, unsigned int* err, cudaStream_t stream,
+                         bool vcm, float base_radius) {
     if (RP.max_path_len + 2 > (uint32_t)BPT_MAX_RECORDS)
         return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "bidirectional mode: max_path_len is limited to 30");
     if (!ctx->bidir) ctx->bidir = std::make_shared<BptState>();
@@ -607,14 +844,14 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
     const uint32_t nrec = RP.max_path_len + 2;
     // a batch of whole samples-per-pixel: vertex records of both sub-paths
     // (64 B each), the counts and the batch's images in about 1 GiB
-    const size_t per_sample = 2ull * nrec * 64 + 4 + 12 + 16ull * nrec * (nrec + 1);
+    const size_t per_sample = 2ull * nrec * 64 + 4 + 12 + 16ull * nrec * (nrec + 1) + (vcm ? 12ull * nrec + 4 : 0);
     const uint64_t max_samples = std::max<uint64_t>(npix, (1ull << 30) / per_sample);
     const uint32_t per_batch = (uint32_t)std::min<uint64_t>(spp, std::max<uint64_t>(1, max_samples / npix));
     const uint64_t nsamp = (uint64_t)npix * per_batch;
     if (nsamp > 0xffffffffull) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "image too large");
     WR_CUDA(ctx, st.eye.reserve(64ull * nrec * nsamp));
     WR_CUDA(ctx, st.light.reserve(64ull * nrec * nsamp));
-    WR_CUDA(ctx, st.counts.reserve(4ull * nsamp + 24));
+    WR_CUDA(ctx, st.counts.reserve(4ull * nsamp + 32));
     WR_CUDA(ctx, st.cand.reserve(8ull * nrec * (nrec + 1) * nsamp));
     WR_CUDA(ctx, st.vis.reserve(8ull * nrec * (nrec + 1) * nsamp));
     const size_t film_bytes = 12ull * nsamp;
@@ -634,7 +871,20 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
     P.film = st.film.as<float>();
     P.cand = st.cand.as<uint2>();
     P.vis = st.vis.as<uint2>();
-    // the two list counters live after the per-sample counts (8-byte aligned)
+    P.vcm = vcm;
+    if (vcm) {
+        WR_CUDA(ctx, st.pts.reserve(8ull * nrec * nsamp));
+        WR_CUDA(ctx, st.next.reserve(4ull * nrec * nsamp));
+        WR_CUDA(ctx, st.head.reserve(4ull * nsamp));
+        WR_CUDA(ctx, st.bbox.reserve(24ull * per_batch));
+        WR_CUDA(ctx, st.radii.reserve(4ull * per_batch));
+        P.pts = st.pts.as<uint2>();
+        P.next = st.next.as<int>();
+        P.head = st.head.as<int>();
+        P.bbox = st.bbox.as<int>();
+        P.radii = st.radii.as<float>();
+    }
+    // the three list counters live after the per-sample counts (8-byte aligned)
     P.ncand = reinterpret_cast<unsigned long long*>(st.counts.as<char>() + ((4ull * nsamp + 7) & ~7ull));
     const int block = 128;
     const size_t smem = (size_t)RP.stack_cap * block * sizeof(uint32_t);
@@ -655,13 +905,30 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
         const int grid = (int)((P.nsamp + block - 1) / block);
         k_bpt_subpaths<<<dim3(grid, 2), block, smem, stream>>>(S, P, err);
         WR_CUDA(ctx, cudaGetLastError());
-        WR_CUDA(ctx, cudaMemsetAsync(P.ncand, 0, 2 * sizeof(unsigned long long), stream));
+        WR_CUDA(ctx, cudaMemsetAsync(P.ncand, 0, 3 * sizeof(unsigned long long), stream));
+        if (vcm) {  // the batch's hash grids: one per slot (iteration)
+            st.h_radii.resize(b);
+            for (uint32_t k = 0; k < b; k++) st.h_radii[k] = vcm_radius(base_radius, P.s0 + k);
+            WR_CUDA(ctx, cudaMemcpyAsync(st.radii.p, st.h_radii.data(), 4ull * b, cudaMemcpyHostToDevice, stream));
+            WR_CUDA(ctx, cudaMemsetAsync(P.bbox, 0, 24ull * b, stream));
+            WR_CUDA(ctx, cudaMemsetAsync(P.head, 0xff, 4ull * P.nsamp, stream));
+            k_vcm_points<<<grid, block, 0, stream>>>(S, P);
+            WR_CUDA(ctx, cudaGetLastError());
+            k_vcm_link<<<std::max(1, ctx->num_sms) * 8, 256, 0, stream>>>(P);
+            WR_CUDA(ctx, cudaGetLastError());
+            ctx->kernel_launches += 2;
+        }
         k_bpt_enum<<<grid, block, 0, stream>>>(S, P);
         WR_CUDA(ctx, cudaGetLastError());
         k_bpt_visible<<<visible_grid, block, smem, stream>>>(S, P, err);
         WR_CUDA(ctx, cudaGetLastError());
         k_bpt_connect<<<connect_grid, block, 0, stream>>>(S, P);
         WR_CUDA(ctx, cudaGetLastError());
+        if (vcm) {
+            k_vcm_merge<<<grid, block, 0, stream>>>(S, P);
+            WR_CUDA(ctx, cudaGetLastError());
+            ctx->kernel_launches += 1;
+        }
         k_bpt_resolve<<<(npix + 255) / 256, 256, 0, stream>>>(S.cam, P.film, npix, b, d_sum, d_sumsq);
         WR_CUDA(ctx, cudaGetLastError());
         ctx->kernel_launches += 5;

@@ -219,8 +219,11 @@ int wr_render_device(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, fl
     if (!ctx || !desc || !d_sum) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "null argument");
     SceneGPU* sc = find_scene(ctx, id);
     if (!sc) return set_error(ctx, WR_ERR_NOT_FOUND, "no such scene");
-    if (desc->mode != WR_MODE_MEGAKERNEL && desc->mode != WR_MODE_WAVEFRONT && desc->mode != WR_MODE_BIDIRECTIONAL)
+    if (desc->mode != WR_MODE_MEGAKERNEL && desc->mode != WR_MODE_WAVEFRONT && desc->mode != WR_MODE_BIDIRECTIONAL &&
+        desc->mode != WR_MODE_VCM)
         return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "unknown render mode");
+    if (desc->mode == WR_MODE_VCM && !(desc->radius >= 0.f && desc->radius < 1e30f))
+        return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "VCM merge radius must be finite and >= 0");
     if (desc->flags & ~RENDER_KNOWN_FLAGS) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "unknown render flags");
     if ((uint64_t)desc->spp_offset + desc->spp > 0xffffffffull)
         return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "sample index range overflows 32 bits");
@@ -239,13 +242,15 @@ int wr_render_device(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, fl
         P.flags = desc->flags;
         P.stack_cap = (int)sc->tree.max_depth + 3;
         const uint64_t npix = (uint64_t)rd->S.cam.width * rd->S.cam.height;
-        if (desc->mode == WR_MODE_BIDIRECTIONAL) {
+        if (desc->mode == WR_MODE_BIDIRECTIONAL || desc->mode == WR_MODE_VCM) {
             if (rd->has_media)
                 return set_error(ctx, WR_ERR_UNSUPPORTED,
-                                 "bidirectional mode: participating media are not supported");
+                                 "bidirectional / VCM mode: participating media are not supported");
             if (desc->flags & WR_RENDER_NEE)
-                return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "bidirectional mode has no NEE switch");
-            return render_bidirectional(ctx, rd->S, P, desc->spp_offset, desc->spp, d_sum, d_sumsq, err, s);
+                return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "bidirectional / VCM mode has no NEE switch");
+            const bool vcm = desc->mode == WR_MODE_VCM;
+            return render_bidirectional(ctx, rd->S, P, desc->spp_offset, desc->spp, d_sum, d_sumsq, err, s, vcm,
+                                        desc->radius > 0.f ? desc->radius : 0.01f);
         }
         if (desc->mode == WR_MODE_WAVEFRONT) {
             rc = render_wavefront(ctx, *rd, P, desc->spp_offset, desc->spp, d_sum, d_sumsq, s);

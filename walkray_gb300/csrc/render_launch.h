@@ -29,9 +29,12 @@ struct RenderParams {
 cudaError_t launch_megakernel(const RenderScene& S, const RenderParams& P, float* film, float* film2,
                               unsigned int* err, cudaStream_t stream);
 
-// WR_MODE_BIDIRECTIONAL (bpt.cu): adds samples [spp_offset, spp_offset + spp)
-// of every pixel to d_sum (and their squares to d_sumsq, may be NULL)
+// WR_MODE_BIDIRECTIONAL and WR_MODE_VCM (bpt.cu): adds samples
+// [spp_offset, spp_offset + spp) of every pixel to d_sum (and their squares
+// to d_sumsq, may be NULL); `vcm` adds vertex merging with base radius
+// `base_radius`
 int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& P, uint32_t spp_offset, uint32_t spp,
-                         float* d_sum, float* d_sumsq, unsigned int* err, cudaStream_t stream);
+                         float* d_sum, float* d_sumsq, unsigned int* err, cudaStream_t stream, bool vcm = false,
+                         float base_radius = 0.01f);
 
 }  // namespace wr
