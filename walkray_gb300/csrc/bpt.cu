@@ -103,7 +103,7 @@ struct BptParams {
     float* film;          // per sample slot of the batch: npix * 3 floats
     uint2* cand;          // connection candidates with a light sub-path (l >= 1): {sample, l | e << 8}
     uint2* vis;           // connections that contribute: visible candidates and whole eye paths
-    unsigned long long* ncand;  // [0]: entries of cand, [1]: entries of vis, [2]: light points
+    unsigned long long* ncand;  // [0]: entries of cand, [1]: entries of vis, [2]: light points, [3]: merges
     // vertex merging (WR_MODE_VCM); per sample slot s of the batch, the hash grid of hashgrid.hxx
     bool vcm;
     const float* radii;   // merge radius of each slot's iteration
@@ -111,6 +111,8 @@ struct BptParams {
     int* bbox;            // per slot: ordered-int keys of min x, y, z, max x, y, z
     int* head;            // per slot: npix buckets, first point or -1
     int* next;            // per point: next point of its bucket or -1
+    uint4* merges;        // merges found by the grid queries: {sample, eye record, point}
+    unsigned long long merge_cap;
 };
 
 // the weight's technique set for a sample of this batch
@@ -744,8 +746,11 @@ __device__ void vcm_merge_one(const RenderScene& S, const BptParams& P, uint32_t
 }
 
 // One thread per sample: every non-delta eye vertex (before an emitter) is a
-// query of the hash grid (HashGrid::Process, hashgrid.hxx:97-161); each query's
-// sum over its merges / nVM goes to the sample's pixel.
+// query of the hash grid (HashGrid::Process, hashgrid.hxx:97-161).  Each light
+// point within the radius is a merge, appended to the merge list for
+// k_vcm_eval; when the list is full the merge is evaluated here.  Each
+// merge's contribution / nVM goes to the sample's pixel (the reference adds a
+// query's sum / nVM: the same up to the order of the additions).
 __global__ void __launch_bounds__(128) k_vcm_merge(RenderScene S, BptParams P) {
     const uint32_t sid = blockIdx.x * blockDim.x + threadIdx.x;
     if (sid >= P.nsamp) return;
@@ -779,7 +784,9 @@ __global__ void __launch_bounds__(128) k_vcm_merge(RenderScene S, BptParams P) {
                     const f3 pos = xyz(__ldg(P.light.at(pt.x, (int)pt.y)));
                     const float dist = length(q.o - pos);
                     if (!(dist * dist <= rr)) continue;
-                    vcm_merge_one(S, P, sid, i, pt.x, (int)pt.y, rev, contrib);
+                    const unsigned long long m = atomicAdd(P.ncand + 3, 1ull);
+                    if (m < P.merge_cap) P.merges[m] = make_uint4(sid, (uint32_t)i, (uint32_t)k, 0u);
+                    else vcm_merge_one(S, P, sid, i, pt.x, (int)pt.y, rev, contrib);
                 }
             }
         }
@@ -787,6 +794,21 @@ __global__ void __launch_bounds__(128) k_vcm_merge(RenderScene S, BptParams P) {
     }
     if (own.x != 0.f || own.y != 0.f || own.z != 0.f)
         film_add(P.film + 3 * (size_t)P.npix * slot, sid % P.npix, own);
+}
+
+// the listed merges, one per thread and step (persistent)
+__global__ void __launch_bounds__(128) k_vcm_eval(RenderScene S, BptParams P) {
+    const unsigned long long n = P.ncand[3], total = n < P.merge_cap ? n : P.merge_cap;
+    double rev[2 * BPT_MAX_RECORDS];
+    for (unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint4 m = P.merges[t];
+        const uint2 pt = P.pts[m.z];
+        f3 contrib = mk(0, 0, 0);
+        vcm_merge_one(S, P, m.x, (int)m.y, pt.x, (int)pt.y, rev, contrib);
+        if (contrib.x != 0.f || contrib.y != 0.f || contrib.z != 0.f)
+            film_add(P.film + 3 * (size_t)P.npix * (m.x / P.npix), m.x % P.npix, divs(contrib, (float)P.npix));
+    }
 }
 
 // each sample's image: isLegalColor, fixVignetting, into the caller's film
@@ -821,7 +843,7 @@ __global__ void k_bpt_resolve(CamParams cam, float* __restrict__ film, uint32_t 
 // ---------------------------------------------------------------------------
 struct BptState {
     DeviceBuffer eye, light, counts, film, cand, vis;
-    DeviceBuffer pts, next, head, bbox, radii;  // vertex merging
+    DeviceBuffer pts, next, head, bbox, radii, merges;  // vertex merging
     std::vector<float> h_radii;
 };
 
@@ -844,14 +866,14 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
     const uint32_t nrec = RP.max_path_len + 2;
     // a batch of whole samples-per-pixel: vertex records of both sub-paths
     // (64 B each), the counts and the batch's images in about 1 GiB
-    const size_t per_sample = 2ull * nrec * 64 + 4 + 12 + 16ull * nrec * (nrec + 1) + (vcm ? 12ull * nrec + 4 : 0);
+    const size_t per_sample = 2ull * nrec * 64 + 4 + 12 + 16ull * nrec * (nrec + 1) + (vcm ? 12ull * nrec + 4 + 128 : 0);
     const uint64_t max_samples = std::max<uint64_t>(npix, (1ull << 30) / per_sample);
     const uint32_t per_batch = (uint32_t)std::min<uint64_t>(spp, std::max<uint64_t>(1, max_samples / npix));
     const uint64_t nsamp = (uint64_t)npix * per_batch;
     if (nsamp > 0xffffffffull) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "image too large");
     WR_CUDA(ctx, st.eye.reserve(64ull * nrec * nsamp));
     WR_CUDA(ctx, st.light.reserve(64ull * nrec * nsamp));
-    WR_CUDA(ctx, st.counts.reserve(4ull * nsamp + 32));
+    WR_CUDA(ctx, st.counts.reserve(4ull * nsamp + 40));
     WR_CUDA(ctx, st.cand.reserve(8ull * nrec * (nrec + 1) * nsamp));
     WR_CUDA(ctx, st.vis.reserve(8ull * nrec * (nrec + 1) * nsamp));
     const size_t film_bytes = 12ull * nsamp;
@@ -883,6 +905,10 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
         P.head = st.head.as<int>();
         P.bbox = st.bbox.as<int>();
         P.radii = st.radii.as<float>();
+        // the merge list: 8 merges per sample of the batch (more are evaluated where found)
+        P.merge_cap = 8ull * nsamp;
+        WR_CUDA(ctx, st.merges.reserve(16ull * P.merge_cap));
+        P.merges = st.merges.as<uint4>();
     }
     // the three list counters live after the per-sample counts (8-byte aligned)
     P.ncand = reinterpret_cast<unsigned long long*>(st.counts.as<char>() + ((4ull * nsamp + 7) & ~7ull));
@@ -905,7 +931,7 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
         const int grid = (int)((P.nsamp + block - 1) / block);
         k_bpt_subpaths<<<dim3(grid, 2), block, smem, stream>>>(S, P, err);
         WR_CUDA(ctx, cudaGetLastError());
-        WR_CUDA(ctx, cudaMemsetAsync(P.ncand, 0, 3 * sizeof(unsigned long long), stream));
+        WR_CUDA(ctx, cudaMemsetAsync(P.ncand, 0, 4 * sizeof(unsigned long long), stream));
         if (vcm) {  // the batch's hash grids: one per slot (iteration)
             st.h_radii.resize(b);
             for (uint32_t k = 0; k < b; k++) st.h_radii[k] = vcm_radius(base_radius, P.s0 + k);
@@ -927,7 +953,9 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
         if (vcm) {
             k_vcm_merge<<<grid, block, 0, stream>>>(S, P);
             WR_CUDA(ctx, cudaGetLastError());
-            ctx->kernel_launches += 1;
+            k_vcm_eval<<<connect_grid, block, 0, stream>>>(S, P);
+            WR_CUDA(ctx, cudaGetLastError());
+            ctx->kernel_launches += 2;
         }
         k_bpt_resolve<<<(npix + 255) / 256, 256, 0, stream>>>(S.cam, P.film, npix, b, d_sum, d_sumsq);
         WR_CUDA(ctx, cudaGetLastError());
