@@ -209,6 +209,7 @@ std::vector<vec3f> GpuPathTracer::renderPixels() {
     d.max_path_len = maxPathLen;
     d.seed = seed;
     d.mode = mode;
+    d.radius = mergeRadius;
     d.flags = useNextEventEstimation ? WR_RENDER_NEE : 0u;
     static_assert(sizeof(vec3f) == 3 * sizeof(float), "vec3f must be three packed floats");
     if (wr_render(ctx, sceneId, &d, &img[0].x) != WR_OK) {

@@ -44,6 +44,8 @@ public:
 
     void setNextEventEstimation(bool on) { useNextEventEstimation = on; }
     void setSeed(uint64_t s) { seed = s; }
+    // WR_MODE_VCM: VCMTracer::setRadius (vcmTracer.h:40); 0 = the reference's default 0.01
+    void setMergeRadius(float r) { mergeRadius = r; }
     const char* lastError() const { return ctx ? wr_last_error(ctx) : "no GPU context"; }
 
 private:
@@ -55,6 +57,7 @@ private:
     bool useNextEventEstimation = false;
     uint32_t mode;
     uint64_t seed = 1;
+    float mergeRadius = 0.f;
     Describe describe;
 };
 
