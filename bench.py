@@ -16,9 +16,10 @@ Prints ONE JSON line (rank 0).  Workloads:
   bpt bidirectional path tracing (WR_MODE_BIDIRECTIONAL) of the Cornell box,
       256x256, max path length 8; one step = one render call of 16 samples
       per pixel (1,048,576 eye + light sub-path pairs, all connections).
-      Metric: Msamples/s (the unidirectional megakernel and vertex
-      connection and merging, WR_MODE_VCM with base radius 0.01, on the same
-      scene beside it).
+      Metric: Msamples/s (the unidirectional megakernel, vertex connection
+      and merging, WR_MODE_VCM, and progressive photon mapping,
+      WR_MODE_PHOTON_MAP, both with base radius 0.01, on the same scene
+      beside it).
 
 `value` is device-timed with CUDA events per step on the launching stream,
 with the L2 flushed (a 512 MiB write) before every step and inputs resident
@@ -392,6 +393,7 @@ def run_bpt(args, world, rank, local):
             step_mode("bidirectional")(i)
             step_mode("megakernel")(i)
             step_mode("vcm")(i)
+            step_mode("photon_map")(i)
     torch.cuda.synchronize()
     barrier(world)
     with ClockSampler(local) as clk:
@@ -400,6 +402,7 @@ def run_bpt(args, world, rank, local):
         n_launch = launches(ctx) - l0
         ms_pt = timed_steps(step_mode("megakernel"), args.steps, stream, flush)
         ms_vcm = timed_steps(step_mode("vcm"), args.steps, stream, flush)
+        ms_ppm = timed_steps(step_mode("photon_map"), args.steps, stream, flush)
     ms_max = allreduce(world, ms, "max")
     samples = float(npix * BPT_SPP * args.steps)
     value = allreduce(world, samples, "sum") / (ms_max / 1e3) / 1e6
@@ -424,6 +427,9 @@ def run_bpt(args, world, rank, local):
                                       "ms_per_step": round(ms_pt / args.steps, 3)},
         "vcm": {"value": round(allreduce(world, samples, "sum") / (allreduce(world, ms_vcm, "max") / 1e3) / 1e6, 3),
                 "unit": "Msamples/s", "ms_per_step": round(ms_vcm / args.steps, 3), "base_radius": 0.01},
+        "photon_map": {"value": round(allreduce(world, samples, "sum") / (allreduce(world, ms_ppm, "max") / 1e3) / 1e6,
+                                      3),
+                       "unit": "Msamples/s", "ms_per_step": round(ms_ppm / args.steps, 3), "base_radius": 0.01},
         "samples_per_step": npix * BPT_SPP, "gpu_launches": int(n_launch), "clocks": clk.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -436,6 +442,11 @@ def run_bpt(args, world, rank, local):
         line["vcm"]["cpu_baseline"] = {"value": round(npix / (time.perf_counter() - t0) / 1e6, 4), "unit": "Msamples/s",
                                        "cores": os.cpu_count() or 1, "kind": "port",
                                        "sample": "1 spp, VCMTracer restated in C (oracle)"}
+        t0 = time.perf_counter()
+        orc.render_ppm(1, BPT_DEPTH, seed=1, radius=0.01, threads=os.cpu_count() or 1)
+        line["photon_map"]["cpu_baseline"] = {"value": round(npix / (time.perf_counter() - t0) / 1e6, 4),
+                                              "unit": "Msamples/s", "cores": os.cpu_count() or 1, "kind": "port",
+                                              "sample": "1 spp, PhotonMap restated in C (oracle)"}
     ctx.close()
     return line
 

@@ -201,6 +201,12 @@ int wr_trace_closest_device(wr_ctx* ctx, wr_scene_id scene, const float* d_rays,
                                     points within the iteration's radius (the reference's hash grid);
                                     wr_render_desc.radius is the base radius (VCMTracer::setRadius;
                                     0 = the reference's default 0.01); surfaces only, max_path_len <= 30 */
+#define WR_MODE_PHOTON_MAP 4u    /* PhotonMap (photonMap.cpp:20-625) as the reference builds it (progressive:
+                                    radius r_s of VCM's schedule, no ray marching): light sub-paths as
+                                    photons in the reference's hash grid, each eye path's first diffuse
+                                    record estimates the photon density (kernel 3(1-d^2/r^2)^2/pi);
+                                    wr_render_desc.radius is the base radius (PhotonMap::setRadius; 0 =
+                                    0.01); surfaces without anisotropic glossy objects, max_path_len <= 30 */
 
 #define WR_RENDER_NEE 1u      /* PathTracer's next-event-estimation branch (pathTracer.cpp:39-66) */
 /* Rendering traverses front to back and skips a box whose entry distance is
@@ -218,7 +224,7 @@ typedef struct wr_render_desc {
     uint32_t mode;         /* WR_MODE_* */
     uint32_t flags;        /* WR_RENDER_* */
     uint32_t spp_offset;   /* index of the first sample (progressive rendering / resume) */
-    float radius;          /* WR_MODE_VCM: base merge radius (0 = 0.01); ignored otherwise */
+    float radius;          /* WR_MODE_VCM / WR_MODE_PHOTON_MAP: base radius (0 = 0.01); ignored otherwise */
 } wr_render_desc;
 
 /* PathTracer::renderPixels (pathTracer.cpp:7-76) on the GPU: rgb_out gets

@@ -15,12 +15,13 @@
  *   dumptree scene.wrs out.bin
  *            the reference tree in depth-first pre-order:
  *            per node {u32 is_leaf, f32 min[3], f32 max[3], u32 ntri, u32 tris[ntri]}
- *   render   scene.wrs spp maxlen seed out.bin [nee|bpt|vcm radius]
+ *   render   scene.wrs spp maxlen seed out.bin [nee|bpt|vcm radius|ppm radius]
  *            PathTracer::renderPixels (pathTracer.cpp:7-76) as it is: the
  *            per-spp tree rebuild and PFM write included; with `bpt`
  *            BidirectionalPathTracer::renderPixels (bidirPathTracer.cpp:10-56);
  *            with `vcm radius` VCMTracer::renderPixels (vcmTracer.cpp:6-92)
- *            with VCMTracer::setRadius(radius).  out: W*H*3 f32
+ *            with VCMTracer::setRadius(radius); with `ppm radius`
+ *            PhotonMap::renderPixels (photonMap.cpp:20-148), setRadius(radius).  out: W*H*3 f32
  *            (row 0 = top, p = y*W + x).  Elapsed seconds on stderr.
  */
 #include "wr_ref_prelude.h"
@@ -52,6 +53,7 @@
 #undef class
 #include "bidirPathTracer.h"
 #include "vcmTracer.h"
+#include "photonMap.h"
 
 extern "C" {
 #include "wrs_io.h"
@@ -250,6 +252,7 @@ static int cmd_render(int argc, char** argv) {
     bool nee = argc > 7 && strcmp(argv[7], "nee") == 0;
     bool bpt = argc > 7 && strcmp(argv[7], "bpt") == 0;
     bool vcm = argc > 8 && strcmp(argv[7], "vcm") == 0;
+    bool ppm = argc > 8 && strcmp(argv[7], "ppm") == 0;
     RenderEngine* eng = new RenderEngine();
     delete eng->rng;
     eng->rng = new Rng(seed);
@@ -262,6 +265,10 @@ static int cmd_render(int argc, char** argv) {
     MCRenderer* pt;
     if (bpt) {
         pt = new BidirectionalPathTracer(eng, spp, maxlen);
+    } else if (ppm) {
+        PhotonMap* m = new PhotonMap(eng, spp, maxlen);
+        m->setRadius((float)atof(argv[8]));
+        pt = m;
     } else if (vcm) {
         VCMTracer* v = new VCMTracer(eng, spp, maxlen);
         v->setRadius((float)atof(argv[8]));

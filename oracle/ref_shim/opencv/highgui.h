@@ -5,4 +5,5 @@
 static inline void cvNamedWindow(const char*) {}
 static inline void cvShowImage(const char*, const IplImage*) {}
 static inline int cvWaitKey(int) { return -1; }
+static inline int cvSaveImage(const char*, const IplImage*) { return 0; }
 static inline void cvDestroyWindow(const char*) {}

@@ -460,3 +460,4 @@ float wro_draw(uint64_t seed, uint32_t pixel, uint32_t sample, uint32_t dim) {
 #include "wr_oracle_pt.inc"
 #include "wr_oracle_bpt.inc"
 #include "wr_oracle_vcm.inc"
+#include "wr_oracle_ppm.inc"

@@ -53,6 +53,8 @@ def load():
         lib.wro_render_vcm.restype = C.c_int
         lib.wro_render_vcm.argtypes = [C.c_void_p, C.c_uint32, C.c_uint64, C.c_float, C.c_uint32, C.c_uint32,
                                        C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_uint64)]
+        lib.wro_render_ppm.restype = C.c_int
+        lib.wro_render_ppm.argtypes = lib.wro_render_vcm.argtypes
         lib.wro_vcm_radius.restype = C.c_float
         lib.wro_vcm_radius.argtypes = [C.c_float, C.c_uint32]
         _lib = lib
@@ -169,4 +171,19 @@ class SceneOracle:
                                      C.byref(rays))
         if rc:
             raise ValueError("the VCM restatement does not cover participating media")
+        return s, s2, rays.value
+
+    def render_ppm(self, spp: int, max_path_len: int, seed: int, radius: float = 0.01, s0: int = 0,
+                   threads: int = 0, want_sumsq: bool = False):
+        """The restated PhotonMap (progressive photon mapping) with base radius
+        `radius`: per-pixel sums over samples [s0, s0 + spp), like render()."""
+        c = self.scene.camera
+        npx = c.width * c.height
+        s = np.zeros((npx, 3), np.float64)
+        s2 = np.zeros((npx, 3), np.float64) if want_sumsq else None
+        rays = C.c_uint64()
+        rc = self.lib.wro_render_ppm(self.h, max_path_len, seed, radius, s0, s0 + spp, _p(s), _p(s2), threads,
+                                     C.byref(rays))
+        if rc:
+            raise ValueError("the photon-mapping restatement covers surfaces without anisotropic objects only")
         return s, s2, rays.value

@@ -28,9 +28,13 @@ from the reference sources) on small seeded scenes and stores its answers:
                       Cornell, mirror and thin-lens scenes, 8 reference
                       renders of 64 spp each
 
-Usage: python tests/golden/make_golden.py [bpt|vcm]   (needs the reference
-tree on this machine; `bpt` / `vcm` remake only those renders; the fixtures
-it writes are what the tests read elsewhere)
+  render_ppm_*.npz    PhotonMap::renderPixels (base radius 0.02) on the
+                      Cornell, mirror, thin-lens and mixed-material scenes, 8
+                      reference renders of 64 spp each
+
+Usage: python tests/golden/make_golden.py [bpt|vcm|ppm]   (needs the
+reference tree on this machine; `bpt` / `vcm` / `ppm` remake only those
+renders; the fixtures it writes are what the tests read elsewhere)
 """
 from __future__ import annotations
 
@@ -240,12 +244,26 @@ def vcm_fixtures(td):
         render_set(sc[name], p, td, f"render_vcm_{name}.npz", extra=("vcm", str(VCM_RADIUS)), spp=64)
 
 
+PPM_SCENES = ("cornell", "mirror", "dof", "mixed_l2")
+PPM_RADIUS = 0.02
+
+
+def ppm_fixtures(td):
+    """PhotonMap::renderPixels (photonMap.cpp:20-148), base radius 0.02, 8
+    reference renders of 64 spp per scene, depth 8."""
+    sc = golden_scenes()
+    p = os.path.join(td, "s.wrs")
+    for name in PPM_SCENES:
+        render_set(sc[name], p, td, f"render_ppm_{name}.npz", extra=("ppm", str(PPM_RADIUS)), spp=64)
+
+
 def main():
     if not os.path.exists(REF):
         sys.exit("build the reference harness first: make -C oracle ref")
-    if sys.argv[1:] in (["bpt"], ["vcm"]):  # only the bidirectional / VCM renders
+    only = {"bpt": bpt_fixtures, "vcm": vcm_fixtures, "ppm": ppm_fixtures}
+    if len(sys.argv) == 2 and sys.argv[1] in only:  # only those renders
         with tempfile.TemporaryDirectory() as td:
-            (bpt_fixtures if sys.argv[1] == "bpt" else vcm_fixtures)(td)
+            only[sys.argv[1]](td)
         return
     sc = golden_scenes()
     with tempfile.TemporaryDirectory() as td:
@@ -305,6 +323,7 @@ def main():
         mesh_fixtures(td)
         bpt_fixtures(td)
         vcm_fixtures(td)
+        ppm_fixtures(td)
     print("golden fixtures written to", HERE)
 
 

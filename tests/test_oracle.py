@@ -203,3 +203,27 @@ def test_oracle_vcm_radius_schedule(built):
         want = np.float32(0.02) * np.sqrt(np.float32(s + 1) ** (np.float32(2.0 / 3) - np.float32(1)))
         assert abs(lib.wro_vcm_radius(0.02, s) / want - 1) < 1e-6
     assert lib.wro_vcm_radius(1e-9, 5) == np.float32(1e-5)
+
+
+@pytest.mark.parametrize("name", ["cornell", "mirror", "dof", "mixed_l2"])
+def test_oracle_photon_map_matches_reference_statistically(built, name):
+    """PhotonMap (photonMap.cpp:20-625, progressive, base radius 0.02): the
+    restated photon density estimation vs 8 reference renders of 64 spp."""
+    g = np.load(os.path.join(GOLDEN, f"render_ppm_{name}.npz"))
+    ref = g["images"].astype(np.float64)
+    s = make_golden.golden_scenes()[name]
+    h, w = s.camera.height, s.camera.width
+    orc = wr_oracle.SceneOracle(s)
+    port = np.stack([(orc.render_ppm(64, 8, seed=700 + k, radius=make_golden.PPM_RADIUS)[0] / 64).reshape(h, w, 3)
+                     for k in range(8)])
+    blk = lambda a: a.reshape(a.shape[0], h // 4, 4, w // 4, 4, 3).mean((2, 4))
+    br, bp = blk(ref), blk(port)
+    z = (br.mean(0) - bp.mean(0)) / np.sqrt(br.var(0, ddof=1) / 8 + bp.var(0, ddof=1) / 8 + 1e-12)
+    assert np.abs(z).max() < 5.0, np.abs(z).max()
+    assert abs(port.mean() / ref.mean() - 1) < 0.02
+
+
+def test_oracle_photon_map_refuses_media_and_anisotropic(built):
+    for name in ("media_small",):
+        with pytest.raises(ValueError):
+            wr_oracle.SceneOracle(make_golden.golden_scenes()[name]).render_ppm(1, 8, seed=1)

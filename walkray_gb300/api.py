@@ -128,7 +128,7 @@ class Context:
     def render(self, sid: int, spp: int, max_path_len: int, seed: int = 1, mode: str = "megakernel",
                nee: bool = False, spp_offset: int = 0, exact: bool = False, radius: float = 0.0) -> np.ndarray:
         """Mean image (H, W, 3) float32, row 0 at the top (wr_render); `radius`
-        is the base merge radius of mode "vcm" (0 = 0.01)."""
+        is the base radius of modes "vcm" and "photon_map" (0 = 0.01)."""
         w, h = self._camera_size(sid)
         out = np.empty((h, w, 3), np.float32)
         d = L.wr_render_desc(spp, max_path_len, seed, MODES[mode], _flags(nee, exact), spp_offset, radius)
@@ -188,7 +188,7 @@ class Context:
         return cam
 
 
-MODES = {"megakernel": 0, "wavefront": 1, "bidirectional": 2, "vcm": 3}
+MODES = {"megakernel": 0, "wavefront": 1, "bidirectional": 2, "vcm": 3, "photon_map": 4}
 
 
 def _flags(nee: bool, exact: bool) -> int:

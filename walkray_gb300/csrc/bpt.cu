@@ -113,6 +113,10 @@ struct BptParams {
     int* next;            // per point: next point of its bucket or -1
     uint4* merges;        // merges found by the grid queries: {sample, eye record, point}
     unsigned long long merge_cap;
+    // progressive photon mapping (WR_MODE_PHOTON_MAP): light sub-paths only,
+    // each photon's throughput
+    bool light_only;
+    float4* tput;
 };
 
 // the weight's technique set for a sample of this batch
@@ -189,7 +193,7 @@ __global__ void __launch_bounds__(128) k_bpt_subpaths(RenderScene S, BptParams P
     const uint32_t sid = blockIdx.x * blockDim.x + threadIdx.x;
     if (sid >= P.nsamp) return;
     const uint32_t pixel = sid % P.npix, sample = P.s0 + sid / P.npix;
-    if (blockIdx.y == 0) {
+    if (blockIdx.y == 0 && !P.light_only) {
         // eye sub-path: the camera ray is traced without a condition (camera.cpp:52)
         PathRng g;
         g.init(P.seed, pixel, sample, 0);
@@ -811,6 +815,131 @@ __global__ void __launch_bounds__(128) k_vcm_eval(RenderScene S, BptParams P) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// progressive photon mapping (PhotonMap::renderPixels, photonMap.cpp:20-148,
+// as built: PPM on, no ray marching, no anisotropic ellipse kernel): the
+// light points of VCM are the photons, in the same hash grid
+// ---------------------------------------------------------------------------
+constexpr uint32_t PPM_MERGE_LEN = 10;  // photonMap.cpp:9
+
+// each photon's throughput up to its record (photonMap.cpp:228-236)
+__global__ void __launch_bounds__(256) k_ppm_tput(RenderScene S, BptParams P) {
+    const unsigned long long total = P.ncand[2];
+    for (unsigned long long k = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; k < total;
+         k += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint2 pt = P.pts[k];
+        f3 t = mk(1, 1, 1);
+        PRay cur = P.light.get(pt.x, 0);
+        for (int i = 0; i < (int)pt.y; i++) {
+            const PRay nx = P.light.get(pt.x, i + 1);
+            t = vmul(t, divs(divs(cur.rad, cur.dP), cur.oP));
+            t = t * cos_term(S, cur);
+            t = vmul(t, radiance_decay(S, cur, length(cur.o - nx.o)));
+            cur = nx;
+        }
+        t = divs(t, cur.oP);
+        P.tput[k] = make_float4(t.x, t.y, t.z, 0.f);
+    }
+}
+
+// Query::Process (photonMap.cpp:219-246): one photon's density estimate at
+// the eye record `out` (direction towards the camera side)
+__device__ __forceinline__ f3 ppm_photon(const RenderScene& S, const BptParams& P, uint32_t k, const PRay& out,
+                                         float radius) {
+    const uint2 pt = P.pts[k];
+    const float4 tp = __ldg(&P.tput[k]);
+    const PRay prevl = P.light.get(pt.x, (int)pt.y - 1);
+    const f3 pos = xyz(__ldg(P.light.at(pt.x, (int)pt.y)));
+    const f3 color = vmul(mk(tp.x, tp.y, tp.z), eval_bsdf(S, prevl.d, out));
+    const float dist_sqr = powf(length(out.o - pos), 2.f);
+    if (!legal(color)) return mk(0, 0, 0);
+    const float x = 1.f - dist_sqr / (radius * radius);
+    const float sk = 0.f > x ? 0.f : x;
+    const float kernel = (float)((double)(3.f * sk * sk) / PI_D);
+    return color * (kernel / ((float)P.npix * radius * radius));
+}
+
+// One thread per sample: the eye path of PhotonMap::sampleMergePath (at most
+// 10 bounces) up to its first emitter (its radiance) or diffuse record (the
+// photon density there, throughputByDensityEstimation), times the camera
+// record's factors, into the sample's image.  Records after that one are
+// never read, so the path is not continued.
+__global__ void __launch_bounds__(128) k_ppm_eye(RenderScene S, BptParams P, unsigned int* __restrict__ err) {
+    extern __shared__ uint32_t s_stack[];
+    uint32_t* stack = s_stack + threadIdx.x;
+    const int stride = blockDim.x;
+    const uint32_t sid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sid >= P.nsamp) return;
+    const uint32_t pixel = sid % P.npix, slot = sid / P.npix, sample = P.s0 + slot;
+    PathRng g;
+    g.init(P.seed, pixel, sample, 0);
+    const PRay cam = camera_ray(S.cam, pixel, g);
+    PRay prev = cam;
+    {
+        RayQ q = make_rayq(cam.o, cam.d, S.tree.scene_mag);
+        q.pf = P.pf;
+        const Hit h = trace_closest<false, true>(S.tree, q, -1, -1, stack, stride, P.stack_cap, err);
+        set_hit(S, prev, h);
+    }
+    InsideStack st;
+    st.reset(prev.inside);
+    f3 surf = mk(0, 0, 0);
+    const GridView G = grid_view(P, slot);
+    const unsigned long long npts = P.ncand[2];
+    for (uint32_t depth = 0;; depth++) {
+        const int self = prev.inside >= 0 ? prev.inside : prev.iobj;
+        if (self < 0) break;  // the terminate record: nothing to estimate
+        const PRay next = scatter(S, self, prev, g, st);
+        const bool ended = length(next.d) < 0.5f;
+        if (!ended && depth + 1 > PPM_MERGE_LEN) break;  // cut: `next` is not a record
+        if (emissive(S, next.contact)) {
+            surf = next.rad;
+            break;
+        }
+        if (next.contact >= 0 && obj_type(S, next.contact) == WR_MAT_DIFFUSE) {  // nonSpecular()
+            PRay out = next;
+            out.d = -prev.d;
+            const f3 q = next.o, dmin = q - G.bmin, dmax = G.bmax - q;
+            if (!(dmin.x < 0.f || dmin.y < 0.f || dmin.z < 0.f || dmax.x < 0.f || dmax.y < 0.f || dmax.z < 0.f)) {
+                const f3 cp = mk(G.inv_cell * dmin.x, G.inv_cell * dmin.y, G.inv_cell * dmin.z);
+                const f3 cf = mk(floorf(cp.x), floorf(cp.y), floorf(cp.z));
+                const int px = (int)cf.x, py = (int)cf.y, pz = (int)cf.z;
+                const f3 fr = cp - cf;
+                const int pxo = px + (fr.x < 0.5f ? -1 : 1), pyo = py + (fr.y < 0.5f ? -1 : 1),
+                          pzo = pz + (fr.z < 0.5f ? -1 : 1);
+                const float rr = G.radius * G.radius;
+                for (int j = 0; j < 8; j++) {
+                    const int cx = (j & 4) ? pxo : px, cy = (j & 2) ? pyo : py, cz = (j & 1) ? pzo : pz;
+                    unsigned long long guard = 0;
+                    for (int k = __ldg(&G.head[grid_bucket(G, cx, cy, cz)]); k >= 0 && guard++ < npts;
+                         k = __ldg(&P.next[k])) {
+                        const uint2 pt = P.pts[k];
+                        const float dist = length(q - xyz(__ldg(P.light.at(pt.x, (int)pt.y))));
+                        if (!(dist * dist <= rr)) continue;
+                        surf = surf + ppm_photon(S, P, (uint32_t)k, out, G.radius);
+                    }
+                }
+            }
+            break;
+        }
+        if (ended) break;
+        st.set_top(next.inside);
+        RayQ q = make_rayq(next.o, next.d, S.tree.scene_mag);
+        q.pf = P.pf;
+        const Hit h = trace_closest<true, true>(S.tree, q, next.inside, next.contact, stack, stride, P.stack_cap, err);
+        if (h.slot < 0) break;  // `next` was the last record and is checked above
+        prev = next;
+        set_hit(S, prev, h);
+    }
+    // color = Tr * SurfaceColor + VolumeColor, times eyeMergePath[0]'s factors (photonMap.cpp:614-623)
+    const f3 f = divs(divs(cam.rad * cos_term(S, cam), cam.dP), cam.oP);
+    const f3 c = vmul(surf, f);
+    float* fl = P.film + 3 * ((size_t)slot * P.npix + pixel);
+    fl[0] += c.x;
+    fl[1] += c.y;
+    fl[2] += c.z;
+}
+
 // each sample's image: isLegalColor, fixVignetting, into the caller's film
 __global__ void k_bpt_resolve(CamParams cam, float* __restrict__ film, uint32_t npix, uint32_t slots,
                               float* __restrict__ sum, float* __restrict__ sumsq) {
@@ -844,6 +973,7 @@ __global__ void k_bpt_resolve(CamParams cam, float* __restrict__ film, uint32_t 
 struct BptState {
     DeviceBuffer eye, light, counts, film, cand, vis;
     DeviceBuffer pts, next, head, bbox, radii, merges;  // vertex merging
+    DeviceBuffer tput;                                  // photon mapping
     std::vector<float> h_radii;
 };
 
@@ -857,25 +987,29 @@ float vcm_radius(float base, uint32_t s) {
 
 int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& RP, uint32_t spp_offset,
                          uint32_t spp, float* d_sum, float* d_sumsq, unsigned int* err, cudaStream_t stream,
-                         bool vcm, float base_radius) {
+                         int kind, float base_radius) {
     if (RP.max_path_len + 2 > (uint32_t)BPT_MAX_RECORDS)
         return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "bidirectional mode: max_path_len is limited to 30");
+    const bool vcm = kind == BIDIR_VCM, ppm = kind == BIDIR_PHOTON_MAP, grid_on = vcm || ppm;
     if (!ctx->bidir) ctx->bidir = std::make_shared<BptState>();
     BptState& st = *static_cast<BptState*>(ctx->bidir.get());
     const uint32_t npix = S.cam.width * S.cam.height;
     const uint32_t nrec = RP.max_path_len + 2;
     // a batch of whole samples-per-pixel: vertex records of both sub-paths
-    // (64 B each), the counts and the batch's images in about 1 GiB
-    const size_t per_sample = 2ull * nrec * 64 + 4 + 12 + 16ull * nrec * (nrec + 1) + (vcm ? 12ull * nrec + 4 + 128 : 0);
+    // (64 B each), the counts, the lists and the batch's images in about 1 GiB
+    const size_t per_sample = (ppm ? 1ull : 2ull) * nrec * 64 + 4 + 12 + (ppm ? 0 : 16ull * nrec * (nrec + 1)) +
+                              (grid_on ? 12ull * nrec + 4 : 0) + (vcm ? 128 : 0) + (ppm ? 16ull * nrec : 0);
     const uint64_t max_samples = std::max<uint64_t>(npix, (1ull << 30) / per_sample);
     const uint32_t per_batch = (uint32_t)std::min<uint64_t>(spp, std::max<uint64_t>(1, max_samples / npix));
     const uint64_t nsamp = (uint64_t)npix * per_batch;
     if (nsamp > 0xffffffffull) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "image too large");
-    WR_CUDA(ctx, st.eye.reserve(64ull * nrec * nsamp));
+    if (!ppm) WR_CUDA(ctx, st.eye.reserve(64ull * nrec * nsamp));
     WR_CUDA(ctx, st.light.reserve(64ull * nrec * nsamp));
     WR_CUDA(ctx, st.counts.reserve(4ull * nsamp + 40));
-    WR_CUDA(ctx, st.cand.reserve(8ull * nrec * (nrec + 1) * nsamp));
-    WR_CUDA(ctx, st.vis.reserve(8ull * nrec * (nrec + 1) * nsamp));
+    if (!ppm) {
+        WR_CUDA(ctx, st.cand.reserve(8ull * nrec * (nrec + 1) * nsamp));
+        WR_CUDA(ctx, st.vis.reserve(8ull * nrec * (nrec + 1) * nsamp));
+    }
     const size_t film_bytes = 12ull * nsamp;
     if (st.film.bytes < film_bytes) {
         WR_CUDA(ctx, st.film.reserve(film_bytes));
@@ -894,7 +1028,8 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
     P.cand = st.cand.as<uint2>();
     P.vis = st.vis.as<uint2>();
     P.vcm = vcm;
-    if (vcm) {
+    P.light_only = ppm;
+    if (grid_on) {
         WR_CUDA(ctx, st.pts.reserve(8ull * nrec * nsamp));
         WR_CUDA(ctx, st.next.reserve(4ull * nrec * nsamp));
         WR_CUDA(ctx, st.head.reserve(4ull * nsamp));
@@ -905,34 +1040,42 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
         P.head = st.head.as<int>();
         P.bbox = st.bbox.as<int>();
         P.radii = st.radii.as<float>();
+    }
+    if (vcm) {
         // the merge list: 8 merges per sample of the batch (more are evaluated where found)
         P.merge_cap = 8ull * nsamp;
         WR_CUDA(ctx, st.merges.reserve(16ull * P.merge_cap));
         P.merges = st.merges.as<uint4>();
     }
-    // the three list counters live after the per-sample counts (8-byte aligned)
+    if (ppm) {
+        WR_CUDA(ctx, st.tput.reserve(16ull * nrec * nsamp));
+        P.tput = st.tput.as<float4>();
+    }
+    // the four list counters live after the per-sample counts (8-byte aligned)
     P.ncand = reinterpret_cast<unsigned long long*>(st.counts.as<char>() + ((4ull * nsamp + 7) & ~7ull));
     const int block = 128;
     const size_t smem = (size_t)RP.stack_cap * block * sizeof(uint32_t);
     if (smem > 48 * 1024) {
         WR_CUDA(ctx, cudaFuncSetAttribute(k_bpt_subpaths, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         WR_CUDA(ctx, cudaFuncSetAttribute(k_bpt_visible, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        WR_CUDA(ctx, cudaFuncSetAttribute(k_ppm_eye, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     }
     int per_sm = 0, per_sm_v = 0;
     WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bpt_connect, block, 0));
     WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_v, k_bpt_visible, block, smem));
     const int connect_grid = std::max(1, per_sm) * std::max(1, ctx->num_sms);
     const int visible_grid = std::max(1, per_sm_v) * std::max(1, ctx->num_sms);
+    const int stride_grid = std::max(1, ctx->num_sms) * 8;
     for (uint32_t done = 0; done < spp; done += per_batch) {
         const uint32_t b = std::min(per_batch, spp - done);
         P.s0 = spp_offset + done;
         P.nsamp = npix * b;
         P.eye.nsamp = P.light.nsamp = P.nsamp;
         const int grid = (int)((P.nsamp + block - 1) / block);
-        k_bpt_subpaths<<<dim3(grid, 2), block, smem, stream>>>(S, P, err);
+        k_bpt_subpaths<<<dim3(grid, ppm ? 1 : 2), block, smem, stream>>>(S, P, err);
         WR_CUDA(ctx, cudaGetLastError());
         WR_CUDA(ctx, cudaMemsetAsync(P.ncand, 0, 4 * sizeof(unsigned long long), stream));
-        if (vcm) {  // the batch's hash grids: one per slot (iteration)
+        if (grid_on) {  // the batch's hash grids: one per slot (iteration)
             st.h_radii.resize(b);
             for (uint32_t k = 0; k < b; k++) st.h_radii[k] = vcm_radius(base_radius, P.s0 + k);
             WR_CUDA(ctx, cudaMemcpyAsync(st.radii.p, st.h_radii.data(), 4ull * b, cudaMemcpyHostToDevice, stream));
@@ -940,16 +1083,25 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
             WR_CUDA(ctx, cudaMemsetAsync(P.head, 0xff, 4ull * P.nsamp, stream));
             k_vcm_points<<<grid, block, 0, stream>>>(S, P);
             WR_CUDA(ctx, cudaGetLastError());
-            k_vcm_link<<<std::max(1, ctx->num_sms) * 8, 256, 0, stream>>>(P);
+            k_vcm_link<<<stride_grid, 256, 0, stream>>>(P);
             WR_CUDA(ctx, cudaGetLastError());
             ctx->kernel_launches += 2;
         }
-        k_bpt_enum<<<grid, block, 0, stream>>>(S, P);
-        WR_CUDA(ctx, cudaGetLastError());
-        k_bpt_visible<<<visible_grid, block, smem, stream>>>(S, P, err);
-        WR_CUDA(ctx, cudaGetLastError());
-        k_bpt_connect<<<connect_grid, block, 0, stream>>>(S, P);
-        WR_CUDA(ctx, cudaGetLastError());
+        if (ppm) {
+            k_ppm_tput<<<stride_grid, 256, 0, stream>>>(S, P);
+            WR_CUDA(ctx, cudaGetLastError());
+            k_ppm_eye<<<grid, block, smem, stream>>>(S, P, err);
+            WR_CUDA(ctx, cudaGetLastError());
+            ctx->kernel_launches += 2;
+        } else {
+            k_bpt_enum<<<grid, block, 0, stream>>>(S, P);
+            WR_CUDA(ctx, cudaGetLastError());
+            k_bpt_visible<<<visible_grid, block, smem, stream>>>(S, P, err);
+            WR_CUDA(ctx, cudaGetLastError());
+            k_bpt_connect<<<connect_grid, block, 0, stream>>>(S, P);
+            WR_CUDA(ctx, cudaGetLastError());
+            ctx->kernel_launches += 3;
+        }
         if (vcm) {
             k_vcm_merge<<<grid, block, 0, stream>>>(S, P);
             WR_CUDA(ctx, cudaGetLastError());
@@ -959,7 +1111,7 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
         }
         k_bpt_resolve<<<(npix + 255) / 256, 256, 0, stream>>>(S.cam, P.film, npix, b, d_sum, d_sumsq);
         WR_CUDA(ctx, cudaGetLastError());
-        ctx->kernel_launches += 5;
+        ctx->kernel_launches += 2;
     }
     return WR_OK;
 }

@@ -17,6 +17,7 @@ struct RenderData {
     std::vector<std::unique_ptr<DeviceBuffer>> grid_data;
     std::string unsupported;  // non-empty: this scene cannot be rendered (why)
     bool has_media = false;
+    bool has_aniso = false;
 };
 
 namespace {
@@ -198,6 +199,7 @@ int prepare_render(wr_ctx* ctx, SceneGPU* sc, RenderData** out) {
     S.grids = rd->grids.as<GridDev>();
     for (const wr_object_desc& m : sc->objects)
         if (m.type == WR_MAT_HOMOGENEOUS || m.type == WR_MAT_HETEROGENEOUS) rd->has_media = true;
+        else if (m.type == WR_MAT_ANISO) rd->has_aniso = true;
     for (const wr_object_desc& m : sc->objects)
         if (m.type == WR_MAT_HETEROGENEOUS &&
             !(m.sigma_s[0] + m.sigma_a[0] == m.sigma_s[1] + m.sigma_a[1] &&
@@ -220,10 +222,10 @@ int wr_render_device(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, fl
     SceneGPU* sc = find_scene(ctx, id);
     if (!sc) return set_error(ctx, WR_ERR_NOT_FOUND, "no such scene");
     if (desc->mode != WR_MODE_MEGAKERNEL && desc->mode != WR_MODE_WAVEFRONT && desc->mode != WR_MODE_BIDIRECTIONAL &&
-        desc->mode != WR_MODE_VCM)
+        desc->mode != WR_MODE_VCM && desc->mode != WR_MODE_PHOTON_MAP)
         return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "unknown render mode");
-    if (desc->mode == WR_MODE_VCM && !(desc->radius >= 0.f && desc->radius < 1e30f))
-        return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "VCM merge radius must be finite and >= 0");
+    if ((desc->mode == WR_MODE_VCM || desc->mode == WR_MODE_PHOTON_MAP) && !(desc->radius >= 0.f && desc->radius < 1e30f))
+        return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "merge / photon radius must be finite and >= 0");
     if (desc->flags & ~RENDER_KNOWN_FLAGS) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "unknown render flags");
     if ((uint64_t)desc->spp_offset + desc->spp > 0xffffffffull)
         return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "sample index range overflows 32 bits");
@@ -242,14 +244,19 @@ int wr_render_device(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, fl
         P.flags = desc->flags;
         P.stack_cap = (int)sc->tree.max_depth + 3;
         const uint64_t npix = (uint64_t)rd->S.cam.width * rd->S.cam.height;
-        if (desc->mode == WR_MODE_BIDIRECTIONAL || desc->mode == WR_MODE_VCM) {
+        if (desc->mode == WR_MODE_BIDIRECTIONAL || desc->mode == WR_MODE_VCM || desc->mode == WR_MODE_PHOTON_MAP) {
             if (rd->has_media)
                 return set_error(ctx, WR_ERR_UNSUPPORTED,
-                                 "bidirectional / VCM mode: participating media are not supported");
+                                 "bidirectional / VCM / photon-mapping mode: participating media are not supported");
             if (desc->flags & WR_RENDER_NEE)
-                return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "bidirectional / VCM mode has no NEE switch");
-            const bool vcm = desc->mode == WR_MODE_VCM;
-            return render_bidirectional(ctx, rd->S, P, desc->spp_offset, desc->spp, d_sum, d_sumsq, err, s, vcm,
+                return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "bidirectional / VCM / photon-mapping mode has no NEE switch");
+            if (desc->mode == WR_MODE_PHOTON_MAP && rd->has_aniso)
+                return set_error(ctx, WR_ERR_UNSUPPORTED,
+                                 "photon-mapping mode: anisotropic glossy objects (the reference's ellipse kernel) are "
+                                 "not supported");
+            const int kind = desc->mode == WR_MODE_VCM ? BIDIR_VCM
+                           : desc->mode == WR_MODE_PHOTON_MAP ? BIDIR_PHOTON_MAP : BIDIR_BPT;
+            return render_bidirectional(ctx, rd->S, P, desc->spp_offset, desc->spp, d_sum, d_sumsq, err, s, kind,
                                         desc->radius > 0.f ? desc->radius : 0.01f);
         }
         if (desc->mode == WR_MODE_WAVEFRONT) {

@@ -29,12 +29,13 @@ struct RenderParams {
 cudaError_t launch_megakernel(const RenderScene& S, const RenderParams& P, float* film, float* film2,
                               unsigned int* err, cudaStream_t stream);
 
-// WR_MODE_BIDIRECTIONAL and WR_MODE_VCM (bpt.cu): adds samples
-// [spp_offset, spp_offset + spp) of every pixel to d_sum (and their squares
-// to d_sumsq, may be NULL); `vcm` adds vertex merging with base radius
-// `base_radius`
+// WR_MODE_BIDIRECTIONAL, WR_MODE_VCM and WR_MODE_PHOTON_MAP (bpt.cu): adds
+// samples [spp_offset, spp_offset + spp) of every pixel to d_sum (and their
+// squares to d_sumsq, may be NULL); `base_radius` is the merge / photon
+// radius of the first iteration
+enum : int { BIDIR_BPT = 0, BIDIR_VCM = 1, BIDIR_PHOTON_MAP = 2 };
 int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& P, uint32_t spp_offset, uint32_t spp,
-                         float* d_sum, float* d_sumsq, unsigned int* err, cudaStream_t stream, bool vcm = false,
+                         float* d_sum, float* d_sumsq, unsigned int* err, cudaStream_t stream, int kind = BIDIR_BPT,
                          float base_radius = 0.01f);
 
 }  // namespace wr
