@@ -22,19 +22,20 @@ from the reference sources) on small seeded scenes and stores its answers:
   mesh_ref.npz        the reference's Mesh::loadShape of those meshes
                       (single objects and a group), world positions
   render_bpt_*.npz    BidirectionalPathTracer::renderPixels on the Cornell,
-                      mirror, thin-lens and mixed-material scenes, 8
-                      reference renders of 64 spp each
+                      mirror, thin-lens, mixed-material and homogeneous-fog
+                      scenes, 8 reference renders of 64 spp each
   render_vcm_*.npz    VCMTracer::renderPixels (base radius 0.02) on the
-                      Cornell, mirror and thin-lens scenes, 8 reference
-                      renders of 64 spp each
+                      Cornell, mirror, thin-lens and homogeneous-fog scenes,
+                      8 reference renders of 64 spp each
 
   render_ppm_*.npz    PhotonMap::renderPixels (base radius 0.02) on the
                       Cornell, mirror, thin-lens and mixed-material scenes, 8
                       reference renders of 64 spp each
 
-Usage: python tests/golden/make_golden.py [bpt|vcm|ppm]   (needs the
-reference tree on this machine; `bpt` / `vcm` / `ppm` remake only those
-renders; the fixtures it writes are what the tests read elsewhere)
+Usage: python tests/golden/make_golden.py [bpt|vcm|ppm [scene ...]]   (needs
+the reference tree on this machine; `bpt` / `vcm` / `ppm` remake only those
+renders, of the scenes named after it if any; the fixtures it writes are what
+the tests read elsewhere)
 """
 from __future__ import annotations
 
@@ -65,6 +66,7 @@ def golden_scenes():
         "media_small": S.cornell_media(32, 32, grid_n=16, seed=3),
         "mirror": S.cornell_mirror(32, 32),
         "dof": S.cornell_dof(32, 32, lens_radius=0.2),
+        "fog": S.cornell_fog(32, 32, ior=1.2),
     }
 
 
@@ -219,28 +221,28 @@ def mesh_fixtures(td):
     np.savez_compressed(os.path.join(HERE, "mesh_ref.npz"), **out)
 
 
-BPT_SCENES = ("cornell", "mirror", "dof", "mixed_l2")
+BPT_SCENES = ("cornell", "mirror", "dof", "mixed_l2", "fog")
 
 
-def bpt_fixtures(td):
+def bpt_fixtures(td, names=BPT_SCENES):
     """BidirectionalPathTracer::renderPixels (bidirPathTracer.cpp:10-56), 8
     reference renders of 64 spp per scene, depth 8."""
     sc = golden_scenes()
     p = os.path.join(td, "s.wrs")
-    for name in BPT_SCENES:
+    for name in names:
         render_set(sc[name], p, td, f"render_bpt_{name}.npz", extra=("bpt",), spp=64)
 
 
-VCM_SCENES = ("cornell", "mirror", "dof")
+VCM_SCENES = ("cornell", "mirror", "dof", "fog")
 VCM_RADIUS = 0.02
 
 
-def vcm_fixtures(td):
+def vcm_fixtures(td, names=VCM_SCENES):
     """VCMTracer::renderPixels (vcmTracer.cpp:6-92), base radius 0.02, 8
     reference renders of 64 spp per scene, depth 8."""
     sc = golden_scenes()
     p = os.path.join(td, "s.wrs")
-    for name in VCM_SCENES:
+    for name in names:
         render_set(sc[name], p, td, f"render_vcm_{name}.npz", extra=("vcm", str(VCM_RADIUS)), spp=64)
 
 
@@ -248,12 +250,12 @@ PPM_SCENES = ("cornell", "mirror", "dof", "mixed_l2")
 PPM_RADIUS = 0.02
 
 
-def ppm_fixtures(td):
+def ppm_fixtures(td, names=PPM_SCENES):
     """PhotonMap::renderPixels (photonMap.cpp:20-148), base radius 0.02, 8
     reference renders of 64 spp per scene, depth 8."""
     sc = golden_scenes()
     p = os.path.join(td, "s.wrs")
-    for name in PPM_SCENES:
+    for name in names:
         render_set(sc[name], p, td, f"render_ppm_{name}.npz", extra=("ppm", str(PPM_RADIUS)), spp=64)
 
 
@@ -261,9 +263,12 @@ def main():
     if not os.path.exists(REF):
         sys.exit("build the reference harness first: make -C oracle ref")
     only = {"bpt": bpt_fixtures, "vcm": vcm_fixtures, "ppm": ppm_fixtures}
-    if len(sys.argv) == 2 and sys.argv[1] in only:  # only those renders
+    if len(sys.argv) >= 2 and sys.argv[1] in only:  # only those renders (of the scenes named after it)
         with tempfile.TemporaryDirectory() as td:
-            only[sys.argv[1]](td)
+            if len(sys.argv) > 2:
+                only[sys.argv[1]](td, sys.argv[2:])
+            else:
+                only[sys.argv[1]](td)
         return
     sc = golden_scenes()
     with tempfile.TemporaryDirectory() as td:

@@ -18,7 +18,7 @@ from walkray_gb300 import scenes as S
 
 pytestmark = pytest.mark.gpu
 
-SCENES = ["cornell", "mirror", "dof", "mixed_l2"]
+SCENES = ["cornell", "mirror", "dof", "mixed_l2", "fog"]
 
 
 def block_z(a, b, k):

@@ -153,7 +153,7 @@ def test_oracle_thin_lens_matches_reference_statistically(built):
     assert np.abs(zp).max() > 4.5, np.abs(zp).max()
 
 
-@pytest.mark.parametrize("name", ["cornell", "mirror", "dof", "mixed_l2"])
+@pytest.mark.parametrize("name", ["cornell", "mirror", "dof", "mixed_l2", "fog"])
 def test_oracle_bidirectional_matches_reference_statistically(built, name):
     """BidirectionalPathTracer (bidirPathTracer.cpp:10-313): the restated
     connections, MIS weights and light-tracing splats vs 8 reference renders
@@ -177,7 +177,7 @@ def test_oracle_bidirectional_refuses_media(built):
         orc.render_bpt(1, 8, seed=1)
 
 
-@pytest.mark.parametrize("name", ["cornell", "mirror", "dof"])
+@pytest.mark.parametrize("name", ["cornell", "mirror", "dof", "fog"])
 def test_oracle_vcm_matches_reference_statistically(built, name):
     """VCMTracer (vcmTracer.cpp:6-446), base radius 0.02: the restated
     connections with VCM weights and merges through the reference's hash grid

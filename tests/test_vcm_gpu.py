@@ -49,7 +49,7 @@ def rotated(s):
     return s
 
 
-@pytest.mark.parametrize("name", ["cornell", "mirror", "dof", "mixed_l2"])
+@pytest.mark.parametrize("name", ["cornell", "mirror", "dof", "mixed_l2", "fog"])
 def test_vcm_paired_with_oracle(ctx, name):
     s = rotated(make_golden.golden_scenes()[name])
     h, w = s.camera.height, s.camera.width

@@ -29,8 +29,10 @@
 // the two connection vertices, which connectEdge changes and which live in
 // registers.  Draws: the eye sub-path takes the Philox stream of (pixel,
 // sample) from draw 0, the light sub-path the same stream from draw 2^30;
-// the connections draw nothing.  Participating media are not covered (their
-// densities in the MIS weight); such scenes are refused by the caller.
+// the connections draw nothing.  Homogeneous media take part (their
+// free-flight densities are origin densities of the MIS weights);
+// heterogeneous ones do not (their densities need an integration along every
+// link) and scenes with one are refused by the caller.
 #include <algorithm>
 #include <memory>
 
@@ -267,6 +269,11 @@ __device__ float bpt_dir_prob(const RenderScene& S, f3 in_d, const PRay& out, bo
         pdf /= 4.f * fabsf(dot(in_d, h));
         return pdf;
     }
+    if (t == WR_MAT_HOMOGENEOUS) {  // homogeneousVolume.cpp:216-223 (a boundary record is delta)
+        if (out.delta) return 0.f;
+        const f3 ss = ld3(m->sigma_s), st = ss + ld3(m->sigma_a);
+        return luminance(ss) / luminance(st) * hg_value(__ldg(&m->g), in_d, out.d);
+    }
     if (t == WR_MAT_REFLECTIVE) {  // reflectiveObj.h:44-46 with the unparenthesised MAX_VEC_COMP
         const f3 c = ld3(m->albedo);
         return c.x > c.y ? c.x : (c.y > c.z ? c.y : c.z);
@@ -279,6 +286,21 @@ __device__ float bpt_dir_prob(const RenderScene& S, f3 in_d, const PRay& out, bo
 __device__ __forceinline__ f3 bpt_eval_bsdf(const RenderScene& S, f3 in_d, const PRay& out) {
     if (out.contact == CAMERA_OBJ) return mk(1, 1, 1);
     return eval_bsdf(S, in_d, out);
+}
+
+// Ray::evalOriginProbability (ray.cpp:24-30) of the link from a record at
+// `in_o` whose inside object is `in_inside` to a record at `out_o`: 1 but in
+// a homogeneous medium, whose surface / medium free-flight density over the
+// distance (homogeneousVolume.cpp:209-214, homogeneousVolume.h:40-53) it is
+__device__ __forceinline__ float bpt_origin_prob(const RenderScene& S, int in_inside, f3 in_o, f3 out_o,
+                                                 int out_contact) {
+    if (in_inside < 0 || obj_type(S, in_inside) != WR_MAT_HOMOGENEOUS) return 1.f;
+    const wr_object_desc* m = &S.objs[in_inside];
+    const f3 st = ld3(m->sigma_s) + ld3(m->sigma_a);
+    const float d0 = length(in_o - out_o);
+    const float dist = (double)d0 > 1e-5 ? d0 : (float)1e-5;
+    const f3 e = mk(expf(-st.x * dist), expf(-st.y * dist), expf(-st.z * dist));
+    return out_contact != -1 ? luminance(e) : luminance(vmul(st, e));
 }
 
 __device__ __forceinline__ bool emissive(const RenderScene& S, int o) {
@@ -332,13 +354,16 @@ __device__ float bpt_mis_weight(const RenderScene& S, const Conn& C, uint32_t pi
         rev[i] = rev[i + 1] * (double)pdf_w_to_a(dist, cos_term(S, lr));
         if (!v1.delta) {
             float dirp;
+            const PRay b = link(C, i + 1, true, v1, vi);
             if (i < n - 2) {
-                const PRay a = link(C, i + 2, true, v2, v1), b = link(C, i + 1, true, v1, vi);
+                const PRay a = link(C, i + 2, true, v2, v1);
                 dirp = bpt_dir_prob(S, a.d, b, false, pixel);
             } else {
                 dirp = bpt_dir_prob(S, v1.d, v1, true, pixel);  // vertex n-1 is the camera, never re-pointed
             }
-            rev[i] *= (double)dirp;
+            // link(i+1, reverse).evalOriginProbability(link(i, reverse))
+            const float ori = bpt_origin_prob(S, b.inside, v1.o, vi.o, vi.contact);
+            rev[i] *= (double)(dirp * ori);
         }
         v2 = v1;
         v1 = vi;
@@ -360,21 +385,24 @@ __device__ float bpt_mis_weight(const RenderScene& S, const Conn& C, uint32_t pi
         const float g = pdf_w_to_a(dist, cos_term(S, lr));
         const double dir_prev = dir;
         dir = dir * (double)g;
-        float dirp = 1.f;
+        float dirp = 1.f, ori = 1.f;
         if (!pm1.delta) {
+            const PRay b = link(C, i - 1, false, pm1, vi);
             if (i > 1) {
-                const PRay a = link(C, i - 2, false, pm2, pm1), b = link(C, i - 1, false, pm1, vi);
+                const PRay a = link(C, i - 2, false, pm2, pm1);
                 dirp = bpt_dir_prob(S, a.d, b, false, pixel);
             } else {
-                const PRay r = link(C, 0, false, pm1, vi);
-                dirp = bpt_dir_prob(S, r.d, r, true, pixel);
+                dirp = bpt_dir_prob(S, b.d, b, true, pixel);
             }
-            dir *= (double)dirp;
+            // link(i-1).evalOriginProbability(link(i))
+            ori = bpt_origin_prob(S, b.inside, pm1.o, vi.o, vi.contact);
+            dir *= (double)(dirp * ori);
         }
         if (K.vcm && i - 1 < n - 2 && !vi.delta) {  // merging at vertex i (vcmTracer.cpp:298-318)
             double p = dir_prev * rev[i];
             if (!pm1.delta) p *= (double)dirp;
-            p *= 1.0;  // link(i-1).evalOriginProbability(link(i)): 1 for surfaces
+            p *= (double)(pm1.delta ? bpt_origin_prob(S, link(C, i - 1, false, pm1, vi).inside, pm1.o, vi.o, vi.contact)
+                                    : ori);  // link(i-1).evalOriginProbability(link(i))
             p *= (double)g;
             p *= PI_D * K.radius * K.radius;
             if (vi.inside >= 0 && vi.contact == -1) p *= 4.0 / 3 * K.radius;
@@ -427,6 +455,7 @@ __device__ void bpt_color_prob(const RenderScene& S, const Conn& C, f3& color, f
         if (merge && i == c) {
             pr = (float)((double)pr * (PI_D * radius * radius));
             pr *= pdf_w_to_a(dist, cos_term(S, nx));  // link(c + 1, reverse): the eye vertex as connected
+            pr *= bpt_origin_prob(S, cur.inside, cur.o, nx.o, nx.contact);  // link(c).evalOriginProbability(link(c+1))
             if (nx.inside >= 0 && nx.contact == -1) pr = (float)((double)pr * (4.0 / 3 * radius));
         }
         prev = cur;

@@ -17,6 +17,7 @@ struct RenderData {
     std::vector<std::unique_ptr<DeviceBuffer>> grid_data;
     std::string unsupported;  // non-empty: this scene cannot be rendered (why)
     bool has_media = false;
+    bool has_hetero = false;
     bool has_aniso = false;
 };
 
@@ -197,9 +198,11 @@ int prepare_render(wr_ctx* ctx, SceneGPU* sc, RenderData** out) {
     }
     WR_CUDA(ctx, upload(rd->grids, gd));
     S.grids = rd->grids.as<GridDev>();
-    for (const wr_object_desc& m : sc->objects)
+    for (const wr_object_desc& m : sc->objects) {
         if (m.type == WR_MAT_HOMOGENEOUS || m.type == WR_MAT_HETEROGENEOUS) rd->has_media = true;
-        else if (m.type == WR_MAT_ANISO) rd->has_aniso = true;
+        if (m.type == WR_MAT_HETEROGENEOUS) rd->has_hetero = true;
+        if (m.type == WR_MAT_ANISO) rd->has_aniso = true;
+    }
     for (const wr_object_desc& m : sc->objects)
         if (m.type == WR_MAT_HETEROGENEOUS &&
             !(m.sigma_s[0] + m.sigma_a[0] == m.sigma_s[1] + m.sigma_a[1] &&
@@ -245,9 +248,12 @@ int wr_render_device(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, fl
         P.stack_cap = (int)sc->tree.max_depth + 3;
         const uint64_t npix = (uint64_t)rd->S.cam.width * rd->S.cam.height;
         if (desc->mode == WR_MODE_BIDIRECTIONAL || desc->mode == WR_MODE_VCM || desc->mode == WR_MODE_PHOTON_MAP) {
-            if (rd->has_media)
+            if (rd->has_hetero)
                 return set_error(ctx, WR_ERR_UNSUPPORTED,
-                                 "bidirectional / VCM / photon-mapping mode: participating media are not supported");
+                                 "bidirectional / VCM / photon-mapping mode: heterogeneous media are not supported");
+            if (desc->mode == WR_MODE_PHOTON_MAP && rd->has_media)
+                return set_error(ctx, WR_ERR_UNSUPPORTED,
+                                 "photon-mapping mode: participating media (volume photons) are not supported");
             if (desc->flags & WR_RENDER_NEE)
                 return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "bidirectional / VCM / photon-mapping mode has no NEE switch");
             if (desc->mode == WR_MODE_PHOTON_MAP && rd->has_aniso)

@@ -509,6 +509,7 @@ __device__ __forceinline__ PRay medium_enter(const RenderScene& S, int self, con
     const float cn = in.inside >= 0 ? obj_ior(S, in.inside) : 1.f, nn = obj_ior(S, self);
     out.contact = self;
     out.cnorm = N;
+    out.delta = true;  // every boundary outcome is a delta direction (homogeneousVolume.cpp:45-80)
     const Fresnel f = fresnel_split(N, in.d, cn, nn);
     if (f.tir) {
         out.d = f.refl;
@@ -552,6 +553,7 @@ __device__ __forceinline__ PRay medium_exit(const RenderScene& S, int self, cons
     const int curOut = st.below(self);
     const float cn = obj_ior(S, self), nn = curOut >= 0 ? obj_ior(S, curOut) : 1.f;
     out.iobj = -1;
+    out.delta = true;  // every boundary outcome is a delta direction (homogeneousVolume.cpp:141-186)
     const Fresnel f = fresnel_split(N, in.d, cn, nn);
     if (f.tir) {
         out.d = f.refl;

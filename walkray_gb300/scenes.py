@@ -523,6 +523,19 @@ def cornell_media(width=512, height=512, grid_n=128, seed=3) -> Scene:
     return s
 
 
+def cornell_fog(width=256, height=256, ior=1.0) -> Scene:
+    """Cornell box plus one homogeneous sphere (radius 0.2, sigma_t = 1.5,
+    albedo 0.8, HG g = -0.2): participating media without a density grid."""
+    s = Scene("cornell_fog")
+    _cornell_objects(s)
+    P, F = icosphere(3)
+    P = (P * 0.2 + np.array([0.55, 0.5, 0.35])).astype(np.float32)
+    s.add(MAT_HOMOGENEOUS, P, F, sigma_s=(1.2, 1.2, 1.2), sigma_a=(0.3, 0.3, 0.3), g=-0.2, ior=ior)
+    c = CORNELL_CAMERA
+    s.camera = Camera.from_fov(c["position"], c["focus"], c["up"], width, height, c["fov"])
+    return s
+
+
 def save_rays(path: str, rays: np.ndarray) -> None:
     rays = np.ascontiguousarray(rays, np.float32)
     with open(path, "wb") as fh:
