@@ -364,6 +364,11 @@ typedef struct wr_scene_file_settings {
     char renderer[32];     /* the <renderer> name, e.g. "PathTracer" / "PT" */
     uint32_t spp;          /* <iter> (0 when absent) */
     uint32_t max_path_len; /* 20, as Config::load sets for every renderer */
+    float radius;          /* <radius> of the VCM / photon-map renderers (0 when absent) */
+    uint32_t mode;         /* the WR_MODE_* of the renderer name (config.cpp:530-572):
+                              PathTracer/PT -> WR_MODE_WAVEFRONT, BidirPathTracer/BPT ->
+                              WR_MODE_BIDIRECTIONAL, VCMTracer/VCM -> WR_MODE_VCM,
+                              PhotonMap/PM -> WR_MODE_PHOTON_MAP; 0xffffffff for any other */
 } wr_scene_file_settings;
 int wr_scene_file_load(const char* config_path, wr_scene_file** out, char* err, size_t err_len);
 int wr_scene_file_get(const wr_scene_file* f, wr_scene_desc* desc, wr_scene_file_settings* settings);

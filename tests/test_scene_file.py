@@ -51,7 +51,7 @@ def test_reference_quirks_are_kept(loaded):
 
 def test_materials_camera_and_settings(loaded):
     scene, settings = loaded
-    assert settings == {"renderer": "PathTracer", "spp": 64, "max_path_len": 20}
+    assert settings == {"renderer": "PathTracer", "spp": 64, "max_path_len": 20, "radius": 0.0, "mode": "wavefront"}
     objs, _, _, grids = scene.flatten()
     t = [int(x) for x in objs["type"]]
     assert t == [S.MAT_GLOSSY, S.MAT_REFLECTIVE, S.MAT_ANISO, S.MAT_REFRACTIVE, S.MAT_HETEROGENEOUS,
@@ -107,6 +107,16 @@ def test_unsupported_or_broken_files_fail_clearly(built, tmp_path, old, new, fil
         api.load_scene_file(cfg)
     if msg:
         assert msg in str(e.value)
+
+
+@pytest.mark.parametrize("name,mode", [("BPT", "bidirectional"), ("BidirPathTracer", "bidirectional"),
+                                       ("VCMTracer", "vcm"), ("PM", "photon_map"), ("Whitted", None)])
+def test_renderer_names_select_modes(built, tmp_path, name, mode):
+    """Config::load's renderer names (config.cpp:530-572) and <radius>."""
+    cfg = _variant(tmp_path, "<renderer>PathTracer</renderer>", f"<renderer>{name}</renderer><radius>0.03</radius>",
+                   "config.xml")
+    _, st = api.load_scene_file(cfg)
+    assert st["mode"] == mode and st["renderer"] == name and st["radius"] == pytest.approx(0.03)
 
 
 def test_missing_config_file(built):

@@ -65,7 +65,8 @@ class wr_scene_desc(C.Structure):
 
 
 class wr_scene_file_settings(C.Structure):
-    _fields_ = [("renderer", C.c_char * 32), ("spp", C.c_uint32), ("max_path_len", C.c_uint32)]
+    _fields_ = [("renderer", C.c_char * 32), ("spp", C.c_uint32), ("max_path_len", C.c_uint32),
+                ("radius", C.c_float), ("mode", C.c_uint32)]
 
 
 class wr_hit(C.Structure):

@@ -291,7 +291,9 @@ def load_scene_file(path: str):
         c = d.camera
         s.camera = Camera(tuple(c.position), tuple(c.focus), tuple(c.up), int(c.width), int(c.height),
                           float(c.image_plane_dist), float(c.lens_radius), float(c.focal_dist))
-        settings = {"renderer": st.renderer.decode(), "spp": int(st.spp), "max_path_len": int(st.max_path_len)}
+        mode = {v: k for k, v in MODES.items()}.get(int(st.mode))
+        settings = {"renderer": st.renderer.decode(), "spp": int(st.spp), "max_path_len": int(st.max_path_len),
+                    "radius": float(st.radius), "mode": mode}
         return s, settings
     finally:
         lib.wr_scene_file_free(h)

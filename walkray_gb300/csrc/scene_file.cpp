@@ -503,6 +503,8 @@ struct wr_scene_file {
     wr_camera_desc camera{};
     char renderer[32] = {0};
     uint32_t spp = 0, max_path_len = 20;
+    float radius = 0.f;
+    uint32_t mode = 0xffffffffu;
 };
 
 namespace {
@@ -842,6 +844,15 @@ int load(const char* config_path, wr_scene_file* out, std::string& err) {
         out->spp = v > 0 ? (uint32_t)std::fmin(v, 4294967295.0) : 0u;
     }
     out->max_path_len = 20;
+    // <radius> of VCMTracer / PhotonMap (config.cpp:560, 571: setRadius(atof(...)))
+    out->radius = 0.f;
+    if (const XNode* rr = config->first("radius")) out->radius = (float)atof(rr->value());
+    const std::string name = out->renderer;
+    out->mode = (name == "PathTracer" || name == "PT")             ? WR_MODE_WAVEFRONT
+                : (name == "BidirPathTracer" || name == "BPT") ? WR_MODE_BIDIRECTIONAL
+                : (name == "VCMTracer" || name == "VCM")       ? WR_MODE_VCM
+                : (name == "PhotonMap" || name == "PM")        ? WR_MODE_PHOTON_MAP
+                                                               : 0xffffffffu;
     for (size_t k = 0; k < out->grids.size(); k++) out->grids[k].density = out->grid_data[k].data();
     return WR_OK;
 }
@@ -890,6 +901,8 @@ int wr_scene_file_get(const wr_scene_file* f, wr_scene_desc* desc, wr_scene_file
         memcpy(settings->renderer, f->renderer, sizeof settings->renderer);
         settings->spp = f->spp;
         settings->max_path_len = f->max_path_len;
+        settings->radius = f->radius;
+        settings->mode = f->mode;
     }
     return WR_OK;
 }
