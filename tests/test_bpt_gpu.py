@@ -97,3 +97,19 @@ def test_bidirectional_without_lights_is_black(ctx):
     img = ctx.render(sid, 4, 8, mode="bidirectional")
     assert not img.any()
     ctx.release(sid)
+
+
+def test_scratch_beyond_the_memory_budget_is_refused():
+    """One sample of every pixel is the smallest batch; a context whose
+    device-memory budget cannot hold its scratch gets WR_ERR_OUT_OF_MEMORY
+    (and stays usable for the path tracer)."""
+    from walkray_gb300.api import Context
+
+    small = Context(device=0, memory_budget=1 << 18)
+    sid = small.upload(make_golden.golden_scenes()["cornell"])
+    for mode in ("bidirectional", "vcm", "photon_map"):
+        with pytest.raises(L.WRError) as e:
+            small.render(sid, 1, 8, mode=mode)
+        assert e.value.code == 2 and "budget" in str(e.value)  # WR_ERR_OUT_OF_MEMORY
+    assert small.render(sid, 1, 8, mode="megakernel").mean() > 0
+    small.close()

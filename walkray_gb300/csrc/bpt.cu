@@ -1032,6 +1032,12 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
     const uint32_t per_batch = (uint32_t)std::min<uint64_t>(spp, std::max<uint64_t>(1, max_samples / npix));
     const uint64_t nsamp = (uint64_t)npix * per_batch;
     if (nsamp > 0xffffffffull) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "image too large");
+    // a batch is at least one sample of every pixel (an iteration of the
+    // reference's loop); it must fit in the context's device-memory budget
+    if ((uint64_t)per_sample * nsamp > ctx->memory_budget)
+        return set_error(ctx, WR_ERR_OUT_OF_MEMORY,
+                         "bidirectional / VCM / photon-mapping scratch for one sample of every pixel (" +
+                             std::to_string((uint64_t)per_sample * nsamp) + " bytes) exceeds the device-memory budget");
     if (!ppm) WR_CUDA(ctx, st.eye.reserve(64ull * nrec * nsamp));
     WR_CUDA(ctx, st.light.reserve(64ull * nrec * nsamp));
     WR_CUDA(ctx, st.counts.reserve(4ull * nsamp + 40));
