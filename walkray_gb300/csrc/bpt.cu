@@ -4,11 +4,13 @@
 // One render call runs in batches of samples-per-pixel; a batch of B samples
 // of every pixel is five kernels:
 //
-//   k_bpt_subpaths  one thread per (pixel, sample): the eye sub-path
-//                   (Camera::generateRay + MCRenderer::samplePath) and the
-//                   light sub-path (Scene::genLightSample + samplePath), every
-//                   ray record written to HBM (64 B per vertex, vertex-major so
-//                   that a warp's stores of vertex k are contiguous);
+//   k_bpt_subpaths  persistent: the eye sub-paths (Camera::generateRay +
+//                   MCRenderer::samplePath) and the light sub-paths
+//                   (Scene::genLightSample + samplePath), one record per lane
+//                   and turn, a lane taking a new sub-path as soon as its own
+//                   ends; every ray record written to HBM (64 B per vertex,
+//                   vertex-major so that stores of vertex k of consecutive
+//                   samples are contiguous);
 //   k_bpt_enum      one thread per (pixel, sample): the (light length, eye
 //                   length) pairs that pass throughputByConnecting's path-shape
 //                   tests, appended to a candidate list in runs of one pair;
@@ -105,7 +107,8 @@ struct BptParams {
     float* film;          // per sample slot of the batch: npix * 3 floats
     uint2* cand;          // connection candidates with a light sub-path (l >= 1): {sample, l | e << 8}
     uint2* vis;           // connections that contribute: visible candidates and whole eye paths
-    unsigned long long* ncand;  // [0]: entries of cand, [1]: entries of vis, [2]: light points, [3]: merges
+    unsigned long long* ncand;  // [0]: entries of cand, [1]: entries of vis, [2]: light points, [3]: merges,
+                                // [4]: sub-paths handed out
     // vertex merging (WR_MODE_VCM); per sample slot s of the batch, the hash grid of hashgrid.hxx
     bool vcm;
     const float* radii;   // merge radius of each slot's iteration
@@ -145,88 +148,149 @@ __device__ __forceinline__ void warp_append(bool ok, uint2 item, uint2* list, un
     if (ok) list[base + __popc(want & ((1u << lane) - 1u))] = item;
 }
 
-// MCRenderer::samplePath (mcRenderer.cpp:16-57) from `prev` (its hit set),
-// every record stored; returns the record count (at most max_path_len + 2)
-__device__ int bpt_sample_path(const RenderScene& S, const BptParams& P, const VtxStore& out, uint32_t sid, PRay prev,
-                               PathRng& g, uint32_t* stack, int stride, unsigned int* err) {
-    InsideStack st;
-    st.reset(prev.inside);
-    int n = 0;
-    for (uint32_t depth = 0;; depth++) {
-        out.put(sid, n++, prev);
-        PRay term = ray_default();
-        term.o = prev.o;
-        term.rad = mk(0, 0, 0);
-        term.delta = true;
-        const int self = prev.inside >= 0 ? prev.inside : prev.iobj;
-        if (self < 0) {
-            out.put(sid, n++, term);
-            break;
-        }
-        PRay next = scatter(S, self, prev, g, st);
-        if (length(next.d) < 0.5f) {
-            out.put(sid, n++, next);
-            break;
-        }
-        if (depth + 1 > P.max_path_len) {
-            out.put(sid, n++, term);
-            break;
-        }
-        st.set_top(next.inside);
-        RayQ q = make_rayq(next.o, next.d, S.tree.scene_mag);
-        q.pf = P.pf;
-        const Hit h = trace_closest<true, true>(S.tree, q, next.inside, next.contact, stack, stride, P.stack_cap, err);
-        if (h.slot < 0) {
-            out.put(sid, n++, next);
-            out.put(sid, n++, term);
-            break;
-        }
-        set_hit(S, next, h);
-        prev = next;
-    }
-    return n;
-}
-
-// blockIdx.y = 0: eye sub-paths, 1: light sub-paths (one kind per warp)
+// Persistent: each lane takes sub-paths from a counter (eye sub-paths of
+// samples 0..nsamp-1, then their light sub-paths; light only for photon
+// mapping) and advances its sub-path one record per turn, so that a lane
+// whose path ends takes the next one instead of waiting for the warp's
+// longest path.  A turn: the lane stores its current record and scatters
+// (MCRenderer::samplePath, mcRenderer.cpp:16-57), then every lane with a ray
+// traces it at one call site (the first ray of a sub-path too: the camera
+// ray unfiltered (camera.cpp:52), which a filter with no inside and no
+// contact object is, the emitted ray with NoSelfCondition).
 __global__ void __launch_bounds__(128) k_bpt_subpaths(RenderScene S, BptParams P, unsigned int* __restrict__ err) {
+    constexpr unsigned FULL = 0xffffffffu;
     extern __shared__ uint32_t s_stack[];
     uint32_t* stack = s_stack + threadIdx.x;
     const int stride = blockDim.x;
-    const uint32_t sid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sid >= P.nsamp) return;
-    const uint32_t pixel = sid % P.npix, sample = P.s0 + sid / P.npix;
-    if (blockIdx.y == 0 && !P.light_only) {
-        // eye sub-path: the camera ray is traced without a condition (camera.cpp:52)
-        PathRng g;
-        g.init(P.seed, pixel, sample, 0);
-        PRay cam = camera_ray(S.cam, pixel, g);
-        RayQ q = make_rayq(cam.o, cam.d, S.tree.scene_mag);
-        q.pf = P.pf;
-        const Hit h = trace_closest<false, true>(S.tree, q, -1, -1, stack, stride, P.stack_cap, err);
-        set_hit(S, cam, h);
-        const int ne = bpt_sample_path(S, P, P.eye, sid, cam, g, stack, stride, err);
-        reinterpret_cast<uint8_t*>(P.counts + sid)[0] = (uint8_t)ne;
-        return;
-    }
-    // light sub-path (Scene::genLightSample -> AbstractObject::genSurfaceSample,
-    // abstractObj.cpp:18-52): the emitted ray is traced with NoSelfCondition
-    int nl = 0;
-    if (S.nlights) {
-        PathRng gl;
-        gl.init(P.seed, pixel, sample, BPT_LIGHT_DIM0);
-        PRay lr = light_sample(S, gl);
-        lr.iobj = -1;
-        if (lr.contact >= 0) {
-            lr.inside = __ldg(&S.light_inside[lr.contact]);
-            RayQ q = make_rayq(lr.o, lr.d, S.tree.scene_mag);
-            q.pf = P.pf;
-            const Hit h = trace_closest<true, true>(S.tree, q, lr.inside, lr.contact, stack, stride, P.stack_cap, err);
-            if (h.slot >= 0 && h.t > 0.f) set_hit(S, lr, h);  // `if(dist > 0)`
-            else lr.iobj = -1;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned long long total = (P.light_only ? 1ull : 2ull) * P.nsamp;
+    unsigned long long* counter = P.ncand + 4;
+    bool active = false, exhausted = false, light = false;
+    uint32_t sid = 0, depth = 0;
+    int n = 0;
+    PRay prev = ray_default(), ray = ray_default();
+    InsideStack st;
+    st.reset(-1);
+    PathRng g;
+    g.init(0, 0, 0, 0);
+    for (;;) {
+        // refill idle lanes
+        const bool want = !active && !exhausted;
+        const unsigned need = __ballot_sync(FULL, want);
+        bool fresh = false, has_ray = false;
+        if (need) {
+            const int leader = __ffs(need) - 1;
+            unsigned long long base = 0;
+            if ((int)lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(need));
+            base = __shfl_sync(FULL, base, leader);
+            if (want) {
+                const unsigned long long w = base + __popc(need & ((1u << lane) - 1u));
+                if (w >= total) {
+                    exhausted = true;
+                } else {
+                    light = P.light_only || w >= P.nsamp;
+                    sid = (uint32_t)(light && !P.light_only ? w - P.nsamp : w);
+                    const uint32_t pixel = sid % P.npix, sample = P.s0 + sid / P.npix;
+                    n = 0;
+                    depth = 0;
+                    active = true;
+                    fresh = true;
+                    if (!light) {
+                        g.init(P.seed, pixel, sample, 0);
+                        ray = camera_ray(S.cam, pixel, g);
+                        has_ray = true;
+                    } else if (S.nlights == 0) {  // no emitter: an empty light sub-path
+                        reinterpret_cast<uint8_t*>(P.counts + sid)[1] = 0;
+                        active = false;
+                        fresh = false;
+                    } else {
+                        // Scene::genLightSample -> AbstractObject::genSurfaceSample (abstractObj.cpp:18-52)
+                        g.init(P.seed, pixel, sample, BPT_LIGHT_DIM0);
+                        ray = light_sample(S, g);
+                        ray.iobj = -1;
+                        if (ray.contact >= 0) {
+                            ray.inside = __ldg(&S.light_inside[ray.contact]);
+                            has_ray = true;
+                        }
+                    }
+                }
+            }
         }
-        nl = bpt_sample_path(S, P, P.light, sid, lr, gl, stack, stride, err);
+        if (__ballot_sync(FULL, active) == 0) {
+            if (__ballot_sync(FULL, !exhausted) == 0) break;
+            continue;
+        }
+        // one record of a running sub-path (the samplePath step up to its next ray)
+        PRay next = ray_default();
+        if (active && !fresh) {
+            const VtxStore& out = light ? P.light : P.eye;
+            out.put(sid, n++, prev);
+            PRay term = ray_default();
+            term.o = prev.o;
+            term.rad = mk(0, 0, 0);
+            term.delta = true;
+            const int self = prev.inside >= 0 ? prev.inside : prev.iobj;
+            bool done = false;
+            if (self < 0) {
+                out.put(sid, n++, term);
+                done = true;
+            } else {
+                next = scatter(S, self, prev, g, st);
+                if (length(next.d) < 0.5f) {
+                    out.put(sid, n++, next);
+                    done = true;
+                } else if (depth + 1 > P.max_path_len) {
+                    out.put(sid, n++, term);
+                    done = true;
+                } else {
+                    st.set_top(next.inside);
+                    ray = next;
+                    has_ray = true;
+                }
+            }
+            if (done) {
+                reinterpret_cast<uint8_t*>(P.counts + sid)[light ? 1 : 0] = (uint8_t)n;
+                active = false;
+            }
+        }
+        // every ray of the turn at one call site
+        Hit h;
+        h.t = __int_as_float(0x7f800000);
+        h.slot = -1;
+        if (has_ray) {
+            RayQ q = make_rayq(ray.o, ray.d, S.tree.scene_mag);
+            q.pf = P.pf;
+            const bool filt = !(fresh && !light);
+            h = trace_closest<true, true>(S.tree, q, filt ? ray.inside : -1, filt ? ray.contact : -1, stack, stride,
+                                          P.stack_cap, err);
+        }
+        if (active && fresh) {  // the sub-path's first record, its hit set
+            if (light) {
+                if (has_ray && h.slot >= 0 && h.t > 0.f) set_hit(S, ray, h);  // `if(dist > 0)`
+                else ray.iobj = -1;
+            } else {
+                set_hit(S, ray, h);
+            }
+            prev = ray;
+            st.reset(prev.inside);
+        } else if (active && has_ray) {
+            if (h.slot < 0) {  // a scattered ray that escapes: it and the terminating record end the path
+                const VtxStore& out = light ? P.light : P.eye;
+                PRay term = ray_default();
+                term.o = prev.o;
+                term.rad = mk(0, 0, 0);
+                term.delta = true;
+                out.put(sid, n++, ray);
+                out.put(sid, n++, term);
+                reinterpret_cast<uint8_t*>(P.counts + sid)[light ? 1 : 0] = (uint8_t)n;
+                active = false;
+            } else {
+                set_hit(S, ray, h);
+                prev = ray;
+                depth++;
+            }
+        }
     }
-    reinterpret_cast<uint8_t*>(P.counts + sid)[1] = (uint8_t)nl;
 }
 
 // ---------------------------------------------------------------------------
@@ -1040,7 +1104,7 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
                              std::to_string((uint64_t)per_sample * nsamp) + " bytes) exceeds the device-memory budget");
     if (!ppm) WR_CUDA(ctx, st.eye.reserve(64ull * nrec * nsamp));
     WR_CUDA(ctx, st.light.reserve(64ull * nrec * nsamp));
-    WR_CUDA(ctx, st.counts.reserve(4ull * nsamp + 40));
+    WR_CUDA(ctx, st.counts.reserve(4ull * nsamp + 48));
     if (!ppm) {
         WR_CUDA(ctx, st.cand.reserve(8ull * nrec * (nrec + 1) * nsamp));
         WR_CUDA(ctx, st.vis.reserve(8ull * nrec * (nrec + 1) * nsamp));
@@ -1086,7 +1150,7 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
         WR_CUDA(ctx, st.tput.reserve(16ull * nrec * nsamp));
         P.tput = st.tput.as<float4>();
     }
-    // the four list counters live after the per-sample counts (8-byte aligned)
+    // the five counters live after the per-sample counts (8-byte aligned)
     P.ncand = reinterpret_cast<unsigned long long*>(st.counts.as<char>() + ((4ull * nsamp + 7) & ~7ull));
     const int block = 128;
     const size_t smem = (size_t)RP.stack_cap * block * sizeof(uint32_t);
@@ -1101,15 +1165,18 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
     const int connect_grid = std::max(1, per_sm) * std::max(1, ctx->num_sms);
     const int visible_grid = std::max(1, per_sm_v) * std::max(1, ctx->num_sms);
     const int stride_grid = std::max(1, ctx->num_sms) * 8;
+    int per_sm_s = 0;
+    WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_s, k_bpt_subpaths, block, smem));
+    const int subpath_grid = std::max(1, per_sm_s) * std::max(1, ctx->num_sms);
     for (uint32_t done = 0; done < spp; done += per_batch) {
         const uint32_t b = std::min(per_batch, spp - done);
         P.s0 = spp_offset + done;
         P.nsamp = npix * b;
         P.eye.nsamp = P.light.nsamp = P.nsamp;
         const int grid = (int)((P.nsamp + block - 1) / block);
-        k_bpt_subpaths<<<dim3(grid, ppm ? 1 : 2), block, smem, stream>>>(S, P, err);
+        WR_CUDA(ctx, cudaMemsetAsync(P.ncand, 0, 5 * sizeof(unsigned long long), stream));
+        k_bpt_subpaths<<<subpath_grid, block, smem, stream>>>(S, P, err);
         WR_CUDA(ctx, cudaGetLastError());
-        WR_CUDA(ctx, cudaMemsetAsync(P.ncand, 0, 4 * sizeof(unsigned long long), stream));
         if (grid_on) {  // the batch's hash grids: one per slot (iteration)
             st.h_radii.resize(b);
             for (uint32_t k = 0; k < b; k++) st.h_radii[k] = vcm_radius(base_radius, P.s0 + k);
