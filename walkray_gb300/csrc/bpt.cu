@@ -783,8 +783,26 @@ __global__ void __launch_bounds__(128) k_vcm_points(RenderScene S, BptParams P) 
         }
         warp_append(ok, item, P.pts, P.ncand + 2);
     }
-    if (any) {
-        int* k = P.bbox + 6 * (sid / P.npix);
+    // the box: every lane's box includes the origin, so a lane without points
+    // is neutral; a warp within one slot reduces first and adds once
+    constexpr unsigned FULL = 0xffffffffu;
+    const uint32_t slot = sid / P.npix;
+    const bool uniform = __all_sync(FULL, __shfl_sync(FULL, slot, 0) == slot && sid < P.nsamp);
+    if (uniform) {
+        const int k0 = __reduce_min_sync(FULL, fkey(lo.x)), k1 = __reduce_min_sync(FULL, fkey(lo.y)),
+                  k2 = __reduce_min_sync(FULL, fkey(lo.z)), k3 = __reduce_max_sync(FULL, fkey(hi.x)),
+                  k4 = __reduce_max_sync(FULL, fkey(hi.y)), k5 = __reduce_max_sync(FULL, fkey(hi.z));
+        if (__ballot_sync(FULL, any) && (threadIdx.x & 31u) == 0) {
+            int* k = P.bbox + 6 * slot;
+            atomicMin(k + 0, k0);
+            atomicMin(k + 1, k1);
+            atomicMin(k + 2, k2);
+            atomicMax(k + 3, k3);
+            atomicMax(k + 4, k4);
+            atomicMax(k + 5, k5);
+        }
+    } else if (any) {
+        int* k = P.bbox + 6 * slot;
         atomicMin(k + 0, fkey(lo.x));
         atomicMin(k + 1, fkey(lo.y));
         atomicMin(k + 2, fkey(lo.z));
