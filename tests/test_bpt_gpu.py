@@ -113,3 +113,16 @@ def test_scratch_beyond_the_memory_budget_is_refused():
         assert e.value.code == 2 and "budget" in str(e.value)  # WR_ERR_OUT_OF_MEMORY
     assert small.render(sid, 1, 8, mode="megakernel").mean() > 0
     small.close()
+
+
+@pytest.mark.parametrize("name,depth", [("cornell", 1), ("cornell", 3), ("mixed_l2", 16), ("fog", 24)])
+def test_bidirectional_paired_at_other_depths(ctx, name, depth):
+    """Sub-path lengths from 3 to 26 records: the same connections on both sides."""
+    s = make_golden.golden_scenes()[name]
+    h, w = s.camera.height, s.camera.width
+    sid = ctx.upload(s)
+    o = wr_oracle.SceneOracle(s).render_bpt(8, depth, seed=61)[0].reshape(h, w, 3) / 8
+    g = ctx.render(sid, 8, depth, seed=61, mode="bidirectional").astype(np.float64)
+    assert abs(g.mean() / o.mean() - 1) < 2e-3, (g.mean(), o.mean())
+    assert np.isclose(g, o, rtol=1e-3, atol=1e-5).mean() > 0.99
+    ctx.release(sid)

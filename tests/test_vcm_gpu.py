@@ -102,3 +102,15 @@ def test_vcm_merging_changes_the_image_and_radius_zero_is_default(ctx):
     with pytest.raises(L.WRError):
         ctx.render(sid, 1, 8, mode="vcm", radius=float("nan"))
     ctx.release(sid)
+
+
+@pytest.mark.parametrize("name,depth", [("cornell", 2), ("mixed_l2", 12)])
+def test_vcm_paired_at_other_depths(ctx, name, depth):
+    s = rotated(make_golden.golden_scenes()[name])
+    h, w = s.camera.height, s.camera.width
+    sid = ctx.upload(s)
+    o = wr_oracle.SceneOracle(s).render_vcm(8, depth, seed=62, radius=0.03)[0].reshape(h, w, 3) / 8
+    g = ctx.render(sid, 8, depth, seed=62, mode="vcm", radius=0.03).astype(np.float64)
+    assert abs(g.mean() / o.mean() - 1) < 2e-3, (g.mean(), o.mean())
+    assert np.isclose(g, o, rtol=1e-3, atol=1e-5).mean() > 0.99
+    ctx.release(sid)
