@@ -205,9 +205,11 @@ int wr_trace_closest_device(wr_ctx* ctx, wr_scene_id scene, const float* d_rays,
 #define WR_MODE_PHOTON_MAP 4u    /* PhotonMap (photonMap.cpp:20-625) as the reference builds it (progressive:
                                     radius r_s of VCM's schedule, no ray marching): light sub-paths as
                                     photons in the reference's hash grid, each eye path's first diffuse
-                                    record estimates the photon density (kernel 3(1-d^2/r^2)^2/pi);
-                                    wr_render_desc.radius is the base radius (PhotonMap::setRadius; 0 =
-                                    0.01); surfaces without anisotropic glossy objects, max_path_len <= 30 */
+                                    record estimates the photon density (kernel 3(1-d^2/r^2)^2/pi; the
+                                    Gaussian-weighted elliptic estimate behind an anisotropic glossy
+                                    reflection, photonMap.cpp:383-652); wr_render_desc.radius is the base
+                                    radius (PhotonMap::setRadius; 0 = 0.01); surfaces only (no media),
+                                    max_path_len <= 30 */
 
 #define WR_RENDER_NEE 1u      /* PathTracer's next-event-estimation branch (pathTracer.cpp:39-66) */
 /* Rendering traverses front to back and skips a box whose entry distance is

@@ -22,7 +22,9 @@
  *            with `vcm radius` VCMTracer::renderPixels (vcmTracer.cpp:6-92)
  *            with VCMTracer::setRadius(radius); with `ppm radius`
  *            PhotonMap::renderPixels (photonMap.cpp:20-148), setRadius(radius).  out: W*H*3 f32
- *            (row 0 = top, p = y*W + x).  Elapsed seconds on stderr.
+ *            (row 0 = top, p = y*W + x).  Elapsed seconds on stderr.  With
+ *            WR_REF_ELLIPSE_LOG=path a `ppm` render also writes the records of
+ *            its anisotropic queries' ellipses there (see wrEllipseLog).
  */
 #include "wr_ref_prelude.h"
 
@@ -89,6 +91,27 @@ struct KDTreeTwin {  // KDTree's members in declaration order (kdtree.h:20-40)
 };
 
 static vec3f v3(const float* p) { return vec3f(p[0], p[1], p[2]); }
+
+// The record hook of the anisotropic photon query (ref_shim/wr_ref_ellipse_log.h):
+// with WR_REF_ELLIPSE_LOG=path, every call appends 22 f32 {kind, in_dir[3],
+// aniso normal[3], reflected dir[3], hit normal[3], Nu, Nv, ratio, mX[3], mY[3]}.
+void wrEllipseLog(int kind, float ix, float iy, float iz, float nx, float ny, float nz, float sx, float sy, float sz,
+                  float hx, float hy, float hz, float nu, float nv, float ratio, float ex, float ey, float ez,
+                  float fx, float fy, float fz) {
+    static FILE* out = NULL;
+    static bool opened = false;
+    const float rec[22] = {(float)kind, ix, iy, iz, nx, ny, nz, sx, sy, sz, hx, hy, hz,
+                           nu, nv, ratio, ex, ey, ez, fx, fy, fz};
+#pragma omp critical(wr_ellipse_log)
+    {
+        if (!opened) {
+            opened = true;
+            const char* path = getenv("WR_REF_ELLIPSE_LOG");
+            out = path ? fopen(path, "wb") : NULL;
+        }
+        if (out) fwrite(rec, sizeof rec, 1, out);
+    }
+}
 
 static void build_scene(RenderEngine& eng, const wrs_scene& ws, Rng* rng) {
     Scene& sc = eng.scene;

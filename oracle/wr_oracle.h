@@ -98,10 +98,16 @@ float wro_vcm_radius(float base, uint32_t s);
 /* ---- progressive photon mapping ----------------------------------------- */
 /* PhotonMap::renderPixels (photonMap.cpp:20-148, PPM) for samples [s0, s1)
  * with base radius r0 (PhotonMap::setRadius); sums as wro_render_bpt.
- * Returns 1 (nothing rendered) for scenes with participating media or
- * anisotropic glossy objects. */
+ * Returns 1 (nothing rendered) for scenes with participating media. */
 int wro_render_ppm(const wro_scene* s, uint32_t max_path_len, uint64_t seed, float r0, uint32_t s0, uint32_t s1,
                    double* sum, double* sumsq, int nthreads, uint64_t* rays_traced);
+/* the elliptic query's set-up (photonMap.cpp:384-613) at a diffuse point of
+ * normal hn reached along sp from an anisotropic surface of normal n and
+ * exponents Nu, Nv entered along in_d: 0 with the axis ratio and the ellipse
+ * frame's ex (long axis) and ey; 1 or 2 for the reference's two fallbacks to
+ * the round kernel (sharp ellipse; degenerate projection or Xi_s/Xi_f <= 1) */
+int wro_ppm_ellipse(const float in_d[3], const float n[3], const float sp[3], const float hn[3], float nu, float nv,
+                    float* ratio, float ex[3], float ey[3]);
 
 #ifdef __cplusplus
 }

@@ -20,6 +20,19 @@ NEE = 1
 DELTA = 4  # heterogeneous media by delta / ratio tracking (the GPU's scheme)
 
 
+def ppm_ellipse(in_d, n, sp, hn, nu: float, nv: float):
+    """The photon query's ellipse set-up (wro_ppm_ellipse): (kind, ratio,
+    ex, ey); kind 0 elliptic, 1 and 2 the two fallbacks to the round kernel."""
+    lib = load()
+    fp = C.POINTER(C.c_float)
+    vs = [np.ascontiguousarray(v, np.float32) for v in (in_d, n, sp, hn)]
+    ratio = C.c_float()
+    ex, ey = np.zeros(3, np.float32), np.zeros(3, np.float32)
+    k = lib.wro_ppm_ellipse(*[v.ctypes.data_as(fp) for v in vs], nu, nv, C.byref(ratio), ex.ctypes.data_as(fp),
+                            ey.ctypes.data_as(fp))
+    return k, np.float32(ratio.value), ex, ey
+
+
 def build() -> None:
     subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
 
@@ -57,6 +70,9 @@ def load():
         lib.wro_render_ppm.argtypes = lib.wro_render_vcm.argtypes
         lib.wro_vcm_radius.restype = C.c_float
         lib.wro_vcm_radius.argtypes = [C.c_float, C.c_uint32]
+        fp = C.POINTER(C.c_float)
+        lib.wro_ppm_ellipse.restype = C.c_int
+        lib.wro_ppm_ellipse.argtypes = [fp, fp, fp, fp, C.c_float, C.c_float, fp, fp, fp]
         _lib = lib
     return _lib
 
@@ -185,5 +201,5 @@ class SceneOracle:
         rc = self.lib.wro_render_ppm(self.h, max_path_len, seed, radius, s0, s0 + spp, _p(s), _p(s2), threads,
                                      C.byref(rays))
         if rc:
-            raise ValueError("the photon-mapping restatement covers surfaces without anisotropic objects only")
+            raise ValueError("the photon-mapping restatement covers surfaces only (no participating media)")
         return s, s2, rays.value

@@ -29,10 +29,14 @@ from the reference sources) on small seeded scenes and stores its answers:
                       8 reference renders of 64 spp each
 
   render_ppm_*.npz    PhotonMap::renderPixels (base radius 0.02) on the
-                      Cornell, mirror, thin-lens and mixed-material scenes, 8
-                      reference renders of 64 spp each
+                      Cornell, mirror, thin-lens, mixed-material and
+                      anisotropic-floor scenes, 8 reference renders of 64 spp
+                      each
+  ppm_ellipse_ref.npz the reference's ellipse set-ups of the anisotropic
+                      photon query (inputs and results), recorded in its own
+                      PhotonMap renders of the anisotropic-floor scene
 
-Usage: python tests/golden/make_golden.py [bpt|vcm|ppm [scene ...]]   (needs
+Usage: python tests/golden/make_golden.py [bpt|vcm|ppm|ellipse [scene ...]]   (needs
 the reference tree on this machine; `bpt` / `vcm` / `ppm` remake only those
 renders, of the scenes named after it if any; the fixtures it writes are what
 the tests read elsewhere)
@@ -67,6 +71,7 @@ def golden_scenes():
         "mirror": S.cornell_mirror(32, 32),
         "dof": S.cornell_dof(32, 32, lens_radius=0.2),
         "fog": S.cornell_fog(32, 32, ior=1.2),
+        "aniso": S.cornell_aniso(32, 32),
     }
 
 
@@ -246,7 +251,7 @@ def vcm_fixtures(td, names=VCM_SCENES):
         render_set(sc[name], p, td, f"render_vcm_{name}.npz", extra=("vcm", str(VCM_RADIUS)), spp=64)
 
 
-PPM_SCENES = ("cornell", "mirror", "dof", "mixed_l2")
+PPM_SCENES = ("cornell", "mirror", "dof", "mixed_l2", "aniso")
 PPM_RADIUS = 0.02
 
 
@@ -259,10 +264,39 @@ def ppm_fixtures(td, names=PPM_SCENES):
         render_set(sc[name], p, td, f"render_ppm_{name}.npz", extra=("ppm", str(PPM_RADIUS)), spp=64)
 
 
+ELLIPSE_LOBES = ((10.0, 100.0), (100.0, 10.0), (50.0, 50.0), (5.0, 500.0), (2.0, 20.0))
+
+
+def ellipse_fixture(td, names=None):
+    """The reference's own ellipse set-ups of the anisotropic photon query
+    (photonMap.cpp:384-652), recorded by the harness (WR_REF_ELLIPSE_LOG) in
+    one 16-spp PhotonMap render of the anisotropic-floor scene per (Nu, Nv) of
+    ELLIPSE_LOBES: every elliptic and degenerate-projection record, at most
+    400 sharp-ellipse fallbacks per lobe.  ppm_ellipse_ref.npz: kind (i32;
+    0 ellipse, 1 sharp, 2 projection), inputs (n, 14) f32 {in_dir, aniso
+    normal, reflected dir, hit normal, Nu, Nv}, ratio (n) f32, ex, ey (n, 3)
+    f32 (the ellipse frame's mX, mY)."""
+    p = os.path.join(td, "s.wrs")
+    recs = []
+    for nu, nv in ELLIPSE_LOBES:
+        S.cornell_aniso(32, 32, nu=nu, nv=nv).save(p)
+        log = os.path.join(td, "ellipse.bin")
+        env = dict(os.environ, OMP_NUM_THREADS="1", WR_REF_WORKDIR=td, WR_REF_ELLIPSE_LOG=log)
+        subprocess.run([REF, "render", p, "16", "8", "1", os.path.join(td, "o.bin"), "ppm", str(PPM_RADIUS)],
+                       env=env, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        r = np.fromfile(log, np.float32).reshape(-1, 22)
+        sharp = np.flatnonzero(r[:, 0] == 1)[:400]
+        keep = np.sort(np.concatenate([np.flatnonzero(r[:, 0] != 1), sharp]))
+        recs.append(r[keep])
+    r = np.concatenate(recs)
+    np.savez_compressed(os.path.join(HERE, "ppm_ellipse_ref.npz"), kind=r[:, 0].astype(np.int32),
+                        inputs=r[:, 1:15], ratio=r[:, 15], ex=r[:, 16:19], ey=r[:, 19:22])
+
+
 def main():
     if not os.path.exists(REF):
         sys.exit("build the reference harness first: make -C oracle ref")
-    only = {"bpt": bpt_fixtures, "vcm": vcm_fixtures, "ppm": ppm_fixtures}
+    only = {"bpt": bpt_fixtures, "vcm": vcm_fixtures, "ppm": ppm_fixtures, "ellipse": ellipse_fixture}
     if len(sys.argv) >= 2 and sys.argv[1] in only:  # only those renders (of the scenes named after it)
         with tempfile.TemporaryDirectory() as td:
             if len(sys.argv) > 2:
@@ -329,6 +363,7 @@ def main():
         bpt_fixtures(td)
         vcm_fixtures(td)
         ppm_fixtures(td)
+        ellipse_fixture(td)
     print("golden fixtures written to", HERE)
 
 

@@ -205,10 +205,11 @@ def test_oracle_vcm_radius_schedule(built):
     assert lib.wro_vcm_radius(1e-9, 5) == np.float32(1e-5)
 
 
-@pytest.mark.parametrize("name", ["cornell", "mirror", "dof", "mixed_l2"])
+@pytest.mark.parametrize("name", ["cornell", "mirror", "dof", "mixed_l2", "aniso"])
 def test_oracle_photon_map_matches_reference_statistically(built, name):
     """PhotonMap (photonMap.cpp:20-625, progressive, base radius 0.02): the
-    restated photon density estimation vs 8 reference renders of 64 spp."""
+    restated photon density estimation vs 8 reference renders of 64 spp
+    ("aniso": the elliptic estimate behind an anisotropic floor)."""
     g = np.load(os.path.join(GOLDEN, f"render_ppm_{name}.npz"))
     ref = g["images"].astype(np.float64)
     s = make_golden.golden_scenes()[name]
@@ -223,7 +224,24 @@ def test_oracle_photon_map_matches_reference_statistically(built, name):
     assert abs(port.mean() / ref.mean() - 1) < 0.02
 
 
-def test_oracle_photon_map_refuses_media_and_anisotropic(built):
+def test_oracle_ellipse_matches_reference_records(built):
+    """The anisotropic photon query's ellipse set-up (photonMap.cpp:384-613)
+    against the reference's own, recorded in its PhotonMap renders of the
+    anisotropic-floor scene for five (Nu, Nv) lobes: the same branch (ellipse,
+    sharp-ellipse or projection fallback) everywhere, and bit-identical axis
+    ratio and frame (both built with the same C library's acosf, sin, cos,
+    exp and sqrt)."""
+    g = np.load(os.path.join(GOLDEN, "ppm_ellipse_ref.npz"))
+    kind, x = g["kind"], g["inputs"]
+    assert set(np.unique(kind)) == {0, 1, 2}
+    for i in range(len(kind)):
+        k, ratio, ex, ey = wr_oracle.ppm_ellipse(x[i, 0:3], x[i, 3:6], x[i, 6:9], x[i, 9:12], x[i, 12], x[i, 13])
+        assert k == kind[i], i
+        if k == 0:
+            assert ratio == g["ratio"][i] and np.array_equal(ex, g["ex"][i]) and np.array_equal(ey, g["ey"][i]), i
+
+
+def test_oracle_photon_map_refuses_media(built):
     for name in ("media_small",):
         with pytest.raises(ValueError):
             wr_oracle.SceneOracle(make_golden.golden_scenes()[name]).render_ppm(1, 8, seed=1)

@@ -20,9 +20,12 @@ pytestmark = pytest.mark.gpu
 R = make_golden.PPM_RADIUS
 
 
-@pytest.mark.parametrize("name", ["cornell", "mirror", "dof", "mixed_l2"])
+@pytest.mark.parametrize("name", ["cornell", "mirror", "dof", "mixed_l2", "aniso"])
 def test_photon_map_paired_with_oracle(ctx, name):
-    s = rotated(make_golden.golden_scenes()[name])
+    """The anisotropic-floor scene (already turned off the axes) takes the
+    elliptic estimate in about a quarter of its diffuse queries."""
+    s = make_golden.golden_scenes()[name]
+    s = s if name == "aniso" else rotated(s)
     h, w = s.camera.height, s.camera.width
     sid = ctx.upload(s)
     orc = wr_oracle.SceneOracle(s)
@@ -47,17 +50,9 @@ def test_photon_map_matches_reference_renders(ctx, name):
     ctx.release(sid)
 
 
-def test_photon_map_refuses_media_and_anisotropic(ctx):
+def test_photon_map_refuses_media(ctx):
     sid = ctx.upload(make_golden.golden_scenes()["media_small"])
-    with pytest.raises(L.WRError):
-        ctx.render(sid, 1, 8, mode="photon_map")
-    ctx.release(sid)
-    s = make_golden.golden_scenes()["cornell"]
-    from walkray_gb300 import scenes as S
-    s.objects[0].type = S.MAT_ANISO
-    s.objects[0].params = {"rs": (0.3, 0.3, 0.3), "rd": (0.2, 0.2, 0.2), "nu": 10.0, "nv": 100.0}
-    sid = ctx.upload(s)
     with pytest.raises(L.WRError) as e:
         ctx.render(sid, 1, 8, mode="photon_map")
-    assert "anisotropic" in str(e.value)
+    assert "media" in str(e.value)
     ctx.release(sid)

@@ -928,8 +928,8 @@ __global__ void __launch_bounds__(128) k_vcm_eval(RenderScene S, BptParams P) {
 
 // ---------------------------------------------------------------------------
 // progressive photon mapping (PhotonMap::renderPixels, photonMap.cpp:20-148,
-// as built: PPM on, no ray marching, no anisotropic ellipse kernel): the
-// light points of VCM are the photons, in the same hash grid
+// as built: PPM on, no ray marching, ANI_PM off): the light points of VCM are
+// the photons, in the same hash grid
 // ---------------------------------------------------------------------------
 constexpr uint32_t PPM_MERGE_LEN = 10;  // photonMap.cpp:9
 
@@ -970,6 +970,184 @@ __device__ __forceinline__ f3 ppm_photon(const RenderScene& S, const BptParams& 
     return color * (kernel / ((float)P.npix * radius * radius));
 }
 
+// ---- the anisotropic (elliptic) photon query, photonMap.cpp:384-652 --------
+// Eigen-decomposition of the symmetric [[a, b], [b, c]] by LAPACK's published
+// DLAEV2 algorithm: rt1 the eigenvalue of larger magnitude, rt2 the other,
+// (cs1, sn1) the unit eigenvector of rt1.
+__device__ void eig2_sym(double a, double b, double c, double& rt1, double& rt2, double& cs1, double& sn1) {
+    const double sm = a + c, df = a - c, adf = fabs(df), tb = b + b, ab = fabs(tb);
+    const double acmx = fabs(a) > fabs(c) ? a : c, acmn = fabs(a) > fabs(c) ? c : a;
+    double rt;
+    if (adf > ab) {
+        const double q = ab / adf;
+        rt = adf * sqrt(q * q + 1.);
+    } else if (adf < ab) {
+        const double q = adf / ab;
+        rt = ab * sqrt(q * q + 1.);
+    } else {
+        rt = ab * sqrt(2.);
+    }
+    int sgn1;
+    if (sm < 0.) {
+        rt1 = (sm - rt) * .5;
+        sgn1 = -1;
+        rt2 = acmx / rt1 * acmn - b / rt1 * b;
+    } else if (sm > 0.) {
+        rt1 = (sm + rt) * .5;
+        sgn1 = 1;
+        rt2 = acmx / rt1 * acmn - b / rt1 * b;
+    } else {
+        rt1 = rt * .5;
+        rt2 = rt * -.5;
+        sgn1 = 1;
+    }
+    const int sgn2 = df >= 0. ? 1 : -1;
+    const double cs = df >= 0. ? df + rt : df - rt;
+    if (fabs(cs) > ab) {
+        const double ct = -tb / cs;
+        sn1 = 1. / sqrt(ct * ct + 1.);
+        cs1 = ct * sn1;
+    } else if (ab == 0.) {
+        cs1 = 1.;
+        sn1 = 0.;
+    } else {
+        const double tn = -cs / tb;
+        cs1 = 1. / sqrt(tn * tn + 1.);
+        sn1 = tn * cs1;
+    }
+    if (sgn1 == sgn2) {
+        const double tn = cs1;
+        cs1 = -sn1;
+        sn1 = tn;
+    }
+}
+
+// derivatives of the anisotropic spherical Gaussian
+// cos(theta) exp(-sin^2(theta) (L cos^2(phi) + M sin^2(phi))) in theta and phi
+// (PhotonMap::ASG_dF_dTheta / ASG_dF_dPhi, photonMap.cpp:681-691)
+__device__ double asg_dtheta(double th, double ph, double L, double M) {
+    const double k = L * cos(ph) * cos(ph) + M * sin(ph) * sin(ph), st = sin(th);
+    return exp(-st * st * k) * st * (2 * cos(th) * cos(th) * (-k) - 1);
+}
+__device__ double asg_dphi(double th, double ph, double L, double M) {
+    const double k = L * cos(ph) * cos(ph) + M * sin(ph) * sin(ph), st = sin(th);
+    return exp(-st * st * k) * 2 * st * st * cos(th) * sin(ph) * cos(ph) * (L - M);
+}
+
+// The ellipse of the photon query at a diffuse point of normal hn reached
+// along sp from an anisotropic surface of normal N (exponents nu, nv) entered
+// along in_d (photonMap.cpp:384-613): the lobe's Hessian in the half-vector
+// frame and its eigenvectors (the warped frame), the fastest and slowest
+// directions of the warped Gaussian at sp with their steps for an error bound
+// of 0.002, projected along sp onto the hit plane.  0 with the long axis ex,
+// ey = hn x ex and the axis ratio; 1 (eigenvectors within |cs| or |sn| > 0.99)
+// or 2 (degenerate projection, Xi_s / Xi_f <= 1) where the reference falls
+// back to the round kernel.  Mixed float / double exactly as the reference's
+// vec3f and double expressions; out of line, so that its FP64 registers stay
+// out of the common path of k_ppm_eye.
+__device__ __noinline__ int ellipse_frame(f3 in_d, f3 N, f3 sp, f3 hn, float nu, float nv, f3& ex, f3& ey,
+                                          float& ratio) {
+    const double lam = (double)(nu / 2.f), miu = (double)(nv / 2.f);
+    const f3 O = -in_d;
+    const float on = dot(O, N);
+    const f3 I = normalize(N * (2.f * on) - O);
+    f3 BX, BY, BZ;
+    frame_from_n(N, BX, BY, BZ);
+    const f3 Xh = normalize(cross(O, N)), Yi = cross(I, Xh);
+    const double dxx = (double)dot(BZ, Xh), dyx = (double)dot(BX, Xh);
+    double HA = lam * (dxx * dxx) + miu * (dyx * dyx);
+    HA /= 4 * ((double)on * (double)on);
+    double HB = (miu - lam) * (dxx * dyx);
+    HB /= (double)(4.f * on);
+    double HD = miu * (dxx * dxx) + lam * (dyx * dyx);
+    HD /= 4;
+    double L1, M1, cs, sn;
+    eig2_sym(HA, HB, HD, L1, M1, cs, sn);
+    L1 = fabs(L1);
+    M1 = fabs(M1);
+    if (fabs(cs) > 0.99 || fabs(sn) > 0.99) return 1;
+    const f3 IX = Xh * (float)cs + Yi * (float)sn;
+    const f3 IY = Xh * (float)-sn + Yi * (float)cs;
+    const float a0 = dot(sp, IX), b0 = dot(sp, IY);
+    const float c2 = 1.f - a0 * a0 - b0 * b0;
+    const float c0 = sqrtf(c2 < 0.f ? 0.f : c2 > 1.f ? 1.f : c2);
+    // acos of a float argument is the C++ float overload (acosf)
+    const double theta = (double)acosf(c0 < -1.f ? -1.f : c0 > 1.f ? 1.f : c0), st = sin(theta);
+    const double ca = (double)a0 / st;
+    const double aphi = acos(ca < -1 ? -1.0 : ca > 1 ? 1.0 : ca);
+    const double phi = b0 > 0.f ? aphi : 2 * PI_D - aphi;
+    const f3 SY = normalize(cross(I, sp)), SX = cross(SY, sp);
+    const double dl = 0.0001;
+    const double fT = asg_dtheta(theta, phi, L1, M1), fP = asg_dphi(theta, phi, L1, M1);
+    const double fTT = (asg_dtheta(theta + dl, phi, L1, M1) - asg_dtheta(theta - dl, phi, L1, M1)) / (2 * dl);
+    const double fPP = (asg_dphi(theta, phi + dl, L1, M1) - asg_dphi(theta, phi - dl, L1, M1)) / (2 * dl);
+    const double fTP = (asg_dtheta(theta, phi + dl, L1, M1) - asg_dtheta(theta, phi - dl, L1, M1)) / (2 * dl);
+    const f3 fastest = normalize(SX * (float)fT + SY * (float)(fP / st));
+    const f3 slowest = cross(sp, fastest);
+    const f3 ltp = normalize(mk((float)fT, (float)(fP / st), 0.f));
+    const double al1 = (double)acosf(fabsf(ltp.x)), al2 = PI_D / 2 - al1;
+    const double eb = 0.002;
+    const double lower = cos(theta) * exp(-st * st * (L1 * cos(phi) * cos(phi) + M1 * sin(phi) * sin(phi)));
+    const double xf = fabs(eb * lower / (fT * cos(al1) + fP * sin(al1) / st));
+    const double xs = sqrt(fabs(2 * eb * lower /
+                                (fTT * cos(al2) * cos(al2) + 2 * fTP * sin(al2) * cos(al2) / st +
+                                 fPP * sin(al2) * sin(al2) / (st * st))));
+    f3 HX, HY, HZ;
+    frame_from_n(hn, HX, HY, HZ);
+    if (fabs((double)dot(sp, I)) < EPS_D || fabs((double)dot(sp, hn)) < EPS_D || fabs(xs / xf) <= 1.0) return 2;
+    // A = [Zh; Xh] (I - D Np^T / D.Np) [fastest slowest]
+    const double dn = (double)dot(sp, HY);
+    const float D[3] = {sp.x, sp.y, sp.z}, Np[3] = {HY.x, HY.y, HY.z};
+    const double Jp[2][3] = {{HZ.x, HZ.y, HZ.z}, {HX.x, HX.y, HX.z}};
+    const double Je[3][2] = {{fastest.x, slowest.x}, {fastest.y, slowest.y}, {fastest.z, slowest.z}};
+    double mid[3][3], pj[2][3] = {{0, 0, 0}, {0, 0, 0}}, A[2][2] = {{0, 0}, {0, 0}};
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) mid[r][c] = (double)(r == c) - (double)(D[r] * Np[c]) / dn;
+#pragma unroll
+    for (int r = 0; r < 2; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+#pragma unroll
+            for (int k = 0; k < 3; k++) pj[r][c] += Jp[r][k] * mid[k][c];
+#pragma unroll
+    for (int r = 0; r < 2; r++)
+#pragma unroll
+        for (int c = 0; c < 2; c++)
+#pragma unroll
+            for (int k = 0; k < 3; k++) A[r][c] += pj[r][k] * Je[k][c];
+    const f3 fast = (HZ * (float)A[0][0] + HX * (float)A[1][0]) * (float)xf;
+    const f3 slow = (HZ * (float)A[0][1] + HX * (float)A[1][1]) * (float)xs;
+    const float lr = length(slow) / length(fast);
+    ratio = (float)((double)lr > 1.0 ? (double)lr : 1.0);
+    ex = normalize(slow);
+    ey = cross(hn, ex);
+    return 0;
+}
+
+// Query::EllipseProcess (photonMap.cpp:262-298): one photon's Gaussian-kernel
+// estimate in the ellipse frame (axes radius * ratio and radius), its weight
+// summed into sumw and counted
+__device__ __forceinline__ f3 ppm_photon_ellipse(const RenderScene& S, const BptParams& P, uint32_t k, const PRay& out,
+                                                 float radius, f3 ex, f3 ey, float ratio, double& sumw, int& count) {
+    const uint2 pt = P.pts[k];
+    const float4 tp = __ldg(&P.tput[k]);
+    const PRay prevl = P.light.get(pt.x, (int)pt.y - 1);
+    const f3 pos = xyz(__ldg(P.light.at(pt.x, (int)pt.y)));
+    const f3 color = vmul(mk(tp.x, tp.y, tp.z), eval_bsdf(S, prevl.d, out));
+    if (!legal(color)) return mk(0, 0, 0);
+    const f3 hp = pos - out.o;
+    const float X = dot(hp, ex), Y = dot(hp, ey);
+    const float A = radius * ratio, B = radius;
+    const float md = X * X / (A * A) + Y * Y / (B * B);
+    const float w = (float)(exp(-(double)md / 2) / (2 * PI_D));
+    sumw += w;
+    count++;
+    const float conv = (float)(1.0 / ((double)P.npix * PI_D * radius * radius));
+    return (color * w) * conv;
+}
+
 // One thread per sample: the eye path of PhotonMap::sampleMergePath (at most
 // 10 bounces) up to its first emitter (its radiance) or diffuse record (the
 // photon density there, throughputByDensityEstimation), times the camera
@@ -995,6 +1173,7 @@ __global__ void __launch_bounds__(128) k_ppm_eye(RenderScene S, BptParams P, uns
     InsideStack st;
     st.reset(prev.inside);
     f3 surf = mk(0, 0, 0);
+    f3 pdir = mk(0, 0, 0);  // direction of the record before `prev` (eyeMergePath[i-2])
     const GridView G = grid_view(P, slot);
     const unsigned long long npts = P.ncand[2];
     for (uint32_t depth = 0;; depth++) {
@@ -1010,6 +1189,14 @@ __global__ void __launch_bounds__(128) k_ppm_eye(RenderScene S, BptParams P, uns
         if (next.contact >= 0 && obj_type(S, next.contact) == WR_MAT_DIFFUSE) {  // nonSpecular()
             PRay out = next;
             out.d = -prev.d;
+            // reached through an anisotropic record: the elliptic estimate
+            f3 ex = mk(0, 0, 0), ey = mk(0, 0, 0);
+            float ratio = 1.f;
+            const bool ell = prev.contact >= 0 && obj_type(S, prev.contact) == WR_MAT_ANISO &&
+                             ellipse_frame(pdir, prev.cnorm, prev.d, next.cnorm, __ldg(&S.objs[prev.contact].nu),
+                                           __ldg(&S.objs[prev.contact].nv), ex, ey, ratio) == 0;
+            double sumw = 0.0;
+            int count = 0;
             const f3 q = next.o, dmin = q - G.bmin, dmax = G.bmax - q;
             if (!(dmin.x < 0.f || dmin.y < 0.f || dmin.z < 0.f || dmax.x < 0.f || dmax.y < 0.f || dmax.z < 0.f)) {
                 const f3 cp = mk(G.inv_cell * dmin.x, G.inv_cell * dmin.y, G.inv_cell * dmin.z);
@@ -1027,9 +1214,15 @@ __global__ void __launch_bounds__(128) k_ppm_eye(RenderScene S, BptParams P, uns
                         const uint2 pt = P.pts[k];
                         const float dist = length(q - xyz(__ldg(P.light.at(pt.x, (int)pt.y))));
                         if (!(dist * dist <= rr)) continue;
-                        surf = surf + ppm_photon(S, P, (uint32_t)k, out, G.radius);
+                        surf = surf + (ell ? ppm_photon_ellipse(S, P, (uint32_t)k, out, G.radius, ex, ey, ratio,
+                                                                sumw, count)
+                                           : ppm_photon(S, P, (uint32_t)k, out, G.radius));
                     }
                 }
+            }
+            if (ell) {  // Query::weightScale (photonMap.cpp:300-302): vec3f /= float
+                const float d = (float)(sumw / count);
+                if (d != 0.f) surf = mk(surf.x / d, surf.y / d, surf.z / d);
             }
             break;
         }
@@ -1039,6 +1232,7 @@ __global__ void __launch_bounds__(128) k_ppm_eye(RenderScene S, BptParams P, uns
         q.pf = P.pf;
         const Hit h = trace_closest<true, true>(S.tree, q, next.inside, next.contact, stack, stride, P.stack_cap, err);
         if (h.slot < 0) break;  // `next` was the last record and is checked above
+        pdir = prev.d;
         prev = next;
         set_hit(S, prev, h);
     }

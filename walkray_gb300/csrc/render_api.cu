@@ -18,7 +18,6 @@ struct RenderData {
     std::string unsupported;  // non-empty: this scene cannot be rendered (why)
     bool has_media = false;
     bool has_hetero = false;
-    bool has_aniso = false;
 };
 
 namespace {
@@ -201,7 +200,6 @@ int prepare_render(wr_ctx* ctx, SceneGPU* sc, RenderData** out) {
     for (const wr_object_desc& m : sc->objects) {
         if (m.type == WR_MAT_HOMOGENEOUS || m.type == WR_MAT_HETEROGENEOUS) rd->has_media = true;
         if (m.type == WR_MAT_HETEROGENEOUS) rd->has_hetero = true;
-        if (m.type == WR_MAT_ANISO) rd->has_aniso = true;
     }
     for (const wr_object_desc& m : sc->objects)
         if (m.type == WR_MAT_HETEROGENEOUS &&
@@ -256,10 +254,6 @@ int wr_render_device(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, fl
                                  "photon-mapping mode: participating media (volume photons) are not supported");
             if (desc->flags & WR_RENDER_NEE)
                 return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "bidirectional / VCM / photon-mapping mode has no NEE switch");
-            if (desc->mode == WR_MODE_PHOTON_MAP && rd->has_aniso)
-                return set_error(ctx, WR_ERR_UNSUPPORTED,
-                                 "photon-mapping mode: anisotropic glossy objects (the reference's ellipse kernel) are "
-                                 "not supported");
             const int kind = desc->mode == WR_MODE_VCM ? BIDIR_VCM
                            : desc->mode == WR_MODE_PHOTON_MAP ? BIDIR_PHOTON_MAP : BIDIR_BPT;
             return render_bidirectional(ctx, rd->S, P, desc->spp_offset, desc->spp, d_sum, d_sumsq, err, s, kind,

@@ -431,6 +431,38 @@ def cornell_dof(width=256, height=256, lens_radius=0.05, focal_dist=1.8) -> Scen
     return s
 
 
+def rotate_scene(s: Scene, y_deg: float, x_deg: float) -> Scene:
+    """Rotate every vertex and the camera by y_deg about y, then x_deg about x
+    (in place; rotation in float64, vertices rounded back to float32)."""
+    a, b = math.radians(y_deg), math.radians(x_deg)
+    ry = np.array([[math.cos(a), 0, math.sin(a)], [0, 1, 0], [-math.sin(a), 0, math.cos(a)]])
+    rx = np.array([[1, 0, 0], [0, math.cos(b), -math.sin(b)], [0, math.sin(b), math.cos(b)]])
+    m = rx @ ry
+    for o in s.objects:
+        o.verts = np.ascontiguousarray((o.verts.astype(np.float64) @ m.T).astype(np.float32))
+    c = s.camera
+    rot = lambda v: tuple(float(x) for x in m @ np.asarray(v, np.float64))
+    c.position, c.focus, c.up = rot(c.position), rot(c.focus), rot(c.up)
+    return s
+
+
+def cornell_aniso(width=256, height=256, nu=10.0, nv=100.0) -> Scene:
+    """The Cornell box with an anisotropic glossy floor (AnisotropicGlossyObject,
+    anisotropicGlossyObj.h; Ashikhmin-Shirley lobe with exponents Nu, Nv), the
+    whole scene turned 20 deg about y and 10 deg about x.  The camera sees the
+    walls and boxes reflected in the floor, where photon mapping takes its
+    elliptic estimate (photonMap.cpp:383-652); the turn sets the floor's
+    tangent frame (Frame::setFromN, frame.h:30-49) about 20 deg off the view,
+    since the estimate falls back to the round kernel when the ellipse is
+    within about 8 deg of that frame's axes (|cs| or |sn| > 0.99)."""
+    s = cornell(width, height)
+    s.name = "cornell_aniso"
+    floor = s.objects[0]
+    floor.type = MAT_ANISO
+    floor.params = {"rs": (0.6, 0.6, 0.6), "rd": (0.3, 0.3, 0.3), "nu": float(nu), "nv": float(nv)}
+    return rotate_scene(s, 20.0, 10.0)
+
+
 def icosphere_kd(level=8, seed=1, amplitude=0.05) -> Scene:
     """Closest-hit microbenchmark mesh: unit icosphere of 20*4^level
     triangles displaced radially by 4-octave value noise of the given
