@@ -194,14 +194,15 @@ int wr_trace_closest_device(wr_ctx* ctx, wr_scene_id scene, const float* d_rays,
 #define WR_MODE_WAVEFRONT 1u  /* generate / extend / shade queues, persistent kernels, graph bounce loop */
 #define WR_MODE_BIDIRECTIONAL 2u /* BidirectionalPathTracer (bidirPathTracer.cpp:10-313): eye and light
                                     sub-paths, all connections, balance-heuristic MIS, light tracing;
-                                    surfaces and homogeneous media (heterogeneous media:
-                                    WR_ERR_UNSUPPORTED), max_path_len <= 30 */
+                                    surfaces and both kinds of media (a heterogeneous medium with the
+                                    reference's own distance sampler and marched integrals),
+                                    max_path_len <= 30 */
 #define WR_MODE_VCM 3u           /* VCMTracer (vcmTracer.cpp:6-446): the bidirectional connections with
                                     VCM weights plus vertex merging of every eye vertex with the light
                                     points within the iteration's radius (the reference's hash grid);
                                     wr_render_desc.radius is the base radius (VCMTracer::setRadius;
-                                    0 = the reference's default 0.01); surfaces and homogeneous media,
-                                    max_path_len <= 30 */
+                                    0 = the reference's default 0.01); surfaces and both kinds of
+                                    media, max_path_len <= 30 */
 #define WR_MODE_PHOTON_MAP 4u    /* PhotonMap (photonMap.cpp:20-625) as the reference builds it (progressive:
                                     radius r_s of VCM's schedule, no ray marching): light sub-paths as
                                     photons in the reference's hash grid, each eye path's first diffuse

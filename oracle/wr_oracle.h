@@ -78,8 +78,7 @@ void wro_render(const wro_scene* s, uint32_t max_path_len, uint64_t seed, uint32
  * samples [s0, s1) of every pixel: eye and light sub-paths, all their
  * connections with balance-heuristic MIS weights and light-tracing splats;
  * each sample's image after isLegalColor and fixVignetting is added to sum
- * (and its square to sumsq).  Returns 1 (nothing rendered) for scenes with a
- * heterogeneous medium, which this restatement does not cover. */
+ * (and its square to sumsq).  Surfaces and both kinds of media; returns 0. */
 int wro_render_bpt(const wro_scene* s, uint32_t max_path_len, uint64_t seed, uint32_t s0, uint32_t s1, double* sum,
                    double* sumsq, int nthreads, uint64_t* rays_traced);
 int wro_scene_has_media(const wro_scene* s);
@@ -88,8 +87,7 @@ int wro_scene_has_hetero(const wro_scene* s);
 /* ---- vertex connection and merging -------------------------------------- */
 /* VCMTracer::renderPixels (vcmTracer.cpp:6-92) for samples [s0, s1) with base
  * merge radius r0 (VCMTracer::setRadius): connections with VCM weights and
- * merges through the reference's hash grid; sums as wro_render_bpt.  Returns
- * 1 (nothing rendered) for scenes with a heterogeneous medium. */
+ * merges through the reference's hash grid; sums as wro_render_bpt; returns 0. */
 int wro_render_vcm(const wro_scene* s, uint32_t max_path_len, uint64_t seed, float r0, uint32_t s0, uint32_t s1,
                    double* sum, double* sumsq, int nthreads, uint64_t* rays_traced);
 /* the merge radius of iteration s (vcmTracer.cpp:27) */

@@ -171,7 +171,7 @@ class SceneOracle:
         rc = self.lib.wro_render_bpt(self.h, max_path_len, seed, s0, s0 + spp, _p(s), _p(s2), threads,
                                      C.byref(rays))
         if rc:
-            raise ValueError("the bidirectional restatement does not cover heterogeneous media")
+            raise RuntimeError("wro_render_bpt failed")
         return s, s2, rays.value
 
     def render_vcm(self, spp: int, max_path_len: int, seed: int, radius: float = 0.01, s0: int = 0,
@@ -186,7 +186,7 @@ class SceneOracle:
         rc = self.lib.wro_render_vcm(self.h, max_path_len, seed, radius, s0, s0 + spp, _p(s), _p(s2), threads,
                                      C.byref(rays))
         if rc:
-            raise ValueError("the VCM restatement does not cover heterogeneous media")
+            raise RuntimeError("wro_render_vcm failed")
         return s, s2, rays.value
 
     def render_ppm(self, spp: int, max_path_len: int, seed: int, radius: float = 0.01, s0: int = 0,

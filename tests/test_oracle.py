@@ -8,7 +8,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN
+from conftest import GOLDEN, means_agree
 import make_golden
 import wr_oracle
 from walkray_gb300 import scenes as S
@@ -153,11 +153,12 @@ def test_oracle_thin_lens_matches_reference_statistically(built):
     assert np.abs(zp).max() > 4.5, np.abs(zp).max()
 
 
-@pytest.mark.parametrize("name", ["cornell", "mirror", "dof", "mixed_l2", "fog"])
+@pytest.mark.parametrize("name", make_golden.BPT_SCENES)
 def test_oracle_bidirectional_matches_reference_statistically(built, name):
     """BidirectionalPathTracer (bidirPathTracer.cpp:10-313): the restated
     connections, MIS weights and light-tracing splats vs 8 reference renders
-    of 64 spp.  Per-pixel z on 4x4 blocks, mean within 1.5 %."""
+    of 64 spp.  Per-pixel z on 4x4 blocks, mean within 1.5 % (or 4 standard
+    errors: the heterogeneous medium's estimate is noisier than that)."""
     g = np.load(os.path.join(GOLDEN, f"render_bpt_{name}.npz"))
     ref = g["images"].astype(np.float64)
     s = make_golden.golden_scenes()[name]
@@ -168,16 +169,10 @@ def test_oracle_bidirectional_matches_reference_statistically(built, name):
     br, bp = blk(ref), blk(port)
     z = (br.mean(0) - bp.mean(0)) / np.sqrt(br.var(0, ddof=1) / 8 + bp.var(0, ddof=1) / 8 + 1e-12)
     assert np.abs(z).max() < 4.8, np.abs(z).max()
-    assert abs(port.mean() / ref.mean() - 1) < 0.015
+    assert means_agree(port, ref, 0.015), (port.mean(), ref.mean())
 
 
-def test_oracle_bidirectional_refuses_media(built):
-    orc = wr_oracle.SceneOracle(make_golden.golden_scenes()["media_small"])
-    with pytest.raises(ValueError):
-        orc.render_bpt(1, 8, seed=1)
-
-
-@pytest.mark.parametrize("name", ["cornell", "mirror", "dof", "fog"])
+@pytest.mark.parametrize("name", make_golden.VCM_SCENES)
 def test_oracle_vcm_matches_reference_statistically(built, name):
     """VCMTracer (vcmTracer.cpp:6-446), base radius 0.02: the restated
     connections with VCM weights and merges through the reference's hash grid
@@ -193,7 +188,7 @@ def test_oracle_vcm_matches_reference_statistically(built, name):
     br, bp = blk(ref), blk(port)
     z = (br.mean(0) - bp.mean(0)) / np.sqrt(br.var(0, ddof=1) / 8 + bp.var(0, ddof=1) / 8 + 1e-12)
     assert np.abs(z).max() < 5.0, np.abs(z).max()
-    assert abs(port.mean() / ref.mean() - 1) < 0.015
+    assert means_agree(port, ref, 0.015), (port.mean(), ref.mean())
 
 
 def test_oracle_vcm_radius_schedule(built):

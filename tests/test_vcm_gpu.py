@@ -17,7 +17,7 @@ import os
 import numpy as np
 import pytest
 
-from conftest import GOLDEN
+from conftest import GOLDEN, means_agree
 import make_golden
 import wr_oracle
 from walkray_gb300 import _lib as L
@@ -49,18 +49,22 @@ def rotated(s):
     return s
 
 
-@pytest.mark.parametrize("name", ["cornell", "mirror", "dof", "mixed_l2", "fog"])
+@pytest.mark.parametrize("name", ["cornell", "mirror", "dof", "mixed_l2", "fog", "hetero"])
 def test_vcm_paired_with_oracle(ctx, name):
+    """The heterogeneous medium as in test_bpt_gpu.PAIRED_BAR, at radius 0.02
+    only (at 0.05 one ulp in the oracle alone already moves 3 % of the values)."""
     s = rotated(make_golden.golden_scenes()[name])
     h, w = s.camera.height, s.camera.width
+    hetero = name == "hetero"
+    frac, mean_tol = (0.85, 1e-2) if hetero else (0.99, 2e-3)
     sid = ctx.upload(s)
     orc = wr_oracle.SceneOracle(s)
-    for seed, radius in ((43, R), (44, 0.05)):
+    for seed, radius in ((43, R), (44, R if hetero else 0.05)):
         o = orc.render_vcm(8, 8, seed=seed, radius=radius)[0].reshape(h, w, 3) / 8
         g = ctx.render(sid, 8, 8, seed=seed, mode="vcm", radius=radius).astype(np.float64)
-        assert abs(g.mean() / o.mean() - 1) < 2e-3, (g.mean(), o.mean())
+        assert abs(g.mean() / o.mean() - 1) < mean_tol, (g.mean(), o.mean())
         close = np.isclose(g, o, rtol=1e-3, atol=1e-5)
-        assert close.mean() > 0.99, close.mean()
+        assert close.mean() > frac, close.mean()
     ctx.release(sid)
 
 
@@ -72,7 +76,7 @@ def test_vcm_matches_reference_renders(ctx, name):
     gpu = np.stack([ctx.render(sid, 64, 8, seed=950 + k, mode="vcm", radius=R).astype(np.float64)
                     for k in range(8)])
     assert np.abs(block_z(gpu, ref, 4)).max() < 5.0
-    assert abs(gpu.mean() / ref.mean() - 1) < 0.015
+    assert means_agree(gpu, ref, 0.015), (gpu.mean(), ref.mean())
     ctx.release(sid)
 
 

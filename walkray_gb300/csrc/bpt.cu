@@ -122,6 +122,7 @@ struct BptParams {
     // each photon's throughput
     bool light_only;
     float4* tput;
+    unsigned int* err;    // error bits of the traversals inside the weights (heterogeneous media)
 };
 
 // the weight's technique set for a sample of this batch
@@ -157,6 +158,7 @@ __device__ __forceinline__ void warp_append(bool ok, uint2 item, uint2* list, un
 // traces it at one call site (the first ray of a sub-path too: the camera
 // ray unfiltered (camera.cpp:52), which a filter with no inside and no
 // contact object is, the emitted ray with NoSelfCondition).
+template <bool HM>
 __global__ void __launch_bounds__(128) k_bpt_subpaths(RenderScene S, BptParams P, unsigned int* __restrict__ err) {
     constexpr unsigned FULL = 0xffffffffu;
     extern __shared__ uint32_t s_stack[];
@@ -235,7 +237,7 @@ __global__ void __launch_bounds__(128) k_bpt_subpaths(RenderScene S, BptParams P
                 out.put(sid, n++, term);
                 done = true;
             } else {
-                next = scatter(S, self, prev, g, st);
+                next = scatter<HM>(S, self, prev, g, st);
                 if (length(next.d) < 0.5f) {
                     out.put(sid, n++, next);
                     done = true;
@@ -333,7 +335,8 @@ __device__ float bpt_dir_prob(const RenderScene& S, f3 in_d, const PRay& out, bo
         pdf /= 4.f * fabsf(dot(in_d, h));
         return pdf;
     }
-    if (t == WR_MAT_HOMOGENEOUS) {  // homogeneousVolume.cpp:216-223 (a boundary record is delta)
+    if (t == WR_MAT_HOMOGENEOUS || t == WR_MAT_HETEROGENEOUS) {
+        // homogeneousVolume.cpp:216-223, HeterogeneousVolume.cpp:430-437 (a boundary record is delta)
         if (out.delta) return 0.f;
         const f3 ss = ld3(m->sigma_s), st = ss + ld3(m->sigma_a);
         return luminance(ss) / luminance(st) * hg_value(__ldg(&m->g), in_d, out.d);
@@ -356,15 +359,121 @@ __device__ __forceinline__ f3 bpt_eval_bsdf(const RenderScene& S, f3 in_d, const
 // `in_o` whose inside object is `in_inside` to a record at `out_o`: 1 but in
 // a homogeneous medium, whose surface / medium free-flight density over the
 // distance (homogeneousVolume.cpp:209-214, homogeneousVolume.h:40-53) it is
-__device__ __forceinline__ float bpt_origin_prob(const RenderScene& S, int in_inside, f3 in_o, f3 out_o,
-                                                 int out_contact) {
-    if (in_inside < 0 || obj_type(S, in_inside) != WR_MAT_HOMOGENEOUS) return 1.f;
-    const wr_object_desc* m = &S.objs[in_inside];
+// ---- heterogeneous media in the weights: the reference's ray-marched
+// integrals (HeterogeneousVolume.cpp:171-248) -------------------------------
+constexpr int HV_STACK = 96;  // traversal stack of these helpers (thread-local memory)
+
+struct HvCtx {  // what their own traversal needs
+    float pf;
+    int cap;
+    unsigned int* err;
+};
+__device__ __forceinline__ HvCtx hv_ctx(const BptParams& P) {
+    return HvCtx{P.pf, P.stack_cap < HV_STACK ? P.stack_cap : HV_STACK, P.err};
+}
+
+// HeterogeneousVolume::check (:171-185) of a record inside the medium (its
+// origin is inside the mesh by the record's inside object): the first hit of
+// the record's ray under its NoSelfCondition
+__device__ __forceinline__ bool hv_first_hit(const RenderScene& S, const PRay& r, const HvCtx& hc, float& idist) {
+    uint32_t stack[HV_STACK];
+    RayQ q = make_rayq(r.o, r.d, S.tree.scene_mag);
+    q.pf = hc.pf;
+    const Hit h = trace_closest<true, true>(S.tree, q, r.inside, r.contact, stack, 1, hc.cap, hc.err);
+    if (h.slot < 0 || !(h.t > 0.f)) return false;
+    idist = h.t;
+    return true;
+}
+
+// integrateDensity (:187-210): Simpson's rule over the density alone (no
+// sigma_t) along the record's ray up to min(dist, first hit), accumulated in
+// double into a float
+__device__ __noinline__ float hv_integrate(const RenderScene& S, const PRay& r, float dist, const HvCtx& hc) {
+    const wr_object_desc* m = &S.objs[r.inside];
+    float idist, acc = 0.f;
+    if (!hv_first_hit(S, r, hc, idist)) return acc;
+    dist = dist < idist ? dist : idist;
+    f3 p = r.o;
+    const unsigned n = (unsigned)ceilf(dist / (2.f * __ldg(&m->step_size)));
+    const double ss = (double)(dist / (float)n), mult = (1.0 / 6.0) * ss;
+    const f3 full = r.d * (float)ss, half = full * 0.5f;
+    float n1 = hv_density_ref(S, r.inside, p);
+    for (unsigned i = 0; i < n; i++) {
+        const float n2 = hv_density_ref(S, r.inside, p + half), n3 = hv_density_ref(S, r.inside, p + full);
+        acc = (float)((double)acc + mult * (double)(n1 + n2 * 4.f + n3));
+        n1 = n3;
+        p = p + full;
+    }
+    return acc;
+}
+
+// randianceDecay (:439-445): exp(-tau) of tau (:212-235), the Simpson
+// integral of sigma_t * density in float vec3 steps
+__device__ __noinline__ f3 hv_transmittance(const RenderScene& S, const PRay& r, float dist, const HvCtx& hc) {
+    const wr_object_desc* m = &S.objs[r.inside];
+    f3 acc = mk(0, 0, 0);
+    float idist;
+    if (hv_first_hit(S, r, hc, idist)) {
+        dist = dist < idist ? dist : idist;
+        const f3 sgt = ld3(m->sigma_s) + ld3(m->sigma_a);
+        f3 p = r.o;
+        const unsigned n = (unsigned)ceilf(dist / (2.f * __ldg(&m->step_size)));
+        const double ss = (double)(dist / (float)n), mult = (1.0 / 6.0) * ss;
+        const f3 full = r.d * (float)ss, half = full * 0.5f;
+        f3 n1 = sgt * hv_density_ref(S, r.inside, p);
+        for (unsigned i = 0; i < n; i++) {
+            const f3 n2 = sgt * hv_density_ref(S, r.inside, p + half), n3 = sgt * hv_density_ref(S, r.inside, p + full);
+            acc = acc + ((n1 + n2 * 4.f) + n3) * (float)mult;
+            n1 = n3;
+            p = p + full;
+        }
+    }
+    return mk(expf(-acc.x), expf(-acc.y), expf(-acc.z));
+}
+
+// HeterogeneousVolume::evalOriginProbability (:422-428): PSurface = exp(-I)
+// towards a record with a contact, else pMedium = Luminance(sigma_t *
+// density(end)) * exp(-I), I the density integral over the distance
+__device__ __noinline__ float hv_origin_prob(const RenderScene& S, const PRay& in, f3 out_o, int out_contact,
+                                            const HvCtx& hc) {
+    const wr_object_desc* m = &S.objs[in.inside];
+    const float d0 = length(in.o - out_o);
+    const float dist = (double)d0 > EPS_D ? d0 : (float)EPS_D;
+    const float tau = hv_integrate(S, in, dist, hc);
+    if (out_contact != -1) return expf(-tau);
     const f3 st = ld3(m->sigma_s) + ld3(m->sigma_a);
-    const float d0 = length(in_o - out_o);
+    const float dens = hv_density_ref(S, in.inside, in.o + in.d * dist);
+    return luminance(st * dens) * expf(-tau);
+}
+
+// Ray::evalOriginProbability (ray.cpp:24-30) of the linked record `in`
+// towards a record at out_o: 1 outside media, else the medium's surface or
+// free-flight density over their distance (homogeneousVolume.cpp:209-214,
+// PSurface / pMedium of homogeneousVolume.h:40-53; heterogeneous above)
+template <bool HM>
+__device__ __forceinline__ float bpt_origin_prob(const RenderScene& S, const PRay& in, f3 out_o, int out_contact,
+                                                 const HvCtx& hc) {
+    if (in.inside < 0) return 1.f;
+    const uint32_t t = obj_type(S, in.inside);
+    if constexpr (HM) {
+        if (t == WR_MAT_HETEROGENEOUS) return hv_origin_prob(S, in, out_o, out_contact, hc);
+    }
+    if (t != WR_MAT_HOMOGENEOUS) return 1.f;
+    const wr_object_desc* m = &S.objs[in.inside];
+    const f3 st = ld3(m->sigma_s) + ld3(m->sigma_a);
+    const float d0 = length(in.o - out_o);
     const float dist = (double)d0 > 1e-5 ? d0 : (float)1e-5;
     const f3 e = mk(expf(-st.x * dist), expf(-st.y * dist), expf(-st.z * dist));
     return out_contact != -1 ? luminance(e) : luminance(vmul(st, e));
+}
+
+// Ray::radianceDecay (ray.cpp:46-50) with the heterogeneous medium's marched tau
+template <bool HM>
+__device__ __forceinline__ f3 bpt_decay(const RenderScene& S, const PRay& r, float dist, const HvCtx& hc) {
+    if constexpr (HM) {
+        if (r.inside >= 0 && obj_type(S, r.inside) == WR_MAT_HETEROGENEOUS) return hv_transmittance(S, r, dist, hc);
+    }
+    return radiance_decay(S, r, dist);
 }
 
 __device__ __forceinline__ bool emissive(const RenderScene& S, int o) {
@@ -405,7 +514,9 @@ __device__ __forceinline__ PRay link(const Conn& C, int start, bool reverse, con
 // BidirectionalPathTracer::connectingMisWeight (bidirPathTracer.cpp:142-220),
 // expTerm = 1; the origin densities of surface vertices are 1
 // (AbstractObject::evalOriginProbability, abstractObj.cpp:54-59)
-__device__ float bpt_mis_weight(const RenderScene& S, const Conn& C, uint32_t pixel, double* rev, const MisKind& K) {
+template <bool HM>
+__device__ float bpt_mis_weight(const RenderScene& S, const Conn& C, uint32_t pixel, double* rev, const MisKind& K,
+                               const HvCtx& hc) {
     const int n = C.n, c = C.c;
     // reverse densities, eye end first (each record read once: a window
     // v2 = v(i + 2), v1 = v(i + 1), vi = v(i) slides towards the light)
@@ -426,7 +537,7 @@ __device__ float bpt_mis_weight(const RenderScene& S, const Conn& C, uint32_t pi
                 dirp = bpt_dir_prob(S, v1.d, v1, true, pixel);  // vertex n-1 is the camera, never re-pointed
             }
             // link(i+1, reverse).evalOriginProbability(link(i, reverse))
-            const float ori = bpt_origin_prob(S, b.inside, v1.o, vi.o, vi.contact);
+            const float ori = bpt_origin_prob<HM>(S, b, vi.o, vi.contact, hc);
             rev[i] *= (double)(dirp * ori);
         }
         v2 = v1;
@@ -459,13 +570,13 @@ __device__ float bpt_mis_weight(const RenderScene& S, const Conn& C, uint32_t pi
                 dirp = bpt_dir_prob(S, b.d, b, true, pixel);
             }
             // link(i-1).evalOriginProbability(link(i))
-            ori = bpt_origin_prob(S, b.inside, pm1.o, vi.o, vi.contact);
+            ori = bpt_origin_prob<HM>(S, b, vi.o, vi.contact, hc);
             dir *= (double)(dirp * ori);
         }
         if (K.vcm && i - 1 < n - 2 && !vi.delta) {  // merging at vertex i (vcmTracer.cpp:298-318)
             double p = dir_prev * rev[i];
             if (!pm1.delta) p *= (double)dirp;
-            p *= (double)(pm1.delta ? bpt_origin_prob(S, link(C, i - 1, false, pm1, vi).inside, pm1.o, vi.o, vi.contact)
+            p *= (double)(pm1.delta ? bpt_origin_prob<HM>(S, link(C, i - 1, false, pm1, vi), vi.o, vi.contact, hc)
                                     : ori);  // link(i-1).evalOriginProbability(link(i))
             p *= (double)g;
             p *= PI_D * K.radius * K.radius;
@@ -496,8 +607,9 @@ __device__ float bpt_mis_weight(const RenderScene& S, const Conn& C, uint32_t pi
 // each record read once (prev = v(i - 1), cur = v(i), nx = v(i + 1))
 // For a merge (VCMTracer::connectingColorProb, vcmTracer.cpp:357-366) the
 // light vertex's density of landing within `radius` is multiplied in.
-__device__ void bpt_color_prob(const RenderScene& S, const Conn& C, f3& color, float& prob, bool merge = false,
-                               float radius = 0.f) {
+template <bool HM>
+__device__ void bpt_color_prob(const RenderScene& S, const Conn& C, const HvCtx& hc, f3& color, float& prob,
+                               bool merge = false, float radius = 0.f) {
     const int n = C.n, c = C.c;
     f3 col = mk(1, 1, 1);
     float pr = 1.f;
@@ -508,18 +620,18 @@ __device__ void bpt_color_prob(const RenderScene& S, const Conn& C, f3& color, f
         float dist = 0.f;
         if (i <= c) {
             dist = max_eps(length(cur.o - nx.o));
-            col = vmul(col, radiance_decay(S, cur, dist));
+            col = vmul(col, bpt_decay<HM>(S, cur, dist, hc));
             if (i == c) col = col * (cos_term(S, cur) * cos_term(S, nx) / (dist * dist));
         } else if (i > c + 1) {
             dist = max_eps(length(prev.o - cur.o));
-            col = vmul(col, radiance_decay(S, cur, dist));
+            col = vmul(col, bpt_decay<HM>(S, cur, dist, hc));
         }
         if (i != c && i != c + 1) col = col * cos_term(S, cur);
         pr *= cur.dP * cur.oP;
         if (merge && i == c) {
             pr = (float)((double)pr * (PI_D * radius * radius));
             pr *= pdf_w_to_a(dist, cos_term(S, nx));  // link(c + 1, reverse): the eye vertex as connected
-            pr *= bpt_origin_prob(S, cur.inside, cur.o, nx.o, nx.contact);  // link(c).evalOriginProbability(link(c+1))
+            pr *= bpt_origin_prob<HM>(S, cur, nx.o, nx.contact, hc);  // link(c).evalOriginProbability(link(c+1))
             if (nx.inside >= 0 && nx.contact == -1) pr = (float)((double)pr * (4.0 / 3 * radius));
         }
         prev = cur;
@@ -656,6 +768,7 @@ __global__ void __launch_bounds__(128) k_bpt_visible(RenderScene S, BptParams P,
 // One contributing connection (sample sid, light length l, eye length e) of
 // throughputByConnecting: connectEdge, the colour / probability product and
 // the MIS weight, added to the sample's image.
+template <bool HM>
 __device__ void bpt_connect_one(const RenderScene& S, const BptParams& P, uint32_t sid, int l, int e) {
     const int W = l + e;
     const uint32_t pixel = sid % P.npix;
@@ -676,11 +789,12 @@ __device__ void bpt_connect_one(const RenderScene& S, const BptParams& P, uint32
     }
     f3 col;
     float prob;
-    bpt_color_prob(S, C, col, prob);
+    const HvCtx hc = hv_ctx(P);
+    bpt_color_prob<HM>(S, C, hc, col, prob);
     if (prob == 0.f) return;
     if (length(col) == 0.f) return;
     double rev[2 * BPT_MAX_RECORDS];
-    const float w = bpt_mis_weight(S, C, pixel, rev, mis_kind(P, sid, false));
+    const float w = bpt_mis_weight<HM>(S, C, pixel, rev, mis_kind(P, sid, false), hc);
     f3 contrib = divs(col, prob) * w;
     if (contrib.x == 0.f && contrib.y == 0.f && contrib.z == 0.f) return;
     if (e > 1) {
@@ -705,12 +819,13 @@ __device__ void bpt_connect_one(const RenderScene& S, const BptParams& P, uint32
 
 // persistent: the grid strides over the contributing connections, 32
 // consecutive ones (mostly one (l, e) pair) per warp
+template <bool HM>
 __global__ void __launch_bounds__(128) k_bpt_connect(RenderScene S, BptParams P) {
     const unsigned long long total = P.ncand[1];
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
          i += (unsigned long long)gridDim.x * blockDim.x) {
         const uint2 c = P.vis[i];
-        bpt_connect_one(S, P, c.x, (int)(c.y & 0xffu), (int)(c.y >> 8));
+        bpt_connect_one<HM>(S, P, c.x, (int)(c.y & 0xffu), (int)(c.y >> 8));
     }
 }
 
@@ -827,6 +942,7 @@ __global__ void __launch_bounds__(256) k_vcm_link(BptParams P) {
 
 // One merge: light records [0, idx) of sample lsid, then eye records i..0 of
 // sample sid (Query::Process, vcmTracer.cpp:188-201).  Adds w * colour / prob.
+template <bool HM>
 __device__ void vcm_merge_one(const RenderScene& S, const BptParams& P, uint32_t sid, int i, uint32_t lsid, int idx,
                               double* rev, f3& contrib) {
     Conn C;
@@ -854,9 +970,10 @@ __device__ void vcm_merge_one(const RenderScene& S, const BptParams& P, uint32_t
     const MisKind K = mis_kind(P, sid, true);
     f3 col;
     float prob;
-    bpt_color_prob(S, C, col, prob, true, K.radius);
+    const HvCtx hc = hv_ctx(P);
+    bpt_color_prob<HM>(S, C, hc, col, prob, true, K.radius);
     if (length(col) == 0.f || prob == 0.f) return;
-    const float w = bpt_mis_weight(S, C, sid % P.npix, rev, K);
+    const float w = bpt_mis_weight<HM>(S, C, sid % P.npix, rev, K, hc);
     contrib = contrib + divs(col * w, prob);
 }
 
@@ -866,6 +983,7 @@ __device__ void vcm_merge_one(const RenderScene& S, const BptParams& P, uint32_t
 // k_vcm_eval; when the list is full the merge is evaluated here.  Each
 // merge's contribution / nVM goes to the sample's pixel (the reference adds a
 // query's sum / nVM: the same up to the order of the additions).
+template <bool HM>
 __global__ void __launch_bounds__(128) k_vcm_merge(RenderScene S, BptParams P) {
     const uint32_t sid = blockIdx.x * blockDim.x + threadIdx.x;
     if (sid >= P.nsamp) return;
@@ -901,7 +1019,7 @@ __global__ void __launch_bounds__(128) k_vcm_merge(RenderScene S, BptParams P) {
                     if (!(dist * dist <= rr)) continue;
                     const unsigned long long m = atomicAdd(P.ncand + 3, 1ull);
                     if (m < P.merge_cap) P.merges[m] = make_uint4(sid, (uint32_t)i, (uint32_t)k, 0u);
-                    else vcm_merge_one(S, P, sid, i, pt.x, (int)pt.y, rev, contrib);
+                    else vcm_merge_one<HM>(S, P, sid, i, pt.x, (int)pt.y, rev, contrib);
                 }
             }
         }
@@ -912,6 +1030,7 @@ __global__ void __launch_bounds__(128) k_vcm_merge(RenderScene S, BptParams P) {
 }
 
 // the listed merges, one per thread and step (persistent)
+template <bool HM>
 __global__ void __launch_bounds__(128) k_vcm_eval(RenderScene S, BptParams P) {
     const unsigned long long n = P.ncand[3], total = n < P.merge_cap ? n : P.merge_cap;
     double rev[2 * BPT_MAX_RECORDS];
@@ -920,7 +1039,7 @@ __global__ void __launch_bounds__(128) k_vcm_eval(RenderScene S, BptParams P) {
         const uint4 m = P.merges[t];
         const uint2 pt = P.pts[m.z];
         f3 contrib = mk(0, 0, 0);
-        vcm_merge_one(S, P, m.x, (int)m.y, pt.x, (int)pt.y, rev, contrib);
+        vcm_merge_one<HM>(S, P, m.x, (int)m.y, pt.x, (int)pt.y, rev, contrib);
         if (contrib.x != 0.f || contrib.y != 0.f || contrib.z != 0.f)
             film_add(P.film + 3 * (size_t)P.npix * (m.x / P.npix), m.x % P.npix, divs(contrib, (float)P.npix));
     }
@@ -1292,7 +1411,7 @@ float vcm_radius(float base, uint32_t s) {
 
 int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& RP, uint32_t spp_offset,
                          uint32_t spp, float* d_sum, float* d_sumsq, unsigned int* err, cudaStream_t stream,
-                         int kind, float base_radius) {
+                         int kind, float base_radius, bool hetero) {
     if (RP.max_path_len + 2 > (uint32_t)BPT_MAX_RECORDS)
         return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "bidirectional mode: max_path_len is limited to 30");
     const bool vcm = kind == BIDIR_VCM, ppm = kind == BIDIR_PHOTON_MAP, grid_on = vcm || ppm;
@@ -1332,6 +1451,7 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
     P.max_path_len = RP.max_path_len;
     P.pf = prune_factor(RP.flags);
     P.stack_cap = RP.stack_cap;
+    P.err = err;
     P.eye.base = st.eye.as<float4>();
     P.light.base = st.light.as<float4>();
     P.counts = st.counts.as<uint32_t>();
@@ -1364,21 +1484,27 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
     }
     // the five counters live after the per-sample counts (8-byte aligned)
     P.ncand = reinterpret_cast<unsigned long long*>(st.counts.as<char>() + ((4ull * nsamp + 7) & ~7ull));
+    // scenes with a heterogeneous medium take the kernels that march its
+    // integrals in the weights; the others compile without those calls
+    const auto k_subpaths = hetero ? k_bpt_subpaths<true> : k_bpt_subpaths<false>;
+    const auto k_connect = hetero ? k_bpt_connect<true> : k_bpt_connect<false>;
+    const auto k_merge = hetero ? k_vcm_merge<true> : k_vcm_merge<false>;
+    const auto k_eval = hetero ? k_vcm_eval<true> : k_vcm_eval<false>;
     const int block = 128;
     const size_t smem = (size_t)RP.stack_cap * block * sizeof(uint32_t);
     if (smem > 48 * 1024) {
-        WR_CUDA(ctx, cudaFuncSetAttribute(k_bpt_subpaths, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        WR_CUDA(ctx, cudaFuncSetAttribute(k_subpaths, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         WR_CUDA(ctx, cudaFuncSetAttribute(k_bpt_visible, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         WR_CUDA(ctx, cudaFuncSetAttribute(k_ppm_eye, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     }
     int per_sm = 0, per_sm_v = 0;
-    WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bpt_connect, block, 0));
+    WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_connect, block, 0));
     WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_v, k_bpt_visible, block, smem));
     const int connect_grid = std::max(1, per_sm) * std::max(1, ctx->num_sms);
     const int visible_grid = std::max(1, per_sm_v) * std::max(1, ctx->num_sms);
     const int stride_grid = std::max(1, ctx->num_sms) * 8;
     int per_sm_s = 0;
-    WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_s, k_bpt_subpaths, block, smem));
+    WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_s, k_subpaths, block, smem));
     const int subpath_grid = std::max(1, per_sm_s) * std::max(1, ctx->num_sms);
     for (uint32_t done = 0; done < spp; done += per_batch) {
         const uint32_t b = std::min(per_batch, spp - done);
@@ -1387,7 +1513,7 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
         P.eye.nsamp = P.light.nsamp = P.nsamp;
         const int grid = (int)((P.nsamp + block - 1) / block);
         WR_CUDA(ctx, cudaMemsetAsync(P.ncand, 0, 5 * sizeof(unsigned long long), stream));
-        k_bpt_subpaths<<<subpath_grid, block, smem, stream>>>(S, P, err);
+        k_subpaths<<<subpath_grid, block, smem, stream>>>(S, P, err);
         WR_CUDA(ctx, cudaGetLastError());
         if (grid_on) {  // the batch's hash grids: one per slot (iteration)
             st.h_radii.resize(b);
@@ -1412,14 +1538,14 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
             WR_CUDA(ctx, cudaGetLastError());
             k_bpt_visible<<<visible_grid, block, smem, stream>>>(S, P, err);
             WR_CUDA(ctx, cudaGetLastError());
-            k_bpt_connect<<<connect_grid, block, 0, stream>>>(S, P);
+            k_connect<<<connect_grid, block, 0, stream>>>(S, P);
             WR_CUDA(ctx, cudaGetLastError());
             ctx->kernel_launches += 3;
         }
         if (vcm) {
-            k_vcm_merge<<<grid, block, 0, stream>>>(S, P);
+            k_merge<<<grid, block, 0, stream>>>(S, P);
             WR_CUDA(ctx, cudaGetLastError());
-            k_vcm_eval<<<connect_grid, block, 0, stream>>>(S, P);
+            k_eval<<<connect_grid, block, 0, stream>>>(S, P);
             WR_CUDA(ctx, cudaGetLastError());
             ctx->kernel_launches += 2;
         }

@@ -246,9 +246,6 @@ int wr_render_device(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, fl
         P.stack_cap = (int)sc->tree.max_depth + 3;
         const uint64_t npix = (uint64_t)rd->S.cam.width * rd->S.cam.height;
         if (desc->mode == WR_MODE_BIDIRECTIONAL || desc->mode == WR_MODE_VCM || desc->mode == WR_MODE_PHOTON_MAP) {
-            if (rd->has_hetero)
-                return set_error(ctx, WR_ERR_UNSUPPORTED,
-                                 "bidirectional / VCM / photon-mapping mode: heterogeneous media are not supported");
             if (desc->mode == WR_MODE_PHOTON_MAP && rd->has_media)
                 return set_error(ctx, WR_ERR_UNSUPPORTED,
                                  "photon-mapping mode: participating media (volume photons) are not supported");
@@ -257,7 +254,7 @@ int wr_render_device(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, fl
             const int kind = desc->mode == WR_MODE_VCM ? BIDIR_VCM
                            : desc->mode == WR_MODE_PHOTON_MAP ? BIDIR_PHOTON_MAP : BIDIR_BPT;
             return render_bidirectional(ctx, rd->S, P, desc->spp_offset, desc->spp, d_sum, d_sumsq, err, s, kind,
-                                        desc->radius > 0.f ? desc->radius : 0.01f);
+                                        desc->radius > 0.f ? desc->radius : 0.01f, rd->has_hetero);
         }
         if (desc->mode == WR_MODE_WAVEFRONT) {
             rc = render_wavefront(ctx, *rd, P, desc->spp_offset, desc->spp, d_sum, d_sumsq, s);

@@ -392,8 +392,6 @@ __device__ __forceinline__ void set_contact(const RenderScene& S, PRay& out, int
     (void)tri;
 }
 
-static __device__ PRay scatter(const RenderScene& S, int self, const PRay& in, PathRng& g, InsideStack& st);
-
 // Diffuse / Glossy / AnisotropicGlossy (diffuseObj.h:34-57, glossyObj.h:39-62, anisotropicGlossyObj.h:54-68)
 __device__ __forceinline__ PRay scatter_surface(const RenderScene& S, int self, const PRay& in, PathRng& g) {
     const wr_object_desc* m = &S.objs[self];
@@ -679,8 +677,172 @@ __device__ __forceinline__ PRay scatter_heterogeneous(const RenderScene& S, int 
     return ray_default();
 }
 
+// lookUpDensity (HeterogeneousVolume.cpp:71-116) in the reference's order of
+// operations (densityScale on each corner before the trilinear blend); the
+// inside-mesh test is implied by the record's inside object
+__device__ __forceinline__ float grid_density_ref(const GridDev& G, f3 p, float scale) {
+    if (p.x > G.p1[0] || p.x < G.p0[0] || p.y > G.p1[1] || p.y < G.p0[1] || p.z > G.p1[2] || p.z < G.p0[2])
+        return 0.f;
+    const float bx = G.p1[0] - G.p0[0], by = G.p1[1] - G.p0[1], bz = G.p1[2] - G.p0[2];
+    const float tx = p.x - G.p0[0], ty = p.y - G.p0[1], tz = p.z - G.p0[2];
+    const int ix = (int)floorf((float)G.nx * tx / bx), iy = (int)floorf((float)G.ny * ty / by),
+              iz = (int)floorf((float)G.nz * tz / bz);
+    if (ix < 0 || ix >= (int)G.nx || iy < 0 || iy >= (int)G.ny || iz < 0 || iz >= (int)G.nz) return 0.f;
+    const float dx = (float)G.nx * tx / bx - (float)ix, dy = (float)G.ny * ty / by - (float)iy,
+                dz = (float)G.nz * tz / bz - (float)iz;
+    const float s00 = lerpf(dx, grid_D(G, ix, iy, iz) * scale, grid_D(G, ix + 1, iy, iz) * scale);
+    const float s10 = lerpf(dx, grid_D(G, ix, iy + 1, iz) * scale, grid_D(G, ix + 1, iy + 1, iz) * scale);
+    const float s01 = lerpf(dx, grid_D(G, ix, iy, iz + 1) * scale, grid_D(G, ix + 1, iy, iz + 1) * scale);
+    const float s11 = lerpf(dx, grid_D(G, ix, iy + 1, iz + 1) * scale, grid_D(G, ix + 1, iy + 1, iz + 1) * scale);
+    return lerpf(dz, lerpf(dy, s00, s10), lerpf(dy, s01, s11));
+}
+
+// Scene::findInsideObjectWithID (scene.cpp:146-178) as lookUpDensity's
+// checkIn (HeterogeneousVolume.cpp:164-169) asks it: the closest hits of the
+// rays from p along -y and +y among object o's own triangles must both leave
+// the mesh (a point on a face, whose ray meets that face at t = 0 against
+// its normal, is outside).  Brute force over the mesh: a medium's boundary is
+// a handful of triangles.
+static __device__ __noinline__ bool inside_mesh(const RenderScene& S, int o, f3 p) {
+    const uint32_t tb = __ldg(&S.objs[o].tri_begin), tc = __ldg(&S.objs[o].tri_count);
+    for (int k = 0; k < 2; k++) {
+        const f3 d = mk(0.f, k == 0 ? -1.f : 1.f, 0.f);
+        const RayQ q = make_rayq(p, d, S.tree.scene_mag);
+        float best = __int_as_float(0x7f800000);
+        f3 bn = mk(0, 0, 0);
+        for (uint32_t t = 0; t < tc; t++) {
+            const TriRec* r = S.tree.tris + __ldg(&S.tri_slot[tb + t]);
+            const f3 v0 = xyz(__ldg(&r->v0)), v1 = xyz(__ldg(&r->v1)), v2 = xyz(__ldg(&r->v2));
+            const float h = tri_test(v0, v1, v2, q);
+            if (h >= 0.f && h < best) {
+                best = h;
+                bn = face_normal(v0, v1, v2);
+            }
+        }
+        if (!(best < __int_as_float(0x7f800000)) || dot(bn, d) < 0.f) return false;
+    }
+    return true;
+}
+
+// lookUpDensity of object `self` with its checkIn
+__device__ __forceinline__ float hv_density_ref(const RenderScene& S, int self, f3 p) {
+    if (!inside_mesh(S, self, p)) return 0.f;
+    const wr_object_desc* m = &S.objs[self];
+    return grid_density_ref(S.grids[__ldg(&m->grid_index)], p, __ldg(&m->density_scale));
+}
+
+// density of the quadratic through one Simpson step at offset x
+// (HeterogeneousVolume.cpp:285-287, 299-301): temp * (float - double + float) in double
+__device__ __forceinline__ float hv_dens_poly(float temp, float n1, float n2, float n3, float sss, double ss, float x) {
+    return (float)((double)temp * ((double)(n1 * sss) - (double)(3.f * n1 - 4.f * n2 + n3) * ss * (double)x +
+                                   (double)(2.f * (n1 - 2.f * n2 + n3) * x * x)));
+}
+
+// findDesiredIntegralDensity (HeterogeneousVolume.cpp:258-344) along the ray
+// of `in`, a record inside the medium: Simpson steps of at most 2 stepSize up
+// to its hit (the reference's check() traces the same ray under the same
+// NoSelfCondition, so its first hit is in.idist), then Newton-bisection on the
+// step's quadratic.  0 found, 2 Newton stopped after 30 iterations (both with
+// t, the integral and the density at t), 1 no hit, 3 no progress, 4 not reached.
+static __device__ __noinline__ int hv_find_ref(const RenderScene& S, int self, const PRay& in, float desired,
+                                               float& t, float& integ, float& dAtT) {
+    if (!(in.iobj >= 0 && in.idist > 0.f)) return 1;
+    const float dist = in.idist;
+    integ = 0.f;
+    f3 p = in.o;
+    const unsigned n = (unsigned)ceilf(dist / (2.f * __ldg(&S.objs[self].step_size)));
+    const double ss = (double)(dist / (float)n), mult = (1.0 / 6.0) * ss;
+    const f3 full = in.d * (float)ss, half = full * 0.5f;
+    float node1 = hv_density_ref(S, self, p);
+    for (unsigned i = 0; i < n; i++) {
+        const float node2 = hv_density_ref(S, self, p + half), node3 = hv_density_ref(S, self, p + full);
+        const float nd = (float)((double)integ + mult * (double)(node1 + node2 * 4.f + node3));
+        if (nd >= desired) {
+            float a = 0.f, b = (float)ss, x = a, fx = integ - desired;
+            const float sss = (float)(ss * ss), temp = (float)(1.0 / (double)sss);
+            for (int it = 1;; it++) {
+                const float dfx = hv_dens_poly(temp, node1, node2, node3, sss, ss, x);
+                x -= fx / dfx;
+                if (x <= a || x >= b || dfx == 0.f) x = (float)(0.5 * (double)(b + a));
+                const float intval =
+                    (float)((double)integ +
+                            (double)temp * (1.0 / 6.0) *
+                                ((double)x * ((double)(6.f * node1 * sss) -
+                                              (double)(3.f * (3.f * node1 - 4.f * node2 + node3)) * ss * (double)x +
+                                              (double)(4.f * (node1 - 2.f * node2 + node3) * x * x))));
+                fx = intval - desired;
+                const float dnow = hv_dens_poly(temp, node1, node2, node3, sss, ss, x);
+                if (fabs((double)fx) < 1e-4 || it + 1 > 30) {
+                    t = (float)((double)x + ss * i);
+                    integ = intval;
+                    dAtT = dnow;
+                    return fabs((double)fx) < 1e-4 ? 0 : 2;
+                }
+                if (fx > 0.f) b = x;
+                else a = x;
+            }
+        }
+        const f3 nxt = p + full;
+        if (nxt.x == p.x && nxt.y == p.y && nxt.z == p.z) return 3;
+        integ = nd;
+        node1 = node3;
+        p = nxt;
+    }
+    return 4;
+}
+
+// HeterogeneousVolume::scatter (HeterogeneousVolume.cpp:449-641) as the
+// reference samples it: sampleDistance (:354-404) inverts the Simpson-
+// integrated density at -log(1-u) / Luminance(sigma_t); a collision keeps
+// oP = exp(-integral) * density(t), passing the medium oP = exp(-integral).
+// Used by the bidirectional renderers, whose weights evaluate the same
+// densities (the unidirectional kernels use delta tracking).
+static __device__ __noinline__ PRay scatter_heterogeneous_ref(const RenderScene& S, int self, const PRay& in,
+                                                              PathRng& g, InsideStack& st, bool* delegate,
+                                                              float* psurf) {
+    const wr_object_desc* m = &S.objs[self];
+    *delegate = false;
+    const bool go_in = in.iobj == self && in.inside != self;
+    const bool be_in = in.inside == self;
+    if (go_in) return medium_enter(S, self, in, g);
+    const f3 ss = ld3(m->sigma_s), st_ = ss + ld3(m->sigma_a);
+    const float desired = (float)(-log(1.0 - (double)g.next()) / (double)luminance(st_));
+    float t = 0.f, integ = 0.f, dAtT = 0.f;
+    const int flag = be_in ? hv_find_ref(S, self, in, desired, t, integ, dAtT) : 1;
+    const float expVal = expf(-integ);
+    const bool ok = flag == 0 || flag == 2;
+    if (be_in && ok) {
+        PRay out = ray_default();
+        out.o = in.o + in.d * t;
+        out.rad = hg_sample(__ldg(&m->g), in.d, g, out.d, out.dP);
+        out.inside = self;
+        const float albedo = luminance(ss) / luminance(st_);
+        if (g.next() < albedo) {
+            out.contact = -1;
+            out.dP *= albedo;
+            out.oP = expVal * dAtT;
+            out.rad = vmul(out.rad, ss * hv_density_ref(S, self, out.o));
+        } else {
+            out.d = mk(0, 0, 0);
+            out.rad = mk(0, 0, 0);
+            out.dP = 1.f;
+            out.oP = expVal * dAtT;
+            out.inside = -1;
+            out.contact = -1;
+        }
+        return out;
+    }
+    if (be_in) {
+        *psurf = expVal;
+        return medium_exit(S, self, in, expVal, g, st, delegate);
+    }
+    return ray_default();
+}
+
 // one scatter() call, following delegations (RefractiveObject handing a hit
-// inside it to the hit object; media handing over to the surface hit)
+// inside it to the hit object; media handing over to the surface hit).
+// RefMedia: heterogeneous media by the reference's own sampler.
+template <bool RefMedia = false>
 static __device__ __forceinline__ PRay scatter(const RenderScene& S, int self, const PRay& in, PathRng& g,
                                             InsideStack& st) {
     PRay cur = in;
@@ -704,7 +866,10 @@ static __device__ __forceinline__ PRay scatter(const RenderScene& S, int self, c
                 }
                 break;
             case WR_MAT_HOMOGENEOUS: out = scatter_homogeneous(S, self, cur, g, st, &del, &ps); break;
-            default: out = scatter_heterogeneous(S, self, cur, g, st, &del, &ps); break;
+            default:
+                if constexpr (RefMedia) out = scatter_heterogeneous_ref(S, self, cur, g, st, &del, &ps);
+                else out = scatter_heterogeneous(S, self, cur, g, st, &del, &ps);
+                break;
         }
         if (del) {  // medium hands over to the surface it hit: scatter there, oP *= P_surface
             oP_scale *= ps;

@@ -534,9 +534,10 @@ def fbm_grid(n=128, octaves=5, seed=3, lo=0.0, hi=4.0) -> np.ndarray:
     return (lo + (hi - lo) * v).reshape(n, n, n).astype(np.float32)
 
 
-def cornell_media(width=512, height=512, grid_n=128, seed=3) -> Scene:
+def cornell_media(width=512, height=512, grid_n=128, seed=3, step_size=0.002) -> Scene:
     """Cornell box plus a heterogeneous medium (grid_n^3 fBm density in
-    [0, 4], HG g = 0.3, albedo 0.8, sigma_t = 1, densityScale 1, IOR 1) in a
+    [0, 4], HG g = 0.3, albedo 0.8, sigma_t = 1, densityScale 1, IOR 1,
+    ray-marching step `step_size`, HeterogeneousVolume's default 0.002) in a
     box just inside the walls, and a homogeneous sphere (sigma_t = 1.5,
     albedo 0.8, g = -0.2, IOR 1) inside that medium."""
     s = Scene("cornell_media")
@@ -546,7 +547,7 @@ def cornell_media(width=512, height=512, grid_n=128, seed=3) -> Scene:
                     (hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]))
     s.grids.append(Grid(fbm_grid(grid_n, 5, seed), tuple(float(x) for x in V.min(0)), tuple(float(x) for x in V.max(0))))
     s.add(MAT_HETEROGENEOUS, V, F, sigma_s=(0.8, 0.8, 0.8), sigma_a=(0.2, 0.2, 0.2), g=0.3, ior=1.0,
-          density_scale=1.0, step_size=0.002, grid_index=0)
+          density_scale=1.0, step_size=float(step_size), grid_index=0)
     P, F2 = icosphere(3)
     P = (P * 0.15 + np.array([0.6, 0.55, 0.25])).astype(np.float32)
     s.add(MAT_HOMOGENEOUS, P, F2, sigma_s=(1.2, 1.2, 1.2), sigma_a=(0.3, 0.3, 0.3), g=-0.2, ior=1.0)
