@@ -82,7 +82,8 @@ typedef struct wr_object_desc {
     float sigma_a[3];        /* media absorption coefficient */
     float g;                 /* Henyey-Greenstein asymmetry */
     float density_scale;     /* heterogeneous: density multiplier (reference default 100) */
-    float step_size;         /* heterogeneous: ray-marching step (reference default 0.002) */
+    float step_size;         /* media: ray-marching step (HeterogeneousVolume default 0.002; photon mapping
+                                marches homogeneous media with it too) */
 } wr_object_desc;
 
 /* Pinhole camera (Camera::setup, camera.h:28-48); image_plane_dist is the
@@ -209,8 +210,9 @@ int wr_trace_closest_device(wr_ctx* ctx, wr_scene_id scene, const float* d_rays,
                                     record estimates the photon density (kernel 3(1-d^2/r^2)^2/pi; the
                                     Gaussian-weighted elliptic estimate behind an anisotropic glossy
                                     reflection, photonMap.cpp:383-652); wr_render_desc.radius is the base
-                                    radius (PhotonMap::setRadius; 0 = 0.01); surfaces only (no media),
-                                    max_path_len <= 30 */
+                                    radius (PhotonMap::setRadius; 0 = 0.01); media: volume photons and
+                                    ray-marched eye segments in steps of each medium's step_size
+                                    (photonMap.cpp:306-367); max_path_len <= 30 */
 
 #define WR_RENDER_NEE 1u      /* PathTracer's next-event-estimation branch (pathTracer.cpp:39-66) */
 /* Rendering traverses front to back and skips a box whose entry distance is

@@ -157,6 +157,9 @@ static void build_scene(RenderEngine& eng, const wrs_scene& ws, Rng* rng) {
             case WR_MAT_HOMOGENEOUS:
                 static_cast<HomogeneousVolume*>(obj)->setSigma(v3(d.sigma_s), v3(d.sigma_a));
                 static_cast<HomogeneousVolume*>(obj)->setIOR(d.ior);
+                // the ray-marching step of PhotonMap's volume estimate; the
+                // constructor leaves it unset (homogeneousVolume.h:11, 76-81)
+                static_cast<HomogeneousVolume*>(obj)->setStepSize(d.step_size);
                 break;
             case WR_MAT_HETEROGENEOUS: {
                 HeterogeneousVolume* hv = static_cast<HeterogeneousVolume*>(obj);

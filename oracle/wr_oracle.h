@@ -96,7 +96,7 @@ float wro_vcm_radius(float base, uint32_t s);
 /* ---- progressive photon mapping ----------------------------------------- */
 /* PhotonMap::renderPixels (photonMap.cpp:20-148, PPM) for samples [s0, s1)
  * with base radius r0 (PhotonMap::setRadius); sums as wro_render_bpt.
- * Returns 1 (nothing rendered) for scenes with participating media. */
+ * Surfaces and both kinds of media (volume photons, marched eye segments); returns 0. */
 int wro_render_ppm(const wro_scene* s, uint32_t max_path_len, uint64_t seed, float r0, uint32_t s0, uint32_t s1,
                    double* sum, double* sumsq, int nthreads, uint64_t* rays_traced);
 /* the elliptic query's set-up (photonMap.cpp:384-613) at a diffuse point of

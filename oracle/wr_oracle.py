@@ -201,5 +201,5 @@ class SceneOracle:
         rc = self.lib.wro_render_ppm(self.h, max_path_len, seed, radius, s0, s0 + spp, _p(s), _p(s2), threads,
                                      C.byref(rays))
         if rc:
-            raise ValueError("the photon-mapping restatement covers surfaces only (no participating media)")
+            raise RuntimeError("wro_render_ppm failed")
         return s, s2, rays.value

@@ -31,9 +31,10 @@ from the reference sources) on small seeded scenes and stores its answers:
                       64 spp each
 
   render_ppm_*.npz    PhotonMap::renderPixels (base radius 0.02) on the
-                      Cornell, mirror, thin-lens, mixed-material and
-                      anisotropic-floor scenes, 8 reference renders of 64 spp
-                      each
+                      Cornell, mirror, thin-lens, mixed-material,
+                      anisotropic-floor, homogeneous-fog and
+                      heterogeneous-medium scenes, 8 reference renders of
+                      64 spp each
   ppm_ellipse_ref.npz the reference's ellipse set-ups of the anisotropic
                       photon query (inputs and results), recorded in its own
                       PhotonMap renders of the anisotropic-floor scene
@@ -254,7 +255,7 @@ def vcm_fixtures(td, names=VCM_SCENES):
         render_set(sc[name], p, td, f"render_vcm_{name}.npz", extra=("vcm", str(VCM_RADIUS)), spp=64)
 
 
-PPM_SCENES = ("cornell", "mirror", "dof", "mixed_l2", "aniso")
+PPM_SCENES = ("cornell", "mirror", "dof", "mixed_l2", "aniso", "fog", "hetero")
 PPM_RADIUS = 0.02
 
 

@@ -51,7 +51,8 @@ constexpr double PI_D = 3.1415926535897932384626433832795;
 constexpr double EPS_D = 1e-5;
 
 // ---------------------------------------------------------------------------
-// vertex records: {o, oP}, {d, dP}, {rad, inside}, {contact normal, contact + 2 | delta << 31}
+// vertex records: {o, oP}, {d, dP}, {rad, inside},
+// {contact normal, contact + 2 | photon type << 28 | delta << 31}
 // ---------------------------------------------------------------------------
 struct VtxStore {
     float4* base;
@@ -65,7 +66,8 @@ struct VtxStore {
         v[1] = make_float4(r.d.x, r.d.y, r.d.z, r.dP);
         v[2] = make_float4(r.rad.x, r.rad.y, r.rad.z, __int_as_float(r.inside));
         v[3] = make_float4(r.cnorm.x, r.cnorm.y, r.cnorm.z,
-                           __uint_as_float((uint32_t)(r.contact + 2) | (r.delta ? 0x80000000u : 0u)));
+                           __uint_as_float((uint32_t)(r.contact + 2) | ((uint32_t)r.ptype << 28) |
+                                           (r.delta ? 0x80000000u : 0u)));
     }
     __device__ __forceinline__ PRay get(uint32_t sid, int k) const {
         const float4* v = at(sid, k);
@@ -79,7 +81,8 @@ struct VtxStore {
         r.inside = __float_as_int(c.w);
         r.cnorm = mk(n.x, n.y, n.z);
         const uint32_t w = __float_as_uint(n.w);
-        r.contact = (int)(w & 0x7fffffffu) - 2;
+        r.contact = (int)(w & 0x0fffffffu) - 2;
+        r.ptype = (uint8_t)((w >> 28) & 3u);
         r.delta = (w >> 31) != 0;
         return r;
     }
@@ -122,6 +125,10 @@ struct BptParams {
     // each photon's throughput
     bool light_only;
     float4* tput;
+    // with participating media the INVOL photons have their own grid: grid
+    // nslots + slot of the same arrays; their point entries carry bit 31
+    bool vol_grid;
+    uint32_t nslots;      // slots (iterations) of the batch
     unsigned int* err;    // error bits of the traversals inside the weights (heterogeneous media)
 };
 
@@ -687,12 +694,12 @@ __global__ void __launch_bounds__(128) k_bpt_enum(RenderScene S, BptParams P) {
         nl = (int)((cnt >> 8) & 0xffu);
         for (int k = 0; k < ne; k++) {
             const uint32_t w = __float_as_uint(__ldg(&P.eye.at(sid, k)[3].w));
-            emE |= (uint32_t)emissive(S, (int)(w & 0x7fffffffu) - 2) << k;
+            emE |= (uint32_t)emissive(S, (int)(w & 0x0fffffffu) - 2) << k;
             dE |= (w >> 31) << k;
         }
         for (int k = 0; k < nl; k++) {
             const uint32_t w = __float_as_uint(__ldg(&P.light.at(sid, k)[3].w));
-            emL |= (uint32_t)emissive(S, (int)(w & 0x7fffffffu) - 2) << k;
+            emL |= (uint32_t)emissive(S, (int)(w & 0x0fffffffu) - 2) << k;
             dL |= (w >> 31) << k;
         }
     }
@@ -881,8 +888,8 @@ __global__ void __launch_bounds__(128) k_vcm_points(RenderScene S, BptParams P) 
     int nl = 0;
     if (sid < P.nsamp) nl = (int)((__ldg(&P.counts[sid]) >> 8) & 0xffu);
     const int nrec = (int)P.max_path_len + 2;
-    f3 lo = mk(0, 0, 0), hi = mk(0, 0, 0);
-    bool any = false, alive = true;
+    f3 lo = mk(0, 0, 0), hi = mk(0, 0, 0), vlo = lo, vhi = hi;
+    bool any = false, vany = false, alive = true;
     for (int i = 1; i < nrec; i++) {  // equal loop bounds in every lane: warp_append needs the whole warp
         bool ok = false;
         uint2 item = make_uint2(sid, (uint32_t)i);
@@ -890,10 +897,20 @@ __global__ void __launch_bounds__(128) k_vcm_points(RenderScene S, BptParams P) 
             const PRay r = P.light.get(sid, i);
             if (emissive(S, r.contact)) alive = false;
             else if (!r.delta) {
-                ok = true;
-                lo = mk(fminf(lo.x, r.o.x), fminf(lo.y, r.o.y), fminf(lo.z, r.o.z));
-                hi = mk(fmaxf(hi.x, r.o.x), fmaxf(hi.y, r.o.y), fmaxf(hi.z, r.o.z));
-                any = true;
+                // photon mapping keeps OUTVOL records as surface photons and
+                // INVOL records as volume photons (photonMap.cpp:74-85)
+                const bool vol = P.light_only && r.ptype == PT_INVOL;
+                ok = !P.light_only || r.ptype == PT_OUTVOL || vol;
+                if (ok && vol) {
+                    item.y |= 0x80000000u;
+                    vlo = mk(fminf(vlo.x, r.o.x), fminf(vlo.y, r.o.y), fminf(vlo.z, r.o.z));
+                    vhi = mk(fmaxf(vhi.x, r.o.x), fmaxf(vhi.y, r.o.y), fmaxf(vhi.z, r.o.z));
+                    vany = true;
+                } else if (ok) {
+                    lo = mk(fminf(lo.x, r.o.x), fminf(lo.y, r.o.y), fminf(lo.z, r.o.z));
+                    hi = mk(fmaxf(hi.x, r.o.x), fmaxf(hi.y, r.o.y), fmaxf(hi.z, r.o.z));
+                    any = true;
+                }
             }
         }
         warp_append(ok, item, P.pts, P.ncand + 2);
@@ -925,6 +942,15 @@ __global__ void __launch_bounds__(128) k_vcm_points(RenderScene S, BptParams P) 
         atomicMax(k + 4, fkey(hi.y));
         atomicMax(k + 5, fkey(hi.z));
     }
+    if (vany) {  // volume photons: the slot's volume grid (its box also includes the origin)
+        int* k = P.bbox + 6 * (P.nslots + slot);
+        atomicMin(k + 0, fkey(vlo.x));
+        atomicMin(k + 1, fkey(vlo.y));
+        atomicMin(k + 2, fkey(vlo.z));
+        atomicMax(k + 3, fkey(vhi.x));
+        atomicMax(k + 4, fkey(vhi.y));
+        atomicMax(k + 5, fkey(vhi.z));
+    }
 }
 
 // HashGrid::Build: every point into its bucket's list
@@ -933,10 +959,11 @@ __global__ void __launch_bounds__(256) k_vcm_link(BptParams P) {
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
          i += (unsigned long long)gridDim.x * blockDim.x) {
         const uint2 pt = P.pts[i];
-        const GridView G = grid_view(P, pt.x / P.npix);
-        const f3 pos = xyz(__ldg(P.light.at(pt.x, (int)pt.y)));
+        const uint32_t gi = pt.x / P.npix + ((pt.y >> 31) ? P.nslots : 0u);
+        const GridView G = grid_view(P, gi);
+        const f3 pos = xyz(__ldg(P.light.at(pt.x, (int)(pt.y & 0xffu))));
         const uint32_t b = grid_bucket(G, pos);
-        P.next[i] = atomicExch(P.head + (size_t)(pt.x / P.npix) * P.npix + b, (int)i);
+        P.next[i] = atomicExch(P.head + (size_t)gi * P.npix + b, (int)i);
     }
 }
 
@@ -1053,18 +1080,21 @@ __global__ void __launch_bounds__(128) k_vcm_eval(RenderScene S, BptParams P) {
 constexpr uint32_t PPM_MERGE_LEN = 10;  // photonMap.cpp:9
 
 // each photon's throughput up to its record (photonMap.cpp:228-236)
+template <bool HM>
 __global__ void __launch_bounds__(256) k_ppm_tput(RenderScene S, BptParams P) {
     const unsigned long long total = P.ncand[2];
+    const HvCtx hc = hv_ctx(P);
     for (unsigned long long k = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; k < total;
          k += (unsigned long long)gridDim.x * blockDim.x) {
         const uint2 pt = P.pts[k];
+        const int idx = (int)(pt.y & 0xffu);
         f3 t = mk(1, 1, 1);
         PRay cur = P.light.get(pt.x, 0);
-        for (int i = 0; i < (int)pt.y; i++) {
+        for (int i = 0; i < idx; i++) {
             const PRay nx = P.light.get(pt.x, i + 1);
             t = vmul(t, divs(divs(cur.rad, cur.dP), cur.oP));
             t = t * cos_term(S, cur);
-            t = vmul(t, radiance_decay(S, cur, length(cur.o - nx.o)));
+            t = vmul(t, bpt_decay<HM>(S, cur, length(cur.o - nx.o), hc));
             cur = nx;
         }
         t = divs(t, cur.oP);
@@ -1073,20 +1103,23 @@ __global__ void __launch_bounds__(256) k_ppm_tput(RenderScene S, BptParams P) {
 }
 
 // Query::Process (photonMap.cpp:219-246): one photon's density estimate at
-// the eye record `out` (direction towards the camera side)
+// the eye record `out` (direction towards the camera side); a volume photon's
+// kernel is over N r^3
 __device__ __forceinline__ f3 ppm_photon(const RenderScene& S, const BptParams& P, uint32_t k, const PRay& out,
-                                         float radius) {
+                                         float radius, bool volume = false) {
     const uint2 pt = P.pts[k];
+    const int idx = (int)(pt.y & 0xffu);
     const float4 tp = __ldg(&P.tput[k]);
-    const PRay prevl = P.light.get(pt.x, (int)pt.y - 1);
-    const f3 pos = xyz(__ldg(P.light.at(pt.x, (int)pt.y)));
+    const PRay prevl = P.light.get(pt.x, idx - 1);
+    const f3 pos = xyz(__ldg(P.light.at(pt.x, idx)));
     const f3 color = vmul(mk(tp.x, tp.y, tp.z), eval_bsdf(S, prevl.d, out));
     const float dist_sqr = powf(length(out.o - pos), 2.f);
     if (!legal(color)) return mk(0, 0, 0);
     const float x = 1.f - dist_sqr / (radius * radius);
     const float sk = 0.f > x ? 0.f : x;
     const float kernel = (float)((double)(3.f * sk * sk) / PI_D);
-    return color * (kernel / ((float)P.npix * radius * radius));
+    return color * (volume ? kernel / ((float)P.npix * radius * radius * radius)
+                           : kernel / ((float)P.npix * radius * radius));
 }
 
 // ---- the anisotropic (elliptic) photon query, photonMap.cpp:384-652 --------
@@ -1252,8 +1285,8 @@ __device__ __forceinline__ f3 ppm_photon_ellipse(const RenderScene& S, const Bpt
                                                  float radius, f3 ex, f3 ey, float ratio, double& sumw, int& count) {
     const uint2 pt = P.pts[k];
     const float4 tp = __ldg(&P.tput[k]);
-    const PRay prevl = P.light.get(pt.x, (int)pt.y - 1);
-    const f3 pos = xyz(__ldg(P.light.at(pt.x, (int)pt.y)));
+    const PRay prevl = P.light.get(pt.x, (int)(pt.y & 0xffu) - 1);
+    const f3 pos = xyz(__ldg(P.light.at(pt.x, (int)(pt.y & 0xffu))));
     const f3 color = vmul(mk(tp.x, tp.y, tp.z), eval_bsdf(S, prevl.d, out));
     if (!legal(color)) return mk(0, 0, 0);
     const f3 hp = pos - out.o;
@@ -1267,11 +1300,50 @@ __device__ __forceinline__ f3 ppm_photon_ellipse(const RenderScene& S, const Bpt
     return (color * w) * conv;
 }
 
+// the 8 cells of HashGrid::Process (hashgrid.hxx:96-165) around q: every
+// photon within the radius through `visit(k)`
+template <typename F>
+__device__ __forceinline__ void ppm_grid_walk(const BptParams& P, const GridView& G, f3 q, F&& visit) {
+    const f3 dmin = q - G.bmin, dmax = G.bmax - q;
+    if (dmin.x < 0.f || dmin.y < 0.f || dmin.z < 0.f || dmax.x < 0.f || dmax.y < 0.f || dmax.z < 0.f) return;
+    const f3 cp = mk(G.inv_cell * dmin.x, G.inv_cell * dmin.y, G.inv_cell * dmin.z);
+    const f3 cf = mk(floorf(cp.x), floorf(cp.y), floorf(cp.z));
+    const int px = (int)cf.x, py = (int)cf.y, pz = (int)cf.z;
+    const f3 fr = cp - cf;
+    const int pxo = px + (fr.x < 0.5f ? -1 : 1), pyo = py + (fr.y < 0.5f ? -1 : 1), pzo = pz + (fr.z < 0.5f ? -1 : 1);
+    const float rr = G.radius * G.radius;
+    const unsigned long long npts = P.ncand[2];
+    for (int j = 0; j < 8; j++) {
+        const int cx = (j & 4) ? pxo : px, cy = (j & 2) ? pyo : py, cz = (j & 1) ? pzo : pz;
+        unsigned long long guard = 0;  // a list is at most every point of the batch long
+        for (int k = __ldg(&G.head[grid_bucket(G, cx, cy, cz)]); k >= 0 && guard++ < npts; k = __ldg(&P.next[k])) {
+            const uint2 pt = P.pts[k];
+            const float dist = length(q - xyz(__ldg(P.light.at(pt.x, (int)(pt.y & 0xffu)))));
+            if (!(dist * dist <= rr)) continue;
+            visit((uint32_t)k);
+        }
+    }
+}
+
+// an eye segment inside a medium before the estimate's record, marched after
+// the whole eye path (its draws come after the path's)
+struct PpmSeg {
+    f3 o, d;
+    float dist;
+    int inside, contact;
+};
+
 // One thread per sample: the eye path of PhotonMap::sampleMergePath (at most
 // 10 bounces) up to its first emitter (its radiance) or diffuse record (the
 // photon density there, throughputByDensityEstimation), times the camera
-// record's factors, into the sample's image.  Records after that one are
-// never read, so the path is not continued.
+// record's factors, into the sample's image.  Without media the records after
+// that one are never read, so the path is not continued.  MEDIA: the merge
+// path's dispatch (a record inside a medium goes on with the object its ray
+// hits; a boundary record whose ray hits a medium jumps to that hit), the
+// whole path sampled (the march offsets are drawn after it), and each segment
+// inside a medium before the estimate ray-marched against the volume photons
+// (photonMap.cpp:306-367): color = Tr * surface + volume.
+template <bool MEDIA, bool HM>
 __global__ void __launch_bounds__(128) k_ppm_eye(RenderScene S, BptParams P, unsigned int* __restrict__ err) {
     extern __shared__ uint32_t s_stack[];
     uint32_t* stack = s_stack + threadIdx.x;
@@ -1294,56 +1366,75 @@ __global__ void __launch_bounds__(128) k_ppm_eye(RenderScene S, BptParams P, uns
     f3 surf = mk(0, 0, 0);
     f3 pdir = mk(0, 0, 0);  // direction of the record before `prev` (eyeMergePath[i-2])
     const GridView G = grid_view(P, slot);
-    const unsigned long long npts = P.ncand[2];
+    constexpr int NSEG = MEDIA ? (int)PPM_MERGE_LEN + 2 : 1;
+    PpmSeg seg[NSEG];
+    int nseg = 0;
+    bool merged = false;  // the estimate's record is found; later records only advance the draws
     for (uint32_t depth = 0;; depth++) {
-        const int self = prev.inside >= 0 ? prev.inside : prev.iobj;
+        int self;
+        if constexpr (MEDIA) self = prev.inside >= 0 && !is_volume(S, prev.inside) ? prev.inside : prev.iobj;
+        else self = prev.inside >= 0 ? prev.inside : prev.iobj;
         if (self < 0) break;  // the terminate record: nothing to estimate
-        const PRay next = scatter(S, self, prev, g, st);
+        PRay next;
+        if constexpr (MEDIA) {
+            PRay cur = prev;
+            const bool jump = self == prev.iobj && is_volume(S, self) && prev.contact >= 0 && is_volume(S, prev.contact);
+            if (jump) {  // photonMap.cpp:165-168
+                cur.o = cur.o + cur.d * cur.idist;
+                cur.idist = 0.f;
+            }
+            if (jump && obj_type(S, self) == WR_MAT_HETEROGENEOUS && cur.inside == self) {
+                // the medium's check() from the moved origin: inside its mesh
+                // (or on it as the record's contact), then the first hit
+                float chk = 0.f;
+                if (cur.contact == self || inside_mesh(S, self, cur.o)) {
+                    RayQ q = make_rayq(cur.o, cur.d, S.tree.scene_mag);
+                    q.pf = P.pf;
+                    const Hit h =
+                        trace_closest<true, true>(S.tree, q, cur.inside, cur.contact, stack, stride, P.stack_cap, err);
+                    if (h.slot >= 0 && h.t > 0.f) chk = h.t;
+                }
+                bool del = false;
+                float ps = 1.f;
+                next = scatter_heterogeneous_ref(S, self, cur, g, st, &del, &ps, chk);
+            } else {
+                next = scatter<HM>(S, self, cur, g, st);
+            }
+        } else {
+            next = scatter(S, self, prev, g, st);
+        }
         const bool ended = length(next.d) < 0.5f;
         if (!ended && depth + 1 > PPM_MERGE_LEN) break;  // cut: `next` is not a record
-        if (emissive(S, next.contact)) {
-            surf = next.rad;
-            break;
-        }
-        if (next.contact >= 0 && obj_type(S, next.contact) == WR_MAT_DIFFUSE) {  // nonSpecular()
-            PRay out = next;
-            out.d = -prev.d;
-            // reached through an anisotropic record: the elliptic estimate
-            f3 ex = mk(0, 0, 0), ey = mk(0, 0, 0);
-            float ratio = 1.f;
-            const bool ell = prev.contact >= 0 && obj_type(S, prev.contact) == WR_MAT_ANISO &&
-                             ellipse_frame(pdir, prev.cnorm, prev.d, next.cnorm, __ldg(&S.objs[prev.contact].nu),
-                                           __ldg(&S.objs[prev.contact].nv), ex, ey, ratio) == 0;
-            double sumw = 0.0;
-            int count = 0;
-            const f3 q = next.o, dmin = q - G.bmin, dmax = G.bmax - q;
-            if (!(dmin.x < 0.f || dmin.y < 0.f || dmin.z < 0.f || dmax.x < 0.f || dmax.y < 0.f || dmax.z < 0.f)) {
-                const f3 cp = mk(G.inv_cell * dmin.x, G.inv_cell * dmin.y, G.inv_cell * dmin.z);
-                const f3 cf = mk(floorf(cp.x), floorf(cp.y), floorf(cp.z));
-                const int px = (int)cf.x, py = (int)cf.y, pz = (int)cf.z;
-                const f3 fr = cp - cf;
-                const int pxo = px + (fr.x < 0.5f ? -1 : 1), pyo = py + (fr.y < 0.5f ? -1 : 1),
-                          pzo = pz + (fr.z < 0.5f ? -1 : 1);
-                const float rr = G.radius * G.radius;
-                for (int j = 0; j < 8; j++) {
-                    const int cx = (j & 4) ? pxo : px, cy = (j & 2) ? pyo : py, cz = (j & 1) ? pzo : pz;
-                    unsigned long long guard = 0;
-                    for (int k = __ldg(&G.head[grid_bucket(G, cx, cy, cz)]); k >= 0 && guard++ < npts;
-                         k = __ldg(&P.next[k])) {
-                        const uint2 pt = P.pts[k];
-                        const float dist = length(q - xyz(__ldg(P.light.at(pt.x, (int)pt.y))));
-                        if (!(dist * dist <= rr)) continue;
-                        surf = surf + (ell ? ppm_photon_ellipse(S, P, (uint32_t)k, out, G.radius, ex, ey, ratio,
-                                                                sumw, count)
-                                           : ppm_photon(S, P, (uint32_t)k, out, G.radius));
-                    }
+        if (!merged) {
+            if constexpr (MEDIA) {
+                if (prev.inside >= 0 && is_volume(S, prev.inside) && nseg < NSEG)
+                    seg[nseg++] = PpmSeg{prev.o, prev.d, max_eps(length(prev.o - next.o)), prev.inside, prev.contact};
+            }
+            if (emissive(S, next.contact)) {
+                surf = next.rad;
+                merged = true;
+            } else if (next.contact >= 0 && obj_type(S, next.contact) == WR_MAT_DIFFUSE) {  // nonSpecular()
+                PRay out = next;
+                out.d = -prev.d;
+                // reached through an anisotropic record: the elliptic estimate
+                f3 ex = mk(0, 0, 0), ey = mk(0, 0, 0);
+                float ratio = 1.f;
+                const bool ell = prev.contact >= 0 && obj_type(S, prev.contact) == WR_MAT_ANISO &&
+                                 ellipse_frame(pdir, prev.cnorm, prev.d, next.cnorm, __ldg(&S.objs[prev.contact].nu),
+                                               __ldg(&S.objs[prev.contact].nv), ex, ey, ratio) == 0;
+                double sumw = 0.0;
+                int count = 0;
+                ppm_grid_walk(P, G, next.o, [&](uint32_t k) {
+                    surf = surf + (ell ? ppm_photon_ellipse(S, P, k, out, G.radius, ex, ey, ratio, sumw, count)
+                                       : ppm_photon(S, P, k, out, G.radius));
+                });
+                if (ell) {  // Query::weightScale (photonMap.cpp:300-302): vec3f /= float
+                    const float d = (float)(sumw / count);
+                    if (d != 0.f) surf = mk(surf.x / d, surf.y / d, surf.z / d);
                 }
+                merged = true;
             }
-            if (ell) {  // Query::weightScale (photonMap.cpp:300-302): vec3f /= float
-                const float d = (float)(sumw / count);
-                if (d != 0.f) surf = mk(surf.x / d, surf.y / d, surf.z / d);
-            }
-            break;
+            if (merged && nseg == 0) break;  // no march: nothing left to draw for
         }
         if (ended) break;
         st.set_top(next.inside);
@@ -1355,9 +1446,39 @@ __global__ void __launch_bounds__(128) k_ppm_eye(RenderScene S, BptParams P, uns
         prev = next;
         set_hit(S, prev, h);
     }
+    f3 Tr = mk(1, 1, 1), vol = mk(0, 0, 0);
+    if constexpr (MEDIA) {
+        const HvCtx hc = hv_ctx(P);
+        const GridView V = grid_view(P, P.nslots + slot);
+        for (int k = 0; k < nseg; k++) {
+            PRay vr = ray_default();
+            vr.o = seg[k].o;
+            vr.d = seg[k].d;
+            vr.inside = seg[k].inside;
+            vr.contact = seg[k].contact;
+            // N = dist / stepSize steps (at least 1; bounded), from a random offset
+            const float nf = seg[k].dist / __ldg(&S.objs[vr.inside].step_size);
+            int N = nf < (float)(1 << 24) ? (int)nf : (1 << 24);
+            if (N == 0) N++;
+            const float step = seg[k].dist / (float)N;
+            const float offset = step * g.next();
+            float t = offset;
+            Tr = vmul(Tr, bpt_decay<HM>(S, vr, offset, hc));
+            for (int j = 0; j < N; j++, t += step) {
+                PRay out = vr;
+                out.d = -vr.d;
+                out.o = vr.o + vr.d * t;
+                out.contact = -1;
+                f3 c = mk(0, 0, 0);
+                ppm_grid_walk(P, V, out.o, [&](uint32_t kk) { c = c + ppm_photon(S, P, kk, out, V.radius, true); });
+                Tr = vmul(Tr, bpt_decay<HM>(S, out, step, hc));
+                vol = vol + vmul(c, Tr) * step;
+            }
+        }
+    }
     // color = Tr * SurfaceColor + VolumeColor, times eyeMergePath[0]'s factors (photonMap.cpp:614-623)
     const f3 f = divs(divs(cam.rad * cos_term(S, cam), cam.dP), cam.oP);
-    const f3 c = vmul(surf, f);
+    const f3 c = vmul(vmul(Tr, surf) + vol, f);
     float* fl = P.film + 3 * ((size_t)slot * P.npix + pixel);
     fl[0] += c.x;
     fl[1] += c.y;
@@ -1411,7 +1532,7 @@ float vcm_radius(float base, uint32_t s) {
 
 int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& RP, uint32_t spp_offset,
                          uint32_t spp, float* d_sum, float* d_sumsq, unsigned int* err, cudaStream_t stream,
-                         int kind, float base_radius, bool hetero) {
+                         int kind, float base_radius, bool hetero, bool media) {
     if (RP.max_path_len + 2 > (uint32_t)BPT_MAX_RECORDS)
         return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "bidirectional mode: max_path_len is limited to 30");
     const bool vcm = kind == BIDIR_VCM, ppm = kind == BIDIR_PHOTON_MAP, grid_on = vcm || ppm;
@@ -1421,8 +1542,10 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
     const uint32_t nrec = RP.max_path_len + 2;
     // a batch of whole samples-per-pixel: vertex records of both sub-paths
     // (64 B each), the counts, the lists and the batch's images in about 1 GiB
+    const bool vol_grid = ppm && media;  // photon mapping's second grid, for the volume photons
+    const uint32_t ngrid = vol_grid ? 2u : 1u;
     const size_t per_sample = (ppm ? 1ull : 2ull) * nrec * 64 + 4 + 12 + (ppm ? 0 : 16ull * nrec * (nrec + 1)) +
-                              (grid_on ? 12ull * nrec + 4 : 0) + (vcm ? 128 : 0) + (ppm ? 16ull * nrec : 0);
+                              (grid_on ? 12ull * nrec + 4ull * ngrid : 0) + (vcm ? 128 : 0) + (ppm ? 16ull * nrec : 0);
     const uint64_t max_samples = std::max<uint64_t>(npix, (1ull << 30) / per_sample);
     const uint32_t per_batch = (uint32_t)std::min<uint64_t>(spp, std::max<uint64_t>(1, max_samples / npix));
     const uint64_t nsamp = (uint64_t)npix * per_batch;
@@ -1460,12 +1583,14 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
     P.vis = st.vis.as<uint2>();
     P.vcm = vcm;
     P.light_only = ppm;
+    P.vol_grid = vol_grid;
+    P.nslots = 1;
     if (grid_on) {
         WR_CUDA(ctx, st.pts.reserve(8ull * nrec * nsamp));
         WR_CUDA(ctx, st.next.reserve(4ull * nrec * nsamp));
-        WR_CUDA(ctx, st.head.reserve(4ull * nsamp));
-        WR_CUDA(ctx, st.bbox.reserve(24ull * per_batch));
-        WR_CUDA(ctx, st.radii.reserve(4ull * per_batch));
+        WR_CUDA(ctx, st.head.reserve(4ull * ngrid * nsamp));
+        WR_CUDA(ctx, st.bbox.reserve(24ull * ngrid * per_batch));
+        WR_CUDA(ctx, st.radii.reserve(4ull * ngrid * per_batch));
         P.pts = st.pts.as<uint2>();
         P.next = st.next.as<int>();
         P.head = st.head.as<int>();
@@ -1490,12 +1615,14 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
     const auto k_connect = hetero ? k_bpt_connect<true> : k_bpt_connect<false>;
     const auto k_merge = hetero ? k_vcm_merge<true> : k_vcm_merge<false>;
     const auto k_eval = hetero ? k_vcm_eval<true> : k_vcm_eval<false>;
+    const auto k_tput = hetero ? k_ppm_tput<true> : k_ppm_tput<false>;
+    const auto k_eye = !media ? k_ppm_eye<false, false> : hetero ? k_ppm_eye<true, true> : k_ppm_eye<true, false>;
     const int block = 128;
     const size_t smem = (size_t)RP.stack_cap * block * sizeof(uint32_t);
     if (smem > 48 * 1024) {
         WR_CUDA(ctx, cudaFuncSetAttribute(k_subpaths, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         WR_CUDA(ctx, cudaFuncSetAttribute(k_bpt_visible, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        WR_CUDA(ctx, cudaFuncSetAttribute(k_ppm_eye, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        WR_CUDA(ctx, cudaFuncSetAttribute(k_eye, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     }
     int per_sm = 0, per_sm_v = 0;
     WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_connect, block, 0));
@@ -1515,12 +1642,14 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
         WR_CUDA(ctx, cudaMemsetAsync(P.ncand, 0, 5 * sizeof(unsigned long long), stream));
         k_subpaths<<<subpath_grid, block, smem, stream>>>(S, P, err);
         WR_CUDA(ctx, cudaGetLastError());
-        if (grid_on) {  // the batch's hash grids: one per slot (iteration)
-            st.h_radii.resize(b);
-            for (uint32_t k = 0; k < b; k++) st.h_radii[k] = vcm_radius(base_radius, P.s0 + k);
-            WR_CUDA(ctx, cudaMemcpyAsync(st.radii.p, st.h_radii.data(), 4ull * b, cudaMemcpyHostToDevice, stream));
-            WR_CUDA(ctx, cudaMemsetAsync(P.bbox, 0, 24ull * b, stream));
-            WR_CUDA(ctx, cudaMemsetAsync(P.head, 0xff, 4ull * P.nsamp, stream));
+        if (grid_on) {  // the batch's hash grids: one per slot (iteration), a second one for volume photons
+            P.nslots = b;
+            st.h_radii.resize((size_t)ngrid * b);
+            for (uint32_t k = 0; k < ngrid * b; k++) st.h_radii[k] = vcm_radius(base_radius, P.s0 + k % b);
+            WR_CUDA(ctx, cudaMemcpyAsync(st.radii.p, st.h_radii.data(), 4ull * ngrid * b, cudaMemcpyHostToDevice,
+                                         stream));
+            WR_CUDA(ctx, cudaMemsetAsync(P.bbox, 0, 24ull * ngrid * b, stream));
+            WR_CUDA(ctx, cudaMemsetAsync(P.head, 0xff, 4ull * ngrid * P.nsamp, stream));
             k_vcm_points<<<grid, block, 0, stream>>>(S, P);
             WR_CUDA(ctx, cudaGetLastError());
             k_vcm_link<<<stride_grid, 256, 0, stream>>>(P);
@@ -1528,9 +1657,9 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
             ctx->kernel_launches += 2;
         }
         if (ppm) {
-            k_ppm_tput<<<stride_grid, 256, 0, stream>>>(S, P);
+            k_tput<<<stride_grid, 256, 0, stream>>>(S, P);
             WR_CUDA(ctx, cudaGetLastError());
-            k_ppm_eye<<<grid, block, smem, stream>>>(S, P, err);
+            k_eye<<<grid, block, smem, stream>>>(S, P, err);
             WR_CUDA(ctx, cudaGetLastError());
             ctx->kernel_launches += 2;
         } else {

@@ -115,6 +115,8 @@ int wr_scene_upload(wr_ctx* ctx, const wr_scene_desc* d, wr_scene_id* out) {
     if ((d->num_objects && !d->objects) || (d->num_vertices && !d->vertices) || (d->num_triangles && !d->triangles) ||
         (d->num_grids && !d->grids))
         return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "null scene array");
+    // the bidirectional renderers' vertex records hold an object id in 28 bits
+    if (d->num_objects > (1u << 27)) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "more than 2^27 objects");
     WR_GUARD_BEGIN
     // validate object ranges (Scene::buildKDTree trusts its objects; this boundary does not)
     uint64_t tri_sum = 0;

@@ -246,15 +246,18 @@ int wr_render_device(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, fl
         P.stack_cap = (int)sc->tree.max_depth + 3;
         const uint64_t npix = (uint64_t)rd->S.cam.width * rd->S.cam.height;
         if (desc->mode == WR_MODE_BIDIRECTIONAL || desc->mode == WR_MODE_VCM || desc->mode == WR_MODE_PHOTON_MAP) {
-            if (desc->mode == WR_MODE_PHOTON_MAP && rd->has_media)
-                return set_error(ctx, WR_ERR_UNSUPPORTED,
-                                 "photon-mapping mode: participating media (volume photons) are not supported");
+            if (desc->mode == WR_MODE_PHOTON_MAP && rd->has_media)  // the march step of each medium's segments
+                for (const wr_object_desc& m : sc->objects)
+                    if ((m.type == WR_MAT_HOMOGENEOUS || m.type == WR_MAT_HETEROGENEOUS) &&
+                        !(m.step_size > 0.f && m.step_size < 3.0e38f))
+                        return set_error(ctx, WR_ERR_INVALID_ARGUMENT,
+                                         "photon-mapping mode: a medium's step_size must be positive and finite");
             if (desc->flags & WR_RENDER_NEE)
                 return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "bidirectional / VCM / photon-mapping mode has no NEE switch");
             const int kind = desc->mode == WR_MODE_VCM ? BIDIR_VCM
                            : desc->mode == WR_MODE_PHOTON_MAP ? BIDIR_PHOTON_MAP : BIDIR_BPT;
             return render_bidirectional(ctx, rd->S, P, desc->spp_offset, desc->spp, d_sum, d_sumsq, err, s, kind,
-                                        desc->radius > 0.f ? desc->radius : 0.01f, rd->has_hetero);
+                                        desc->radius > 0.f ? desc->radius : 0.01f, rd->has_hetero, rd->has_media);
         }
         if (desc->mode == WR_MODE_WAVEFRONT) {
             rc = render_wavefront(ctx, *rd, P, desc->spp_offset, desc->spp, d_sum, d_sumsq, s);

@@ -33,10 +33,11 @@ cudaError_t launch_megakernel(const RenderScene& S, const RenderParams& P, float
 // samples [spp_offset, spp_offset + spp) of every pixel to d_sum (and their
 // squares to d_sumsq, may be NULL); `base_radius` is the merge / photon
 // radius of the first iteration; `hetero`: the scene has a heterogeneous
-// medium (its integrals are marched inside the weights)
+// medium (its integrals are marched inside the weights); `media`: it has a
+// participating medium (photon mapping's volume photons and marched segments)
 enum : int { BIDIR_BPT = 0, BIDIR_VCM = 1, BIDIR_PHOTON_MAP = 2 };
 int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& P, uint32_t spp_offset, uint32_t spp,
                          float* d_sum, float* d_sumsq, unsigned int* err, cudaStream_t stream, int kind = BIDIR_BPT,
-                         float base_radius = 0.01f, bool hetero = false);
+                         float base_radius = 0.01f, bool hetero = false, bool media = false);
 
 }  // namespace wr

@@ -100,7 +100,10 @@ struct PRay {
     int contact;    // object, CAMERA_OBJ or -1
     f3 cnorm;       // contact normal (valid when contact != -1)
     bool delta;     // isDeltaDirection (read by the bidirectional renderer only)
+    uint8_t ptype;  // Ray::photonType (ray.h:12; read by photon mapping only)
 };
+// Ray::PhotonType
+constexpr uint8_t PT_INVOL = 0, PT_OUTVOL = 1, PT_NOUSE = 2, PT_HITVOL = 3;
 
 __device__ __forceinline__ PRay ray_default() {
     PRay r;
@@ -116,6 +119,7 @@ __device__ __forceinline__ PRay ray_default() {
     r.contact = -1;
     r.cnorm = mk(0, 0, 0);
     r.delta = false;
+    r.ptype = PT_OUTVOL;
     return r;
 }
 
@@ -509,6 +513,7 @@ __device__ __forceinline__ PRay medium_enter(const RenderScene& S, int self, con
     out.cnorm = N;
     out.delta = true;  // every boundary outcome is a delta direction (homogeneousVolume.cpp:45-80)
     const Fresnel f = fresnel_split(N, in.d, cn, nn);
+    out.ptype = PT_NOUSE;
     if (f.tir) {
         out.d = f.refl;
         out.inside = in.inside;
@@ -524,6 +529,7 @@ __device__ __forceinline__ PRay medium_enter(const RenderScene& S, int self, con
         out.rad = out.rad * ((1.f - f.er) / cos_term(S, out));
         out.dP = 1.f - f.er;
         out.inside = self;
+        out.ptype = PT_HITVOL;
     }
     out.d = normalize(out.d);
     return out;
@@ -552,6 +558,7 @@ __device__ __forceinline__ PRay medium_exit(const RenderScene& S, int self, cons
     const float cn = obj_ior(S, self), nn = curOut >= 0 ? obj_ior(S, curOut) : 1.f;
     out.iobj = -1;
     out.delta = true;  // every boundary outcome is a delta direction (homogeneousVolume.cpp:141-186)
+    out.ptype = PT_NOUSE;
     const Fresnel f = fresnel_split(N, in.d, cn, nn);
     if (f.tir) {
         out.d = f.refl;
@@ -593,6 +600,7 @@ __device__ __forceinline__ PRay scatter_homogeneous(const RenderScene& S, int se
         out.o = in.o + in.d * sampDist;
         out.rad = hg_sample(__ldg(&m->g), in.d, g, out.d, out.dP);
         out.inside = self;
+        out.ptype = PT_INVOL;
         const float albedo = luminance(ss) / lt;
         const f3 pm = mk(st_.x * expf(-st_.x * sampDist), st_.y * expf(-st_.y * sampDist), st_.z * expf(-st_.z * sampDist));
         if (g.next() < albedo) {
@@ -654,6 +662,7 @@ __device__ __forceinline__ PRay scatter_heterogeneous(const RenderScene& S, int 
         out.o = in.o + in.d * t;
         out.rad = hg_sample(__ldg(&m->g), in.d, g, out.d, out.dP);
         out.inside = self;
+        out.ptype = PT_INVOL;
         const float albedo = luminance(ss) / luminance(st_);
         if (g.next() < albedo) {
             out.contact = -1;
@@ -741,13 +750,15 @@ __device__ __forceinline__ float hv_dens_poly(float temp, float n1, float n2, fl
 // findDesiredIntegralDensity (HeterogeneousVolume.cpp:258-344) along the ray
 // of `in`, a record inside the medium: Simpson steps of at most 2 stepSize up
 // to its hit (the reference's check() traces the same ray under the same
-// NoSelfCondition, so its first hit is in.idist), then Newton-bisection on the
-// step's quadratic.  0 found, 2 Newton stopped after 30 iterations (both with
-// t, the integral and the density at t), 1 no hit, 3 no progress, 4 not reached.
+// NoSelfCondition, so its first hit is in.idist; chk >= 0 gives check()'s
+// distance where it differs, 0 for a failed check), then Newton-bisection on
+// the step's quadratic.  0 found, 2 Newton stopped after 30 iterations (both
+// with t, the integral and the density at t), 1 no hit, 3 no progress, 4 not
+// reached.
 static __device__ __noinline__ int hv_find_ref(const RenderScene& S, int self, const PRay& in, float desired,
-                                               float& t, float& integ, float& dAtT) {
-    if (!(in.iobj >= 0 && in.idist > 0.f)) return 1;
-    const float dist = in.idist;
+                                               float& t, float& integ, float& dAtT, float chk) {
+    if (chk >= 0.f ? !(chk > 0.f) : !(in.iobj >= 0 && in.idist > 0.f)) return 1;
+    const float dist = chk >= 0.f ? chk : in.idist;
     integ = 0.f;
     f3 p = in.o;
     const unsigned n = (unsigned)ceilf(dist / (2.f * __ldg(&S.objs[self].step_size)));
@@ -799,7 +810,7 @@ static __device__ __noinline__ int hv_find_ref(const RenderScene& S, int self, c
 // densities (the unidirectional kernels use delta tracking).
 static __device__ __noinline__ PRay scatter_heterogeneous_ref(const RenderScene& S, int self, const PRay& in,
                                                               PathRng& g, InsideStack& st, bool* delegate,
-                                                              float* psurf) {
+                                                              float* psurf, float chk = -1.f) {
     const wr_object_desc* m = &S.objs[self];
     *delegate = false;
     const bool go_in = in.iobj == self && in.inside != self;
@@ -808,7 +819,7 @@ static __device__ __noinline__ PRay scatter_heterogeneous_ref(const RenderScene&
     const f3 ss = ld3(m->sigma_s), st_ = ss + ld3(m->sigma_a);
     const float desired = (float)(-log(1.0 - (double)g.next()) / (double)luminance(st_));
     float t = 0.f, integ = 0.f, dAtT = 0.f;
-    const int flag = be_in ? hv_find_ref(S, self, in, desired, t, integ, dAtT) : 1;
+    const int flag = be_in ? hv_find_ref(S, self, in, desired, t, integ, dAtT, chk) : 1;
     const float expVal = expf(-integ);
     const bool ok = flag == 0 || flag == 2;
     if (be_in && ok) {
@@ -816,6 +827,7 @@ static __device__ __noinline__ PRay scatter_heterogeneous_ref(const RenderScene&
         out.o = in.o + in.d * t;
         out.rad = hg_sample(__ldg(&m->g), in.d, g, out.d, out.dP);
         out.inside = self;
+        out.ptype = PT_INVOL;
         const float albedo = luminance(ss) / luminance(st_);
         if (g.next() < albedo) {
             out.contact = -1;
@@ -847,6 +859,7 @@ static __device__ __forceinline__ PRay scatter(const RenderScene& S, int self, c
                                             InsideStack& st) {
     PRay cur = in;
     float oP_scale = 1.f;
+    int medium_hit = -1;  // the object a medium handed over to (photonType, homogeneousVolume.cpp:192-194)
     for (int hop = 0; hop < 4; hop++) {
         const uint32_t type = obj_type(S, self);
         bool del = false;
@@ -874,10 +887,12 @@ static __device__ __forceinline__ PRay scatter(const RenderScene& S, int self, c
         if (del) {  // medium hands over to the surface it hit: scatter there, oP *= P_surface
             oP_scale *= ps;
             self = cur.iobj;
+            medium_hit = self;
             cur = out;
             continue;
         }
         out.oP *= oP_scale;
+        if (medium_hit >= 0) out.ptype = is_volume(S, medium_hit) ? PT_NOUSE : PT_OUTVOL;
         return out;
     }
     PRay dead = ray_default();
