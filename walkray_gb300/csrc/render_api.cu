@@ -277,6 +277,12 @@ int wr_render_device(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, fl
     }
 }
 
+// the film's sum over samples times 1/spp, in place (grid-stride)
+__global__ void k_scale(float* __restrict__ a, size_t n, float s) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        a[i] *= s;
+}
+
 int wr_render(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, float* rgb_out) {
     if (!ctx || !desc || !rgb_out) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "null argument");
     SceneGPU* sc = find_scene(ctx, id);
@@ -284,7 +290,9 @@ int wr_render(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, float* rg
     try {
         WR_CUDA(ctx, cudaSetDevice(ctx->device));
         const size_t n = 3ull * sc->camera.width * sc->camera.height;
-        DeviceBuffer film;
+        // the context's film (grown when a larger image comes; a context is
+        // used by one thread at a time), the mean taken on the device
+        DeviceBuffer& film = ctx->film;
         WR_CUDA(ctx, film.reserve(sizeof(float) * std::max<size_t>(n, 1)));
         cudaStream_t s = ctx->stream;
         unsigned int* err = reinterpret_cast<unsigned int*>(ctx->scratch_words.as<unsigned long long>() + 1);
@@ -292,13 +300,15 @@ int wr_render(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, float* rg
         WR_CUDA(ctx, cudaMemsetAsync(film.p, 0, sizeof(float) * n, s));
         int rc = wr_render_device(ctx, id, desc, film.as<float>(), nullptr, s);
         if (rc != WR_OK) return rc;
+        const float inv = desc->spp ? 1.0f / (float)desc->spp : 0.f;
+        k_scale<<<(unsigned)std::min<size_t>((n + 255) / 256, 65535), 256, 0, s>>>(film.as<float>(), n, inv);
+        WR_CUDA(ctx, cudaGetLastError());
+        ctx->kernel_launches++;
         WR_CUDA(ctx, cudaMemcpyAsync(rgb_out, film.p, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
         unsigned int herr = 0;
         WR_CUDA(ctx, cudaMemcpyAsync(&herr, err, sizeof herr, cudaMemcpyDeviceToHost, s));
         WR_CUDA(ctx, cudaStreamSynchronize(s));
         if (herr) return set_error(ctx, WR_ERR_INTERNAL, "traversal stack overflow");
-        const float inv = desc->spp ? 1.0f / (float)desc->spp : 0.f;
-        for (size_t i = 0; i < n; i++) rgb_out[i] *= inv;
         return WR_OK;
     } catch (const std::exception& ex) {
         return set_error(ctx, WR_ERR_INTERNAL, ex.what());

@@ -73,6 +73,7 @@ struct wr_ctx {
     uint32_t next_scene = 1;
     wr::DeviceBuffer rays, hits, inside, contact;
     wr::DeviceBuffer scratch_words;  // counters / error flags
+    wr::DeviceBuffer film;           // wr_render's image, kept between calls (no allocation per call)
     bool trace_prune = false;
     int last_trace_blocks = 0;
     uint64_t kernel_launches = 0;  // kernels this library has launched on the context
