@@ -183,3 +183,30 @@ def test_device_entry_point_matches_host_entry_point(ctx):
     assert np.array_equal(got[:, 0], want["tri"])
     assert np.array_equal(got[:, 1], want["t"].view(np.uint32))
     ctx.release(sid)
+
+
+def test_large_filtered_host_batch_matches_device_entry_point(ctx):
+    """4.5 M filtered rays through the host-buffer entry point: the same hits
+    as the device-buffer entry point."""
+    torch = pytest.importorskip("torch")
+    s = make_golden.golden_scenes()["mixed_l2"]
+    n = 4_500_000
+    rays = S.kd_rays(s, n, seed=21)
+    rng = np.random.default_rng(21)
+    ids = rng.integers(-1, len(s.objects), size=(n, 2)).astype(np.int32)
+    sid = ctx.upload(s)
+    want = ctx.trace_closest(sid, rays, ids[:, 0], ids[:, 1])
+    d_rays = torch.from_numpy(rays).cuda()
+    d_in = torch.from_numpy(np.ascontiguousarray(ids[:, 0])).cuda()
+    d_ct = torch.from_numpy(np.ascontiguousarray(ids[:, 1])).cuda()
+    d_hits = torch.empty((n, 4), dtype=torch.int32, device="cuda")
+    ctx.trace_closest_device(sid, d_rays.data_ptr(), n, d_hits.data_ptr(),
+                             stream=torch.cuda.current_stream().cuda_stream, d_inside=d_in.data_ptr(),
+                             d_contact=d_ct.data_ptr())
+    torch.cuda.synchronize()
+    got = d_hits.cpu().numpy().view(np.uint32)
+    assert np.array_equal(got[:, 0], want["tri"])
+    assert np.array_equal(got[:, 1], want["t"].view(np.uint32))
+    assert (want["tri"] != NO_HIT).mean() > 0.05
+    ctx.release(sid)
+

@@ -97,6 +97,7 @@ int wr_ctx_destroy(wr_ctx* ctx) {
     ctx->inside.release();
     ctx->contact.release();
     ctx->scratch_words.release();
+    ctx->film.release();
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return WR_OK;
@@ -267,15 +268,17 @@ int wr_trace_closest(wr_ctx* ctx, wr_scene_id id, const float* rays, uint64_t n,
         WR_CUDA(ctx, ctx->contact.reserve(n * sizeof(int32_t)));
     }
     cudaStream_t s = ctx->stream;
+    unsigned long long* counter = ctx->scratch_words.as<unsigned long long>();
+    unsigned int* err = reinterpret_cast<unsigned int*>(counter + 1);
+    WR_CUDA(ctx, cudaMemsetAsync(err, 0, sizeof(unsigned int), s));
+    const TraceTune tt = trace_tune_of(ctx);
     WR_CUDA(ctx, cudaMemcpyAsync(ctx->rays.p, rays, n * 6 * sizeof(float), cudaMemcpyHostToDevice, s));
     if (filtered) {
         WR_CUDA(ctx, cudaMemcpyAsync(ctx->inside.p, filter->inside_obj, n * 4, cudaMemcpyHostToDevice, s));
         WR_CUDA(ctx, cudaMemcpyAsync(ctx->contact.p, filter->contact_obj, n * 4, cudaMemcpyHostToDevice, s));
     }
-    unsigned long long* counter = ctx->scratch_words.as<unsigned long long>();
-    unsigned int* err = reinterpret_cast<unsigned int*>(counter + 1);
-    WR_CUDA(ctx, cudaMemsetAsync(err, 0, sizeof(unsigned int), s));
-    const TraceTune tt = trace_tune_of(ctx);
+    // one launch after the whole copy: copies running beside the traversal
+    // stream through the L2 that holds the tree and slow it more than they save
     WR_CUDA(ctx, launch_trace_closest(sc->tree, ctx->rays.as<float>(), n, filtered ? ctx->inside.as<int32_t>() : nullptr,
                                       filtered ? ctx->contact.as<int32_t>() : nullptr, ctx->hits.as<wr_hit>(), counter,
                                       err, ctx->num_sms, ctx->trace_prune, s, &ctx->last_trace_blocks, &tt,
