@@ -230,7 +230,7 @@ static ExtendKernel extend_kernel(int ctas_per_sm, bool stats) {
 }
 
 // shade: one bounce per path; survivors compacted into Y, finished paths to the film
-__global__ void __launch_bounds__(128) k_wf_shade(const RenderScene* __restrict__ scenes,
+__global__ void __launch_bounds__(128, 4) k_wf_shade(const RenderScene* __restrict__ scenes,
                                                     const WfJob* __restrict__ jobs,
                                                     WfJobCounters* __restrict__ counters, WfSide X,
                                                     const int2* __restrict__ hits, WfSide Y, WfShadow Q, WfSort B,
