@@ -16,7 +16,7 @@ extern "C" {
 int wr_set_wavefront_config(wr_ctx* ctx, const wr_wavefront_config* cfg) {
     if (!ctx || !cfg) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "null argument");
     if (cfg->capacity < 1024 || cfg->capacity > (1u << 25) || (cfg->extend_block % 32) || (cfg->shade_block % 32) ||
-        cfg->extend_block <= 0 || cfg->extend_block > 128 || cfg->shade_block <= 0 || cfg->shade_block > 1024 ||
+        cfg->extend_block <= 0 || cfg->extend_block > 128 || cfg->shade_block <= 0 || cfg->shade_block > 128 ||
         cfg->iters_per_graph <= 0 || cfg->iters_per_graph > 64 || cfg->ctas_per_sm < 0 || cfg->refill_min < 0 ||
         cfg->refill_min > 32 || cfg->leaf_min < 0 || cfg->leaf_min > 32 || cfg->drain_paths < 0)
         return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "wavefront configuration out of range");
@@ -44,7 +44,7 @@ int wr_autotune(wr_ctx* ctx, wr_scene_id scene, uint32_t spp_per_trial, uint32_t
     std::vector<wr_wavefront_config> cands;
     for (uint32_t cap : {1u << 19, 1u << 20, 1u << 21, 1u << 22})
         for (int eb : {64, 128})
-            for (int sb : {128, 256})
+            for (int sb : {64, 128})  // the shade / generate kernels are built for at most 128 threads
                 for (int it : {2, 8}) cands.push_back(wr_wavefront_config{cap, eb, sb, 0, it, 0, 0, 0, 0.0});
     cudaEvent_t a, b;
     WR_CUDA(ctx, cudaEventCreate(&a));
