@@ -826,8 +826,11 @@ __device__ void bpt_connect_one(const RenderScene& S, const BptParams& P, uint32
 
 // persistent: the grid strides over the contributing connections, 32
 // consecutive ones (mostly one (l, e) pair) per warp
-template <bool HM>
-__global__ void __launch_bounds__(128) k_bpt_connect(RenderScene S, BptParams P) {
+// MINB: resident blocks per SM the registers are fitted to (5 for the
+// bidirectional weights: 96 registers, +5 % over 4 blocks; VCM's weights
+// spill at that size and take 4; the marching instantiation 1)
+template <bool HM, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_bpt_connect(RenderScene S, BptParams P) {
     const unsigned long long total = P.ncand[1];
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
          i += (unsigned long long)gridDim.x * blockDim.x) {
@@ -1612,7 +1615,7 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
     // scenes with a heterogeneous medium take the kernels that march its
     // integrals in the weights; the others compile without those calls
     const auto k_subpaths = hetero ? k_bpt_subpaths<true> : k_bpt_subpaths<false>;
-    const auto k_connect = hetero ? k_bpt_connect<true> : k_bpt_connect<false>;
+    const auto k_connect = hetero ? k_bpt_connect<true, 1> : vcm ? k_bpt_connect<false, 4> : k_bpt_connect<false, 5>;
     const auto k_merge = hetero ? k_vcm_merge<true> : k_vcm_merge<false>;
     const auto k_eval = hetero ? k_vcm_eval<true> : k_vcm_eval<false>;
     const auto k_tput = hetero ? k_ppm_tput<true> : k_ppm_tput<false>;
