@@ -1007,54 +1007,61 @@ __device__ void vcm_merge_one(const RenderScene& S, const BptParams& P, uint32_t
     contrib = contrib + divs(col * w, prob);
 }
 
-// One thread per sample: every non-delta eye vertex (before an emitter) is a
-// query of the hash grid (HashGrid::Process, hashgrid.hxx:97-161).  Each light
-// point within the radius is a merge, appended to the merge list for
-// k_vcm_eval; when the list is full the merge is evaluated here.  Each
-// merge's contribution / nVM goes to the sample's pixel (the reference adds a
-// query's sum / nVM: the same up to the order of the additions).
+// One thread per (sample, eye vertex): every non-delta eye vertex before the
+// sample's first emitter is a query of the hash grid (HashGrid::Process,
+// hashgrid.hxx:97-161); neighbouring lanes take neighbouring samples at the
+// same depth.  Each light point within the radius is a merge, appended to
+// the merge list for k_vcm_eval; when the list is full the merge is
+// evaluated here.  Each merge's contribution / nVM goes to the sample's pixel
+// (the reference adds a query's sum / nVM: the same up to the order of the
+// additions).
 template <bool HM>
 __global__ void __launch_bounds__(128) k_vcm_merge(RenderScene S, BptParams P) {
-    const uint32_t sid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sid >= P.nsamp) return;
+    const int nrec = (int)P.max_path_len + 2;
+    const unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (unsigned long long)P.nsamp * (unsigned long long)(nrec - 1)) return;
+    const uint32_t sid = (uint32_t)(t % P.nsamp);
+    const int i = 1 + (int)(t / P.nsamp);
     const int ne = (int)(__ldg(&P.counts[sid]) & 0xffu);
+    if (i >= ne) return;
+    // the sample's loop over its eye records stops at the first emitter (vcmTracer.cpp:213-215)
+    for (int j = 1; j <= i; j++) {
+        const uint32_t w = __float_as_uint(__ldg(P.eye.at(sid, j) + 3).w);
+        if (emissive(S, (int)(w & 0x0fffffffu) - 2)) return;
+    }
+    const PRay q = P.eye.get(sid, i);
+    if (q.delta) return;
     const uint32_t slot = sid / P.npix;
     const GridView G = grid_view(P, slot);
     const float rr = G.radius * G.radius;
     const unsigned long long npts = P.ncand[2];
     double rev[2 * BPT_MAX_RECORDS];
-    f3 own = mk(0, 0, 0);
-    for (int i = 1; i < ne; i++) {
-        const PRay q = P.eye.get(sid, i);
-        if (emissive(S, q.contact)) break;
-        if (q.delta) continue;
-        f3 contrib = mk(0, 0, 0);
-        const f3 dmin = q.o - G.bmin, dmax = G.bmax - q.o;
-        if (!(dmin.x < 0.f || dmin.y < 0.f || dmin.z < 0.f || dmax.x < 0.f || dmax.y < 0.f || dmax.z < 0.f)) {
-            const f3 cp = mk(G.inv_cell * dmin.x, G.inv_cell * dmin.y, G.inv_cell * dmin.z);
-            const f3 cf = mk(floorf(cp.x), floorf(cp.y), floorf(cp.z));
-            const int px = (int)cf.x, py = (int)cf.y, pz = (int)cf.z;
-            const f3 fr = cp - cf;
-            const int pxo = px + (fr.x < 0.5f ? -1 : 1), pyo = py + (fr.y < 0.5f ? -1 : 1),
-                      pzo = pz + (fr.z < 0.5f ? -1 : 1);
-            for (int j = 0; j < 8; j++) {
-                const int cx = (j & 4) ? pxo : px, cy = (j & 2) ? pyo : py, cz = (j & 1) ? pzo : pz;
-                // a list is at most every point of the batch long (bounded walk)
-                unsigned long long guard = 0;
-                for (int k = __ldg(&G.head[grid_bucket(G, cx, cy, cz)]); k >= 0 && guard++ < npts;
-                     k = __ldg(&P.next[k])) {
-                    const uint2 pt = P.pts[k];
-                    const f3 pos = xyz(__ldg(P.light.at(pt.x, (int)pt.y)));
-                    const float dist = length(q.o - pos);
-                    if (!(dist * dist <= rr)) continue;
-                    const unsigned long long m = atomicAdd(P.ncand + 3, 1ull);
-                    if (m < P.merge_cap) P.merges[m] = make_uint4(sid, (uint32_t)i, (uint32_t)k, 0u);
-                    else vcm_merge_one<HM>(S, P, sid, i, pt.x, (int)pt.y, rev, contrib);
-                }
+    f3 contrib = mk(0, 0, 0);
+    const f3 dmin = q.o - G.bmin, dmax = G.bmax - q.o;
+    if (!(dmin.x < 0.f || dmin.y < 0.f || dmin.z < 0.f || dmax.x < 0.f || dmax.y < 0.f || dmax.z < 0.f)) {
+        const f3 cp = mk(G.inv_cell * dmin.x, G.inv_cell * dmin.y, G.inv_cell * dmin.z);
+        const f3 cf = mk(floorf(cp.x), floorf(cp.y), floorf(cp.z));
+        const int px = (int)cf.x, py = (int)cf.y, pz = (int)cf.z;
+        const f3 fr = cp - cf;
+        const int pxo = px + (fr.x < 0.5f ? -1 : 1), pyo = py + (fr.y < 0.5f ? -1 : 1),
+                  pzo = pz + (fr.z < 0.5f ? -1 : 1);
+        for (int jc = 0; jc < 8; jc++) {
+            const int cx = (jc & 4) ? pxo : px, cy = (jc & 2) ? pyo : py, cz = (jc & 1) ? pzo : pz;
+            // a list is at most every point of the batch long (bounded walk)
+            unsigned long long guard = 0;
+            for (int k = __ldg(&G.head[grid_bucket(G, cx, cy, cz)]); k >= 0 && guard++ < npts;
+                 k = __ldg(&P.next[k])) {
+                const uint2 pt = P.pts[k];
+                const f3 pos = xyz(__ldg(P.light.at(pt.x, (int)pt.y)));
+                const float dist = length(q.o - pos);
+                if (!(dist * dist <= rr)) continue;
+                const unsigned long long m = atomicAdd(P.ncand + 3, 1ull);
+                if (m < P.merge_cap) P.merges[m] = make_uint4(sid, (uint32_t)i, (uint32_t)k, 0u);
+                else vcm_merge_one<HM>(S, P, sid, i, pt.x, (int)pt.y, rev, contrib);
             }
         }
-        own = own + divs(contrib, (float)P.npix);
     }
+    const f3 own = divs(contrib, (float)P.npix);
     if (own.x != 0.f || own.y != 0.f || own.z != 0.f)
         film_add(P.film + 3 * (size_t)P.npix * slot, sid % P.npix, own);
 }
@@ -1675,7 +1682,7 @@ int render_bidirectional(wr_ctx* ctx, const RenderScene& S, const RenderParams& 
             ctx->kernel_launches += 3;
         }
         if (vcm) {
-            k_merge<<<grid, block, 0, stream>>>(S, P);
+            k_merge<<<(unsigned)((P.nsamp * (unsigned long long)(nrec - 1) + block - 1) / block), block, 0, stream>>>(S, P);
             WR_CUDA(ctx, cudaGetLastError());
             k_eval<<<connect_grid, block, 0, stream>>>(S, P);
             WR_CUDA(ctx, cudaGetLastError());
