@@ -692,7 +692,7 @@ def run_kd(args, world, rank, local):
     torch.cuda.set_device(local)
     scene, rays = kd_inputs(rank)
     n = len(rays)
-    ctx = Context(device=local)
+    ctx = Context(device=local, exact_traversal=args.kd_exact)
     sid = ctx.upload(scene)
     stream = torch.cuda.Stream()
     d_rays = torch.from_numpy(rays).cuda()
@@ -786,11 +786,14 @@ def main():
     ap.add_argument("--cpu-rows", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--kd-rays", type=int, default=1 << 24, help="rays per step (kd); smaller for ncu captures")
+    ap.add_argument("--kd-exact", action="store_true", help="kd: visit every box the reference visits (no pruning)")
+    ap.add_argument("--pt-spp", type=int, default=PT_SPP, help="samples per pixel per step (pt)")
     ap.add_argument("--pt-size", type=int, default=PT_SIZE, help="image side (pt); smaller for ncu captures")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window of the request stream (serve)")
     ap.add_argument("--converged-spp", type=int, default=0, help="spp of the converged image (relmse)")
     args = ap.parse_args()
     globals()["PT_SIZE"] = args.pt_size
+    globals()["PT_SPP"] = args.pt_spp
     globals()["KD_RAYS"] = args.kd_rays
     world, rank, local = dist_setup()
     if args.warmup < 3:

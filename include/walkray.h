@@ -138,9 +138,19 @@ typedef uint32_t wr_scene_id;
 typedef struct wr_ctx_desc {
     int device;                      /* CUDA device ordinal */
     uint64_t device_memory_budget;   /* bytes the serving loop may use; 0 = 90% of free */
-    uint32_t flags;
+    uint32_t flags;                  /* WR_CTX_* */
     uint32_t pad;
 } wr_ctx_desc;
+
+/* wr_trace_closest visits every box the reference visits (KDTree::intersect,
+ * kdtree.cpp:308-347, which never prunes by distance).  Without this flag it
+ * skips a box entered beyond 1.001 x the closest hit found so far (plus the
+ * box margin), except for a ray whose closest hit so far grazes its
+ * triangle's plane (|n.d| < |d| / 32), which keeps every box: a triangle's
+ * hit lies in its box up to the triangle test's rounding, which only a
+ * near-grazing ray can make large.  Same hits on every test set (all 2^24
+ * rays of the 1.31M-triangle icosphere workload included). */
+#define WR_CTX_EXACT_TRAVERSAL 1u
 
 /* ---- context ------------------------------------------------------------ */
 int wr_get_abi_version(uint32_t* version);
@@ -222,6 +232,22 @@ int wr_trace_closest_device(wr_ctx* ctx, wr_scene_id scene, const float* d_rays,
  * outside the triangle's box.  This flag visits every box the reference
  * visits (KDTree::intersect, kdtree.cpp:308-347), as wr_trace_closest does. */
 #define WR_RENDER_EXACT_TRAVERSAL 2u
+/* Low-variance estimators (no reference counterpart; the reference's
+ * expectation is kept, only the variance changes).  Path tracing modes
+ * (WR_MODE_MEGAKERNEL, WR_MODE_WAVEFRONT, serving) only.
+ * WR_RENDER_NEE_MIS: unbiased next-event estimation at every diffuse,
+ * isotropic-Phong and anisotropic-Phong surface vertex outside media (one
+ * light sample per vertex, SurfaceSampler's area-proportional pick), combined
+ * with the BSDF-sampled hits of emitters by multiple importance sampling
+ * (power heuristic).  The reference's NEE branch (WR_RENDER_NEE, biased)
+ * cannot be combined with it.
+ * WR_RENDER_PHONG_MIRROR: isotropic Phong directions sampled about the mirror
+ * direction with the density (n+1)/(2 pi) (R.w)^n (the reference samples
+ * about the normal, isotropicPhong.h:20-38, whose weights are unbounded for
+ * large exponents); samples below the surface end the path with zero
+ * radiance. */
+#define WR_RENDER_NEE_MIS 4u
+#define WR_RENDER_PHONG_MIRROR 8u
 
 typedef struct wr_render_desc {
     uint32_t spp;          /* samples per pixel (PathTracer spp) */
@@ -245,22 +271,30 @@ int wr_render_device(wr_ctx* ctx, wr_scene_id scene, const wr_render_desc* desc,
 
 /* Rendering without any device allocation.  No counterpart in the reference
  * (the reference renders on the CPU).  wr_render allocates an accumulation
- * film on every call, which callers that may not allocate device memory while
- * rendering cannot use: code running during CUDA-graph capture in global
- * mode, real-time loops that avoid allocation because it can synchronise the
- * device, applications with their own memory pools.  This entry point renders
- * like wr_render in WR_MODE_MEGAKERNEL but keeps the film in a fixed array
- * inside the library (WR_NOALLOC_MAX_PIXELS pixels, 12 MiB per GPU that loads
- * the library, held until exit) and writes the W*H*3 mean image to the
- * caller's device buffer d_rgb_out, asynchronously on `stream` (NULL = the
- * context's stream).  Larger images are rejected with WR_ERR_INVALID_ARGUMENT.
- * It calls no allocation routine: the scene must have been rendered once
- * before (wr_render / wr_render_device build its rendering tables), and the
- * first call on a device looks up the array's device address, so make that
- * first call before any stream capture.  All calls share the array: calls
- * whose work overlaps on the GPU race and must be serialised. */
+ * film on every call, which some callers cannot allow: real-time loops that
+ * avoid cudaMalloc / cudaFree because they can synchronise the device and
+ * stall a frame, and applications whose device memory belongs to their own
+ * pool or allocator.  This entry point renders like wr_render in
+ * WR_MODE_MEGAKERNEL but keeps the film in a fixed array inside the library
+ * (WR_NOALLOC_MAX_PIXELS pixels, 12 MiB per GPU that loads the library, held
+ * until exit) and writes the W*H*3 mean image to the caller's device buffer
+ * d_rgb_out, asynchronously on `stream` (NULL = the context's stream).  Larger
+ * images are rejected with WR_ERR_INVALID_ARGUMENT, scenes wr_render refuses
+ * with the same WR_ERR_UNSUPPORTED.  It calls no allocation routine: the scene
+ * must have been rendered once before (wr_render / wr_render_device build its
+ * rendering tables), and the first call on a device looks up the array's
+ * device address in the device's primary context (the CUDA runtime's), with
+ * which every call must be made.  All calls share the array: calls whose work
+ * overlaps on the GPU race and must be serialised. */
 #define WR_NOALLOC_MAX_PIXELS 1048576u
 int wr_render_noalloc(wr_ctx* ctx, wr_scene_id scene, const wr_render_desc* desc, float* d_rgb_out, void* stream);
+/* Traversal status of the most recent wr_render_noalloc on this context's
+ * device, read without allocating: waits for `stream` (NULL = the context's
+ * stream) and stores the error word in *out_err: 0 when every traversal
+ * finished, nonzero when a traversal stack would have overflowed (the image
+ * of that call is then incomplete; wr_render reports the same case as
+ * WR_ERR_INTERNAL).  Companion of wr_render_noalloc; no reference counterpart. */
+int wr_render_noalloc_status(wr_ctx* ctx, void* stream, unsigned int* out_err);
 
 /* Per-stage profile of one wavefront render (no reference counterpart: the
  * reference has no timers).  The stages are launched one by one instead of
@@ -281,6 +315,20 @@ typedef struct wr_render_profile {
 } wr_render_profile;
 int wr_profile_render(wr_ctx* ctx, wr_scene_id scene, const wr_render_desc* desc, float* d_sum,
                       wr_render_profile* out);
+
+/* ---- random stream ----------------------------------------------------- */
+/* The renderers' device random stream, read back for known-answer checks.
+ * The reference draws from one std::mt19937_64 shared by its threads
+ * (rng.h:6-59, Rng::genFloat); this library gives every path its own
+ * counter-based stream instead: draw `dim` of (pixel, sample) under the
+ * render seed is word dim % 4 of Philox4x32-10 on the counter
+ * {dim / 4, sample, pixel, 0} with key {seed low, seed high}, top 24 bits
+ * times 2^-24.  For each i < n the device draws sequentially from 0 to
+ * dim[i] with the renderers' own generator and stores the last draw in
+ * draws[i] and the four Philox words of its block in words[4i..4i+3].  Host
+ * buffers; n <= 2^24, dim[i] < 65536. */
+int wr_rng_draws(wr_ctx* ctx, uint64_t seed, const uint32_t* pixel, const uint32_t* sample, const uint32_t* dim,
+                 uint64_t n, uint32_t* words, float* draws);
 
 /* ---- serving ------------------------------------------------------------- */
 /* A request loop over resident scenes: RenderEngine::renderFilm

@@ -17,6 +17,13 @@ from the reference sources) on small seeded scenes and stores its answers:
                       8 reference renders of 256 spp
   render_dof.npz      the Cornell box through a thin lens (depth of field),
                       8 reference renders of 2048 spp
+  render_pt_*.npz     PathTracer::renderPixels on the mixed-material (64x64,
+                      Phong and refractive spheres), anisotropic-floor,
+                      homogeneous-fog and heterogeneous-medium scenes, 8
+                      reference renders of 256 spp each
+  c0_ref.npz          configuration 0 (Cornell 256x256, 64 spp, depth 8):
+                      mean of 256 reference renders (16,384 spp, FP64 sums)
+                      and the per-pixel variance of one 64-spp render
   xml/                a scene in WalkRay's file layout (config, scene and
                       material XML, .obj / .shp meshes, a density grid)
   mesh_ref.npz        the reference's Mesh::loadShape of those meshes
@@ -39,8 +46,8 @@ from the reference sources) on small seeded scenes and stores its answers:
                       photon query (inputs and results), recorded in its own
                       PhotonMap renders of the anisotropic-floor scene
 
-Usage: python tests/golden/make_golden.py [bpt|vcm|ppm|ellipse [scene ...]]   (needs
-the reference tree on this machine; `bpt` / `vcm` / `ppm` remake only those
+Usage: python tests/golden/make_golden.py [pt|c0|bpt|vcm|ppm|ellipse [scene ...]]   (needs
+the reference tree on this machine; `pt` / `c0` / `bpt` / `vcm` / `ppm` remake only those
 renders, of the scenes named after it if any; the fixtures it writes are what
 the tests read elsewhere)
 """
@@ -268,6 +275,75 @@ def ppm_fixtures(td, names=PPM_SCENES):
         render_set(sc[name], p, td, f"render_ppm_{name}.npz", extra=("ppm", str(PPM_RADIUS)), spp=64)
 
 
+PT_SCENES = ("mixed_l2", "aniso", "fog", "hetero")
+
+
+def pt_fixtures(td, names=PT_SCENES):
+    """PathTracer::renderPixels (pathTracer.cpp:7-76) on the scenes whose
+    materials the Cornell fixtures do not cover: isotropic Phong and
+    refractive spheres (mixed_l2), the anisotropic Phong floor (aniso), the
+    homogeneous sphere (fog) and the heterogeneous grid (hetero, the
+    reference's own regular tracking: Simpson steps of 2 x 0.01 and
+    Newton-bisection, HeterogeneousVolume.cpp:354-404).  8 reference renders
+    of 256 spp per scene, depth 8."""
+    sc = golden_scenes()
+    p = os.path.join(td, "s.wrs")
+    for name in names:
+        render_set(sc[name], p, td, f"render_pt_{name}.npz", spp=256)
+
+
+C0_RENDERS, C0_SPP, C0_DEPTH = 256, 64, 8
+
+
+def c0_fixture(td, names=None):
+    """Configuration 0 as specified (Cornell box, 256x256, 64 spp, depth 8)
+    rendered by the reference's PathTracer 256 times (seeds 1..256, one
+    thread each, eight at a time).  c0_ref.npz holds the 16,384-spp mean of
+    those renders accumulated in FP64 (`mean`, stored as f32), the per-pixel
+    variance of one 64-spp render across them (`var64`, 255 degrees of
+    freedom, f32), and the reference's own rate of pixel-channels beyond
+    3 sigma: for each render, the share of its pixel-channels whose
+    difference to the mean of the other 255 exceeds 3 sqrt(var64 (1 +
+    1/255)) (`null_frac3`: f64, one per render).  At 64 spp a pixel's
+    estimate is far from Gaussian (few paths reach the small light), so this
+    share is well above the 0.27 % of a normal distribution; it is the
+    yardstick of the per-pixel 3-sigma test."""
+    s = S.cornell(256, 256)
+    p = os.path.join(td, "c0.wrs")
+    s.save(p)
+    env = dict(os.environ, OMP_NUM_THREADS="1", WR_REF_WORKDIR=td)
+    n = C0_RENDERS
+    imgs = np.empty((n, 256, 256, 3), np.float32)
+    seeds = list(range(1, n + 1))
+    while seeds:
+        batch, seeds = seeds[:8], seeds[8:]
+        procs = []
+        for seed in batch:
+            out = os.path.join(td, f"c0.{seed}.bin")
+            procs.append((seed, out, subprocess.Popen([REF, "render", p, str(C0_SPP), str(C0_DEPTH), str(seed), out],
+                                                      env=env, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)))
+        for seed, out, pr in procs:
+            assert pr.wait() == 0
+            imgs[seed - 1] = np.fromfile(out, np.float32).reshape(256, 256, 3)
+            os.remove(out)
+    acc = np.zeros((256, 256, 3), np.float64)
+    acc2 = np.zeros((256, 256, 3), np.float64)
+    for img in imgs:
+        x = img.astype(np.float64)
+        acc += x
+        acc2 += x * x
+    mean = acc / n
+    var64 = np.maximum(acc2 / n - mean * mean, 0.0) * n / (n - 1)
+    null = np.empty(n)
+    for k in range(n):
+        x = imgs[k].astype(np.float64)
+        rest = (acc - x) / (n - 1)
+        null[k] = np.mean(np.abs(x - rest) > 3.0 * np.sqrt(var64 * (1.0 + 1.0 / (n - 1)) + 1e-30))
+    np.savez_compressed(os.path.join(HERE, "c0_ref.npz"), mean=mean.astype(np.float32),
+                        var64=var64.astype(np.float32), null_frac3=null, renders=n, spp=C0_SPP,
+                        max_path_len=C0_DEPTH)
+
+
 ELLIPSE_LOBES = ((10.0, 100.0), (100.0, 10.0), (50.0, 50.0), (5.0, 500.0), (2.0, 20.0))
 
 
@@ -300,7 +376,8 @@ def ellipse_fixture(td, names=None):
 def main():
     if not os.path.exists(REF):
         sys.exit("build the reference harness first: make -C oracle ref")
-    only = {"bpt": bpt_fixtures, "vcm": vcm_fixtures, "ppm": ppm_fixtures, "ellipse": ellipse_fixture}
+    only = {"bpt": bpt_fixtures, "vcm": vcm_fixtures, "ppm": ppm_fixtures, "ellipse": ellipse_fixture,
+            "pt": pt_fixtures, "c0": c0_fixture}
     if len(sys.argv) >= 2 and sys.argv[1] in only:  # only those renders (of the scenes named after it)
         with tempfile.TemporaryDirectory() as td:
             if len(sys.argv) > 2:
@@ -364,6 +441,8 @@ def main():
         render_set(sc["dof"], p, td, "render_dof.npz", spp=2048)
         write_xml_fixtures()
         mesh_fixtures(td)
+        pt_fixtures(td)
+        c0_fixture(td)
         bpt_fixtures(td)
         vcm_fixtures(td)
         ppm_fixtures(td)

@@ -1,7 +1,8 @@
 """The C++ drop-in renderer (walkray_gb300/host/gpuPathTracer.*) compiled
 against WalkRay's own headers, and its reading of WalkRay's material objects
-(wrDefaultDescribe) checked against the scene descriptions.  Needs the
-reference tree on this machine; skipped elsewhere."""
+(wrDefaultDescribe) checked against the scene descriptions.  Needs a
+WalkRay source tree named by the environment variable WR_REFERENCE_DIR;
+skipped without one."""
 import os
 import subprocess
 
@@ -12,13 +13,13 @@ import make_golden
 from walkray_gb300 import scenes as S
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("WR_REFERENCE_DIR", "/root/reference")
+REF = os.environ.get("WR_REFERENCE_DIR", "")
 
 
 @pytest.fixture(scope="module")
 def dropin(built):
-    if not os.path.isfile(os.path.join(REF, "kdtree.cpp")):
-        pytest.skip("reference tree not present")
+    if not REF or not os.path.isfile(os.path.join(REF, "kdtree.cpp")):
+        pytest.skip("WR_REFERENCE_DIR does not name a WalkRay source tree")
     subprocess.run(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle"), "dropin", f"REF={REF}"], check=True)
     return os.path.join(ROOT, "oracle", "_ref", "wr_ref_dropin")
 

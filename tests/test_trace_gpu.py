@@ -210,3 +210,53 @@ def test_large_filtered_host_batch_matches_device_entry_point(ctx):
     assert (want["tri"] != NO_HIT).mean() > 0.05
     ctx.release(sid)
 
+
+
+def test_exact_context_visits_every_box_with_the_same_hits():
+    """WR_CTX_EXACT_TRAVERSAL (no distance pruning, every box the reference
+    visits): the reference's golden hits, filtered and unfiltered, and the
+    same answers as the default pruned traversal on 1M random rays."""
+    from walkray_gb300.api import Context
+
+    with Context(exact_traversal=True) as ex, Context() as pr:
+        s = make_golden.golden_scenes()["ico4"]
+        g = np.load(os.path.join(GOLDEN, "trace_ico4.npz"))
+        rays = S.kd_rays(s, 32768, seed=2)
+        sid = ex.upload(s)
+        h = ex.trace_closest(sid, rays)
+        assert np.array_equal(h["tri"], g["tri"])
+        s2 = make_golden.golden_scenes()["mixed_l2"]
+        g2 = np.load(os.path.join(GOLDEN, "trace_filtered.npz"))
+        rays2, ids = make_golden.filtered_rays(s2, 32768, seed=5)
+        sid2 = ex.upload(s2)
+        h2 = ex.trace_closest(sid2, rays2, ids[:, 0], ids[:, 1])
+        assert np.array_equal(h2["tri"], g2["tri"])
+        big = S.kd_rays(s, 1 << 20, seed=31)
+        psid = pr.upload(s)
+        a, b = ex.trace_closest(sid, big), pr.trace_closest(psid, big)
+        assert np.array_equal(a["tri"], b["tri"])
+        assert np.array_equal(a["t"].view(np.uint32), b["t"].view(np.uint32))
+
+
+def test_device_random_stream_matches_oracle_word_for_word(ctx):
+    """The renderers' PathRng on the device, drawn sequentially (block caching
+    included), against the oracle's Philox4x32-10 restatement: every raw
+    word and every draw bit-identical, for seeds that use both key halves,
+    pixels and samples up to 2^32 - 1 and draw indices across block
+    boundaries."""
+    rng = np.random.default_rng(12)
+    n = 4096
+    pixel = rng.integers(0, 1 << 32, n, dtype=np.uint64).astype(np.uint32)
+    sample = rng.integers(0, 1 << 32, n, dtype=np.uint64).astype(np.uint32)
+    dim = rng.integers(0, 130, n).astype(np.uint32)
+    pixel[:4] = [0, 0xFFFFFFFF, 1, 7]
+    sample[:4] = [0, 0xFFFFFFFF, 2, 0]
+    dim[:8] = [0, 1, 2, 3, 4, 5, 127, 128]
+    for seed in (1, 0xDEADBEEF, (0x12345678 << 32) | 0x9ABCDEF0):
+        words, draws = ctx.rng_draws(seed, pixel, sample, dim)
+        key = [seed & 0xFFFFFFFF, seed >> 32]
+        for i in range(n):
+            w = wr_oracle.philox([int(dim[i]) >> 2, int(sample[i]), int(pixel[i]), 0], key)
+            assert np.array_equal(words[i], w), (seed, i)
+            d = np.float32(wr_oracle.draw(seed, int(pixel[i]), int(sample[i]), int(dim[i])))
+            assert draws[i].view(np.uint32) == d.view(np.uint32), (seed, i)

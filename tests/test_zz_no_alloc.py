@@ -1,10 +1,12 @@
 """wr_render_noalloc: rendering for callers that may not allocate device
-memory while they render (CUDA-graph capture in global mode, real-time loops,
-applications with their own memory pools).  Through the C ABI it must give
-the image wr_render gives, on two calls in a row (the shared film array keeps
-the previous call's contents and must be cleared by each call), reject
-images larger than its fixed film, and refuse scenes whose rendering tables
-were never built.  Collected last on purpose (file name)."""
+memory while they render (real-time loops that avoid cudaMalloc / cudaFree
+because they can stall the device, applications whose device memory belongs
+to their own pool).  Through the C ABI it must give the image wr_render gives,
+on two calls in a row (the shared film array keeps the previous call's
+contents and must be cleared by each call), report a clean traversal status
+through wr_render_noalloc_status, reject images larger than its fixed film,
+refuse scenes whose rendering tables were never built and scenes wr_render
+itself refuses.  Collected last on purpose (file name)."""
 import ctypes as C
 
 import numpy as np
@@ -21,6 +23,13 @@ def _noalloc(lib):
     f = lib.wr_render_noalloc
     f.restype = C.c_int
     f.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(L.wr_render_desc), C.c_void_p, C.c_void_p]
+    return f
+
+
+def _status(lib):
+    f = lib.wr_render_noalloc_status
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint)]
     return f
 
 
@@ -44,6 +53,9 @@ def test_noalloc_matches_wr_render_twice(built):
             torch.cuda.synchronize()
             got = out.cpu().numpy()
             assert np.allclose(got, ref, rtol=1e-4, atol=1e-5), np.abs(got - ref).max()
+            word = C.c_uint(12345)
+            assert _status(ctx.lib)(ctx.h, C.c_void_p(stream.cuda_stream), C.byref(word)) == 0
+            assert word.value == 0
         # a different image through the same film after a larger one
         d2 = L.wr_render_desc(4, 8, 6, 0, 0, 0, 0)
         ref2 = ctx.render(sid, 4, 8, seed=6, mode="megakernel")
@@ -70,5 +82,27 @@ def test_noalloc_rejects_oversized_and_wavefront(built):
         ctx.render(small, 1, 8)
         dw = L.wr_render_desc(1, 8, 1, 1, 0, 0, 0)  # wavefront mode
         assert fn(ctx.h, small, C.byref(dw), C.c_void_p(out.data_ptr()), None) == 8
+    finally:
+        ctx.close()
+
+
+def test_noalloc_refuses_what_wr_render_refuses(built):
+    """A heterogeneous medium whose sigma_t is not grey: wr_render answers
+    WR_ERR_UNSUPPORTED (delta tracking needs equal channels), and so must the
+    no-allocation entry point, instead of rendering a wrong image."""
+    torch = pytest.importorskip("torch")
+    ctx = Context()
+    try:
+        s = S.cornell_media(16, 16, grid_n=8)
+        het = next(o for o in s.objects if o.type == S.MAT_HETEROGENEOUS)
+        het.params["sigma_s"] = (0.8, 0.5, 0.8)
+        sid = ctx.upload(s)
+        with pytest.raises(RuntimeError):
+            ctx.render(sid, 1, 8, mode="megakernel")  # builds the tables, then refuses
+        fn = _noalloc(ctx.lib)
+        out = torch.empty((16, 16, 3), dtype=torch.float32, device="cuda")
+        d = L.wr_render_desc(1, 8, 1, 0, 0, 0, 0)
+        assert fn(ctx.h, sid, C.byref(d), C.c_void_p(out.data_ptr()), None) == 8
+        assert b"grey" in ctx.lib.wr_last_error(ctx.h)
     finally:
         ctx.close()

@@ -124,6 +124,9 @@ class wr_render_profile(C.Structure):
 
 WR_RENDER_NEE = 1
 WR_RENDER_EXACT_TRAVERSAL = 2
+WR_RENDER_NEE_MIS = 4
+WR_RENDER_PHONG_MIRROR = 8
+WR_CTX_EXACT_TRAVERSAL = 1
 
 HIT_DTYPE = np.dtype([("tri", "<u4"), ("t", "<f4"), ("b1", "<f4"), ("b2", "<f4")])
 
@@ -165,6 +168,9 @@ _SIGS = {
                                        C.POINTER(C.c_uint32)]),
     "wr_kdtree_host_export": (C.c_int, [C.c_void_p] + [C.c_void_p] * 6),
     "wr_kdtree_host_free": (C.c_int, [C.c_void_p]),
+    "wr_rng_draws": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p,
+                               C.c_void_p]),
+    "wr_render_noalloc_status": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint)]),
 }
 
 _lib = None

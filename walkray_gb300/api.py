@@ -49,9 +49,11 @@ def scene_desc(scene: Scene):
 
 
 class Context:
-    def __init__(self, device: int = 0, memory_budget: int = 0):
+    def __init__(self, device: int = 0, memory_budget: int = 0, exact_traversal: bool = False):
+        """`exact_traversal`: trace_closest visits every box the reference
+        visits (WR_CTX_EXACT_TRAVERSAL) instead of pruning by distance."""
         self.lib = L.load()
-        desc = L.wr_ctx_desc(device, memory_budget, 0, 0)
+        desc = L.wr_ctx_desc(device, memory_budget, L.WR_CTX_EXACT_TRAVERSAL if exact_traversal else 0, 0)
         h = C.c_void_p()
         rc = self.lib.wr_ctx_create(C.byref(desc), C.byref(h))
         if rc != L.WR_OK:
@@ -126,25 +128,27 @@ class Context:
 
     # ---- rendering ------------------------------------------------------
     def render(self, sid: int, spp: int, max_path_len: int, seed: int = 1, mode: str = "megakernel",
-               nee: bool = False, spp_offset: int = 0, exact: bool = False, radius: float = 0.0) -> np.ndarray:
+               nee: bool = False, spp_offset: int = 0, exact: bool = False, radius: float = 0.0,
+               flags: int = 0) -> np.ndarray:
         """Mean image (H, W, 3) float32, row 0 at the top (wr_render); `radius`
-        is the base radius of modes "vcm" and "photon_map" (0 = 0.01)."""
+        is the base radius of modes "vcm" and "photon_map" (0 = 0.01);
+        `flags`: further WR_RENDER_* bits (e.g. LOW_VARIANCE)."""
         w, h = self._camera_size(sid)
         out = np.empty((h, w, 3), np.float32)
-        d = L.wr_render_desc(spp, max_path_len, seed, MODES[mode], _flags(nee, exact), spp_offset, radius)
+        d = L.wr_render_desc(spp, max_path_len, seed, MODES[mode], _flags(nee, exact) | flags, spp_offset, radius)
         self._check(self.lib.wr_render(self.h, sid, C.byref(d), L.ptr(out)))
         return out
 
     def render_device(self, sid: int, spp: int, max_path_len: int, d_sum: int, d_sumsq: int = 0, seed: int = 1,
                       mode: str = "megakernel", nee: bool = False, spp_offset: int = 0, stream: int = 0,
-                      exact: bool = False, radius: float = 0.0) -> None:
+                      exact: bool = False, radius: float = 0.0, flags: int = 0) -> None:
         """Adds spp samples to a device film (wr_render_device), asynchronous on `stream`."""
-        d = L.wr_render_desc(spp, max_path_len, seed, MODES[mode], _flags(nee, exact), spp_offset, radius)
+        d = L.wr_render_desc(spp, max_path_len, seed, MODES[mode], _flags(nee, exact) | flags, spp_offset, radius)
         self._check(self.lib.wr_render_device(self.h, sid, C.byref(d), C.c_void_p(d_sum), C.c_void_p(d_sumsq or None),
                                               C.c_void_p(stream or None)))
 
     def render_stats(self, sid: int, spp: int, max_path_len: int, seed: int = 1, mode: str = "megakernel",
-                     nee: bool = False, exact: bool = False, radius: float = 0.0):
+                     nee: bool = False, exact: bool = False, radius: float = 0.0, flags: int = 0):
         """Per-pixel sum and sum of squares (H, W, 3) over spp samples, via torch device buffers."""
         import torch
 
@@ -153,14 +157,14 @@ class Context:
         s2 = torch.zeros((h, w, 3), dtype=torch.float32, device="cuda")
         torch.cuda.synchronize()
         self.render_device(sid, spp, max_path_len, s.data_ptr(), s2.data_ptr(), seed, mode, nee,
-                           stream=torch.cuda.current_stream().cuda_stream, exact=exact, radius=radius)
+                           stream=torch.cuda.current_stream().cuda_stream, exact=exact, radius=radius, flags=flags)
         torch.cuda.synchronize()
         return s.cpu().numpy().astype(np.float64), s2.cpu().numpy().astype(np.float64)
 
     def profile_render(self, sid: int, spp: int, max_path_len: int, d_sum: int, seed: int = 1,
-                       nee: bool = False, exact: bool = False) -> dict:
+                       nee: bool = False, exact: bool = False, flags: int = 0) -> dict:
         """Wavefront render with per-stage CUDA-event timings and traversal work counts."""
-        d = L.wr_render_desc(spp, max_path_len, seed, 1, _flags(nee, exact), 0, 0)
+        d = L.wr_render_desc(spp, max_path_len, seed, 1, _flags(nee, exact) | flags, 0, 0)
         p = L.wr_render_profile()
         self._check(self.lib.wr_profile_render(self.h, sid, C.byref(d), C.c_void_p(d_sum), C.byref(p)))
         return {k: (list(getattr(p, k)) if k.startswith("iter_") else getattr(p, k))
@@ -181,6 +185,20 @@ class Context:
         self._check(self.lib.wr_autotune(self.h, sid, spp_per_trial, max_path_len, C.byref(c)))
         return {k: getattr(c, k) for k, _ in L.wr_wavefront_config._fields_}
 
+    def rng_draws(self, seed: int, pixel, sample, dim):
+        """The device random stream (wr_rng_draws): (words (n, 4) uint32,
+        draws (n,) float32) of draw dim[i] of (pixel[i], sample[i])."""
+        px = np.ascontiguousarray(pixel, np.uint32)
+        sm = np.ascontiguousarray(sample, np.uint32)
+        dm = np.ascontiguousarray(dim, np.uint32)
+        n = len(px)
+        assert len(sm) == n and len(dm) == n
+        words = np.empty((n, 4), np.uint32)
+        draws = np.empty(n, np.float32)
+        self._check(self.lib.wr_rng_draws(self.h, seed, L.ptr(px), L.ptr(sm), L.ptr(dm), n, L.ptr(words),
+                                          L.ptr(draws)))
+        return words, draws
+
     def _camera_size(self, sid):
         cam = self._cams.get(sid)
         if cam is None:
@@ -189,6 +207,9 @@ class Context:
 
 
 MODES = {"megakernel": 0, "wavefront": 1, "bidirectional": 2, "vcm": 3, "photon_map": 4}
+# the low-variance estimators of the path tracer: unbiased NEE with MIS and
+# mirror-lobe Phong sampling (same expectation as the reference's estimator)
+LOW_VARIANCE = L.WR_RENDER_NEE_MIS | L.WR_RENDER_PHONG_MIRROR
 
 
 def _flags(nee: bool, exact: bool) -> int:
@@ -209,8 +230,8 @@ class Server:
         self.sizes: dict[int, tuple[int, int]] = {}
 
     def submit(self, sid: int, width: int, height: int, spp: int, max_path_len: int, seed: int = 1,
-               nee: bool = False, exact: bool = False) -> int:
-        r = L.wr_request_desc(sid, width, height, spp, max_path_len, _flags(nee, exact), seed)
+               nee: bool = False, exact: bool = False, flags: int = 0) -> int:
+        r = L.wr_request_desc(sid, width, height, spp, max_path_len, _flags(nee, exact) | flags, seed)
         rid = C.c_uint64()
         self.ctx._check(self.ctx.lib.wr_submit(self.ctx.h, C.byref(r), C.byref(rid)))
         self.sizes[rid.value] = (width, height)

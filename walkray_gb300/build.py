@@ -74,14 +74,14 @@ def build_lib(verbose: bool = False) -> str:
 
 
 def build_oracle(verbose: bool = False) -> None:
-    """The C restatement always; the reference harness when the reference
-    tree is present on this machine."""
+    """The C restatement always; the reference harness too when the
+    environment variable WR_REFERENCE_DIR names a WalkRay source tree."""
     odir = os.path.join(ROOT, "oracle")
     r = subprocess.run(["make", "-s", "-C", odir, "port"], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
-    ref = os.environ.get("WR_REFERENCE_DIR", "/root/reference")
-    if os.path.isfile(os.path.join(ref, "kdtree.cpp")):
+    ref = os.environ.get("WR_REFERENCE_DIR", "")
+    if ref and os.path.isfile(os.path.join(ref, "kdtree.cpp")):
         r = subprocess.run(["make", "-s", "-j8", "-C", odir, "ref", f"REF={ref}"], capture_output=True, text=True)
         if r.returncode != 0 and verbose:
             print("reference harness not built:", r.stderr[-2000:])

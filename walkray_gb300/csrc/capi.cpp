@@ -81,6 +81,7 @@ int wr_ctx_create(const wr_ctx_desc* desc, wr_ctx** out) {
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     ctx->memory_budget = (desc && desc->device_memory_budget) ? desc->device_memory_budget : (uint64_t)(free_b * 0.9);
+    ctx->trace_prune = !(desc && (desc->flags & WR_CTX_EXACT_TRAVERSAL));
     *out = ctx;
     return WR_OK;
 }

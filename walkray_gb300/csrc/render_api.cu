@@ -227,7 +227,8 @@ int wr_render_device(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, fl
         return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "unknown render mode");
     if ((desc->mode == WR_MODE_VCM || desc->mode == WR_MODE_PHOTON_MAP) && !(desc->radius >= 0.f && desc->radius < 1e30f))
         return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "merge / photon radius must be finite and >= 0");
-    if (desc->flags & ~RENDER_KNOWN_FLAGS) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "unknown render flags");
+    if (const char* why = render_flags_problem(desc->flags, desc->mode))
+        return set_error(ctx, WR_ERR_INVALID_ARGUMENT, why);
     if ((uint64_t)desc->spp_offset + desc->spp > 0xffffffffull)
         return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "sample index range overflows 32 bits");
     try {
@@ -320,6 +321,7 @@ int wr_render(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, float* rg
 namespace wr {
 
 const RenderScene& RenderDataView::scene(const RenderData* rd) { return rd->S; }
+const std::string& RenderDataView::unsupported(const RenderData* rd) { return rd->unsupported; }
 
 // the wavefront configuration: what wr_autotune picked for this context, else defaults
 WfConfig wf_tuned_config(wr_ctx* ctx) {
@@ -346,7 +348,8 @@ extern "C" int wr_profile_render(wr_ctx* ctx, wr_scene_id id, const wr_render_de
     if (!ctx || !desc || !d_sum || !out) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "null argument");
     SceneGPU* sc = find_scene(ctx, id);
     if (!sc) return set_error(ctx, WR_ERR_NOT_FOUND, "no such scene");
-    if (desc->flags & ~RENDER_KNOWN_FLAGS) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "unknown render flags");
+    if (const char* why = render_flags_problem(desc->flags, WR_MODE_WAVEFRONT))
+        return set_error(ctx, WR_ERR_INVALID_ARGUMENT, why);
     WR_CUDA(ctx, cudaSetDevice(ctx->device));
     RenderData* rd = nullptr;
     int rc = prepare_render(ctx, sc, &rd);

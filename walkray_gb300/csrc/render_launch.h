@@ -9,7 +9,20 @@ struct wr_ctx;
 
 namespace wr {
 
-constexpr uint32_t RENDER_KNOWN_FLAGS = WR_RENDER_NEE | WR_RENDER_EXACT_TRAVERSAL;
+constexpr uint32_t RENDER_KNOWN_FLAGS =
+    WR_RENDER_NEE | WR_RENDER_EXACT_TRAVERSAL | WR_RENDER_NEE_MIS | WR_RENDER_PHONG_MIRROR;
+// flags of the unidirectional path tracer only
+constexpr uint32_t RENDER_PT_ONLY_FLAGS = WR_RENDER_NEE_MIS | WR_RENDER_PHONG_MIRROR;
+
+// why a set of render flags cannot be used with a mode (nullptr: it can)
+inline const char* render_flags_problem(uint32_t flags, uint32_t mode) {
+    if (flags & ~RENDER_KNOWN_FLAGS) return "unknown render flags";
+    if ((flags & WR_RENDER_NEE) && (flags & WR_RENDER_NEE_MIS))
+        return "WR_RENDER_NEE (the reference's branch) and WR_RENDER_NEE_MIS exclude each other";
+    if ((flags & RENDER_PT_ONLY_FLAGS) && mode != WR_MODE_MEGAKERNEL && mode != WR_MODE_WAVEFRONT)
+        return "WR_RENDER_NEE_MIS and WR_RENDER_PHONG_MIRROR apply to the path tracing modes only";
+    return nullptr;
+}
 
 // factor on the closest hit's distance beyond which a box is skipped
 __host__ __device__ __forceinline__ float prune_factor(uint32_t flags) {

@@ -19,17 +19,19 @@ __global__ void __launch_bounds__(128) k_megakernel(RenderScene S, RenderParams 
     if (pixel >= npix) return;
     f3 acc = mk(0, 0, 0), acc2 = mk(0, 0, 0);
     const float pf = prune_factor(P.flags);
+    const bool nee = (P.flags & WR_RENDER_NEE) != 0;
     for (uint32_t s = P.s0; s < P.s1; s++) {
         PathRng g;
         g.init(P.seed, pixel, s);
         PRay cur = camera_ray(S.cam, pixel, g);
         InsideStack st;
         st.reset(cur.inside);
-        f3 color = mk(1, 1, 1), result = mk(0, 0, 0), prev_d = mk(0, 0, 0);
+        f3 color = mk(1, 1, 1), result = mk(0, 0, 0), prev_d = mk(0, 0, 0), lit = mk(0, 0, 0);
         uint32_t depth = 0;
         bool filtered = false;  // the eye ray is traced without a condition (camera.cpp:52)
-        const bool nee = (P.flags & WR_RENDER_NEE) != 0;
-        bool nee_here = false;
+        bool nee_here = false, has_lr = false;
+        float mis_pdf = 0.f;
+        LightReq lr;
         for (;;) {
             RayQ q = make_rayq(cur.o, cur.d, S.tree.scene_mag);
             q.pf = pf;
@@ -42,7 +44,16 @@ __global__ void __launch_bounds__(128) k_megakernel(RenderScene S, RenderParams 
             }
             set_hit(S, cur, h);
             filtered = true;
-            if (path_advance(S, cur, color, prev_d, depth, st, g, P.max_path_len, nee, result, nee_here)) break;
+            const bool done = path_advance(S, cur, color, prev_d, depth, st, g, P.max_path_len, P.flags, result,
+                                           nee_here, mis_pdf, lr, has_lr);
+            if (has_lr) {  // the light connection of WR_RENDER_NEE_MIS, traced inline
+                RayQ lq = make_rayq(lr.o, lr.d, S.tree.scene_mag);
+                lq.pf = pf;
+                const Hit lh =
+                    trace_closest<true, true>(S.tree, lq, lr.inside, lr.contact, stack, stride, P.stack_cap, err);
+                if (light_req_visible(S, lh, lr)) lit = lit + lr.contrib;
+            }
+            if (done) break;
         }
         if (nee_here) {  // the connection of the NEE branch, traced inline
             ShadowReq sr;
@@ -55,6 +66,7 @@ __global__ void __launch_bounds__(128) k_megakernel(RenderScene S, RenderParams 
             }
         }
         if (!legal(result)) result = mk(0, 0, 0);
+        result = result + lit;
         const f3 c = fix_vignetting(S.cam, result, pixel);
         acc = acc + c;
         if (STATS) acc2 = acc2 + vmul(c, c);

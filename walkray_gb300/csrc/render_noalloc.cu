@@ -2,12 +2,13 @@
 // no device memory at all.
 //
 // Who needs it: callers that may not call cudaMalloc / cudaFree while they
-// render.  Examples are code that runs while a CUDA graph is being captured
-// in global capture mode (where allocation calls are illegal), real-time
-// loops that forbid allocation because it can synchronise the device, and
-// applications whose device memory is owned by their own pool or allocator.
-// wr_render allocates an accumulation film on every call; this variant keeps
-// that film in one fixed array in the library instead.
+// render.  Examples are real-time loops that forbid allocation because
+// cudaMalloc and cudaFree can synchronise the device and stall a frame, and
+// applications whose device memory is owned by their own pool or allocator
+// (an engine that reserves its device memory up front and lets no library
+// allocate behind its back).  wr_render allocates an accumulation film on
+// every call; this variant keeps that film in one fixed array in the library
+// instead.
 //
 // The scratch: `g_film` below, a file-scope device array of
 // WR_NOALLOC_MAX_PIXELS * 3 floats (12 MiB) plus an error word.  Every GPU
@@ -19,10 +20,17 @@
 // Host code cannot pass `g_film` to a kernel by name (in host code that name
 // is a host-side stand-in, not a device address); the device address is
 // obtained once per device with cudaGetSymbolAddress, on the first call made
-// with that device current.  That first call should therefore come before any
-// stream capture.
+// with that device current.  The address belongs to the device's primary
+// context (the one the CUDA runtime uses); calls must be made with that
+// context current.
+//
+// The traversal error word (a per-thread stack that would overflow) is
+// cleared by each call and set by its kernels; wr_render_noalloc_status reads
+// it back, also without allocating.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <exception>
 #include <mutex>
 
 #include "render_launch.h"
@@ -71,14 +79,14 @@ __global__ void k_film_mean(const float* __restrict__ sum, float* __restrict__ o
 
 using namespace wr;
 
-extern "C" int wr_render_noalloc(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, float* d_rgb_out,
-                                 void* stream) {
-    if (!ctx || !desc || !d_rgb_out) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "null argument");
+static int render_noalloc_body(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, float* d_rgb_out,
+                               void* stream) {
     SceneGPU* sc = find_scene(ctx, id);
     if (!sc) return set_error(ctx, WR_ERR_NOT_FOUND, "no such scene");
     if (desc->mode != WR_MODE_MEGAKERNEL)
         return set_error(ctx, WR_ERR_UNSUPPORTED, "wr_render_noalloc renders with the megakernel (WR_MODE_MEGAKERNEL)");
-    if (desc->flags & ~RENDER_KNOWN_FLAGS) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "unknown render flags");
+    if (const char* why = render_flags_problem(desc->flags, desc->mode))
+        return set_error(ctx, WR_ERR_INVALID_ARGUMENT, why);
     const uint64_t npix = (uint64_t)sc->camera.width * sc->camera.height;
     if (npix > WR_NOALLOC_MAX_PIXELS)
         return set_error(ctx, WR_ERR_INVALID_ARGUMENT,
@@ -89,7 +97,12 @@ extern "C" int wr_render_noalloc(wr_ctx* ctx, wr_scene_id id, const wr_render_de
         return set_error(ctx, WR_ERR_UNSUPPORTED,
                          "the scene's rendering tables are not resident yet: render it once with wr_render or "
                          "wr_render_device (which build them) before calling wr_render_noalloc");
-    const RenderScene& S = RenderDataView::scene(static_cast<const RenderData*>(sc->render_data.get()));
+    const RenderData* rd = static_cast<const RenderData*>(sc->render_data.get());
+    // the same refusals as wr_render (for example a heterogeneous medium whose
+    // sigma_t is not grey, which delta tracking cannot render)
+    if (!RenderDataView::unsupported(rd).empty())
+        return set_error(ctx, WR_ERR_UNSUPPORTED, RenderDataView::unsupported(rd));
+    const RenderScene& S = RenderDataView::scene(rd);
     WR_CUDA(ctx, cudaSetDevice(ctx->device));
     float* film = nullptr;
     unsigned int* err = nullptr;
@@ -114,4 +127,33 @@ extern "C" int wr_render_noalloc(wr_ctx* ctx, wr_scene_id id, const wr_render_de
     k_film_mean<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, s>>>(film, d_rgb_out, n, inv);
     WR_CUDA(ctx, cudaGetLastError());
     return WR_OK;
+}
+
+extern "C" int wr_render_noalloc(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, float* d_rgb_out,
+                                 void* stream) {
+    if (!ctx || !desc || !d_rgb_out) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "null argument");
+    try {
+        return render_noalloc_body(ctx, id, desc, d_rgb_out, stream);
+    } catch (const std::exception& ex) {
+        return set_error(ctx, WR_ERR_INTERNAL, ex.what());
+    }
+}
+
+extern "C" int wr_render_noalloc_status(wr_ctx* ctx, void* stream, unsigned int* out_err) {
+    if (!ctx || !out_err) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "null argument");
+    try {
+        WR_CUDA(ctx, cudaSetDevice(ctx->device));
+        float* film = nullptr;
+        unsigned int* err = nullptr;
+        int rc = scratch_for(ctx, &film, &err);
+        if (rc != WR_OK) return rc;
+        cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+        unsigned int word = 0;
+        WR_CUDA(ctx, cudaMemcpyAsync(&word, err, sizeof word, cudaMemcpyDeviceToHost, s));
+        WR_CUDA(ctx, cudaStreamSynchronize(s));
+        *out_err = word;
+        return WR_OK;
+    } catch (const std::exception& ex) {
+        return set_error(ctx, WR_ERR_INTERNAL, ex.what());
+    }
 }

@@ -308,7 +308,8 @@ int wr_submit(wr_ctx* ctx, const wr_request_desc* req, wr_req_id* out) {
     if (!S) return set_error(ctx, WR_ERR_NOT_FOUND, "the serving loop is not running");
     if (req->width == 0 || req->height == 0 || req->width > 16384 || req->height > 16384)
         return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "bad resolution");
-    if (req->flags & ~RENDER_KNOWN_FLAGS) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "unknown render flags");
+    if (const char* why = render_flags_problem(req->flags, WR_MODE_WAVEFRONT))
+        return set_error(ctx, WR_ERR_INVALID_ARGUMENT, why);
     if ((uint64_t)req->width * req->height * req->spp == 0)
         return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "a request needs at least one path");
     const uint64_t film = sizeof(float) * 3ull * req->width * req->height;

@@ -24,6 +24,8 @@ struct WfPath {
     InsideStack st;
     uint32_t pixel, sample, dim;
     int job;
+    float mis_pdf;  // density of the current ray's scatter (WR_RENDER_NEE_MIS)
+    f3 acc;         // light connections counted so far (WR_RENDER_NEE_MIS)
 };
 
 __device__ __forceinline__ void wf_load(const WfSide& X, uint32_t i, WfPath& p) {
@@ -51,6 +53,13 @@ __device__ __forceinline__ void wf_load(const WfSide& X, uint32_t i, WfPath& p) 
     p.st.v3 = stk.w;
     const float4 a4 = X.a4[i];
     p.prev_d = mk(a4.x, a4.y, a4.z);
+    p.mis_pdf = a4.w;
+    p.acc = mk(0, 0, 0);
+}
+
+__device__ __forceinline__ void wf_load_acc(const WfSide& X, uint32_t i, WfPath& p) {
+    const float4 a5 = X.a5[i];
+    p.acc = mk(a5.x, a5.y, a5.z);
 }
 
 __device__ __forceinline__ void wf_store(const WfSide& Y, uint32_t j, const WfPath& p) {
@@ -62,7 +71,11 @@ __device__ __forceinline__ void wf_store(const WfSide& Y, uint32_t j, const WfPa
     Y.misc[j] = make_int4((int)p.sample, (int)p.dim, (int)(p.depth | ((uint32_t)p.st.n << 16)),
                           __float_as_int(p.cur.cnorm.z));
     Y.stk[j] = make_int4(p.st.v0, p.st.v1, p.st.v2, p.st.v3);
-    Y.a4[j] = make_float4(p.prev_d.x, p.prev_d.y, p.prev_d.z, 0.f);
+    Y.a4[j] = make_float4(p.prev_d.x, p.prev_d.y, p.prev_d.z, p.mis_pdf);
+}
+
+__device__ __forceinline__ void wf_store_acc(const WfSide& Y, uint32_t j, const WfPath& p) {
+    Y.a5[j] = make_float4(p.acc.x, p.acc.y, p.acc.z, 0.f);
 }
 
 // warp-aggregated append: returns this lane's position (valid if `want`)
@@ -138,10 +151,11 @@ __device__ __forceinline__ void film_add(const WfJob& J, uint32_t pixel, f3 resu
     }
 }
 
-// shadow stage: visibility of every NEE connection, visible contributions to the film
+// shadow stage: visibility of every NEE connection and light connection
+// (WF_SHADOW_*): visible contributions to the film or to their path
 __global__ void __launch_bounds__(128) k_wf_shadow(const RenderScene* __restrict__ scenes,
-                                                     const WfJob* __restrict__ jobs, WfShadow Q, int stack_cap,
-                                                     unsigned int* __restrict__ err) {
+                                                     const WfJob* __restrict__ jobs, WfShadow Q, WfSide Y,
+                                                     int stack_cap, unsigned int* __restrict__ err) {
     extern __shared__ uint32_t s_stack[];
     uint32_t* stack = s_stack + threadIdx.x;
     const uint32_t n = *Q.count;
@@ -149,11 +163,35 @@ __global__ void __launch_bounds__(128) k_wf_shadow(const RenderScene* __restrict
         const float4 o = Q.o[i], d = Q.d[i], c = Q.c[i];
         const int4 ids = Q.ids[i];
         const WfJob& J = jobs[ids.z];
-        const DevTree& T = scenes[J.scene].tree;
-        RayQ q = make_rayq(mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), T.scene_mag);
+        const RenderScene& S = scenes[J.scene];
+        RayQ q = make_rayq(mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), S.tree.scene_mag);
         q.pf = prune_factor(J.flags);
-        const Hit h = trace_closest<true, true>(T, q, ids.x, ids.y, stack, blockDim.x, stack_cap, err);
-        if (nee_visible(h, o.w)) film_add(J, (uint32_t)ids.w, mk(c.x, c.y, c.z));
+        const Hit h = trace_closest<true, true>(S.tree, q, ids.x, ids.y, stack, blockDim.x, stack_cap, err);
+        const int kind = __float_as_int(c.w);
+        const f3 contrib = mk(c.x, c.y, c.z);
+        if (kind == WF_SHADOW_NEE) {
+            if (nee_visible(h, o.w)) film_add(J, (uint32_t)ids.w, contrib);
+            continue;
+        }
+        LightReq lr;
+        lr.dist = o.w;
+        lr.light = __float_as_int(d.w);
+        const bool vis = light_req_visible(S, h, lr);
+        const float4 r = Q.r[i];
+        if (kind == WF_SHADOW_MIS_KEEP) {
+            if (vis) {
+                const int t = __float_as_int(r.w);
+                float4 a = Y.a5[t];
+                a.x += contrib.x;
+                a.y += contrib.y;
+                a.z += contrib.z;
+                Y.a5[t] = a;
+            }
+        } else {
+            f3 tot = mk(r.x, r.y, r.z);
+            if (vis) tot = tot + contrib;
+            if (tot.x != 0.f || tot.y != 0.f || tot.z != 0.f) film_add(J, (uint32_t)ids.w, tot);
+        }
     }
 }
 
@@ -258,13 +296,16 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade(const RenderScene* __restri
             i = B.idx[(size_t)k * capacity + (j - s_first[k])];
         }
         WfPath p;
-        bool keep = false, done = false, shadow = false;
+        bool keep = false, done = false, shadow = false, has_lr = false, mis = false;
         f3 result = mk(0, 0, 0);
         ShadowReq sr;
+        LightReq lr;
         if (valid) {
             wf_load(X, i, p);
             const WfJob& J = jobs[p.job];
             const RenderScene& S = scenes[J.scene];
+            mis = (J.flags & WR_RENDER_NEE_MIS) != 0;
+            if (mis) wf_load_acc(X, i, p);
             const int2 hv = hits[i];
             Hit h;
             h.slot = hv.x;
@@ -278,23 +319,41 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade(const RenderScene* __restri
                 nee_here = nee;
             } else {
                 set_hit(S, p.cur, h);
-                done = path_advance(S, p.cur, p.color, p.prev_d, p.depth, p.st, g, J.max_path_len, nee, result,
-                                    nee_here);
+                done = path_advance(S, p.cur, p.color, p.prev_d, p.depth, p.st, g, J.max_path_len, J.flags, result,
+                                    nee_here, p.mis_pdf, lr, has_lr);
             }
             if (nee_here) shadow = nee_prepare(S, p.cur, p.prev_d, p.color, g, sr);
             p.dim = g.dim;
             keep = !done;
-            if (done && !shadow && (result.x != 0.f || result.y != 0.f || result.z != 0.f))
-                film_add(J, p.pixel, result);
+            if (done) {
+                if (!legal(result)) result = mk(0, 0, 0);
+                result = result + p.acc;  // light connections of earlier vertices
+                if (!shadow && !has_lr && (result.x != 0.f || result.y != 0.f || result.z != 0.f))
+                    film_add(J, p.pixel, result);
+            }
+        }
+        // survivors, compacted into Y
+        const uint32_t out = warp_append(&Y.counts[0], keep, 0);
+        if (keep) {
+            wf_store(Y, out, p);
+            if (mis) wf_store_acc(Y, out, p);
         }
         // connections whose visibility the shadow stage decides
         {
-            const uint32_t k = warp_append(Q.count, shadow, 0);
+            const bool any = shadow || has_lr;
+            const uint32_t k = warp_append(Q.count, any, 0);
             if (shadow) {
                 Q.o[k] = make_float4(sr.o.x, sr.o.y, sr.o.z, sr.dist);
                 Q.d[k] = make_float4(sr.d.x, sr.d.y, sr.d.z, 0.f);
-                Q.c[k] = make_float4(sr.contrib.x, sr.contrib.y, sr.contrib.z, 0.f);
+                Q.c[k] = make_float4(sr.contrib.x, sr.contrib.y, sr.contrib.z, __int_as_float(WF_SHADOW_NEE));
                 Q.ids[k] = make_int4(sr.inside, sr.contact, p.job, (int)p.pixel);
+            } else if (has_lr) {
+                Q.o[k] = make_float4(lr.o.x, lr.o.y, lr.o.z, lr.dist);
+                Q.d[k] = make_float4(lr.d.x, lr.d.y, lr.d.z, __int_as_float(lr.light));
+                Q.c[k] = make_float4(lr.contrib.x, lr.contrib.y, lr.contrib.z,
+                                     __int_as_float(keep ? WF_SHADOW_MIS_KEEP : WF_SHADOW_MIS_DONE));
+                Q.r[k] = make_float4(result.x, result.y, result.z, __int_as_float((int)out));
+                Q.ids[k] = make_int4(lr.inside, lr.contact, p.job, (int)p.pixel);
             }
         }
         // finished-path counts per job, aggregated over the lanes sharing a job
@@ -306,8 +365,6 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade(const RenderScene* __restri
                     atomicAdd(&counters[p.job].finished, (unsigned long long)__popc(same));
             }
         }
-        const uint32_t out = warp_append(&Y.counts[0], keep, 0);
-        if (keep) wf_store(Y, out, p);
     }
 }
 
@@ -329,12 +386,14 @@ __global__ void __launch_bounds__(128) k_wf_drain(const RenderScene* __restrict_
     wf_load(X, i, p);
     const WfJob& J = jobs[p.job];
     const RenderScene& S = scenes[J.scene];
+    if (J.flags & WR_RENDER_NEE_MIS) wf_load_acc(X, i, p);
     PathRng g;
     g.init(J.seed, p.pixel, p.sample, p.dim);
     const bool nee = (J.flags & WR_RENDER_NEE) != 0;
     const float pf = prune_factor(J.flags);
-    bool filtered = p.cur.contact != CAMERA_OBJ, nee_here = false;
+    bool filtered = p.cur.contact != CAMERA_OBJ, nee_here = false, has_lr = false;
     f3 result = mk(0, 0, 0);
+    LightReq lr;
     for (;;) {
         RayQ q = make_rayq(p.cur.o, p.cur.d, S.tree.scene_mag);
         q.pf = pf;
@@ -347,8 +406,16 @@ __global__ void __launch_bounds__(128) k_wf_drain(const RenderScene* __restrict_
         }
         set_hit(S, p.cur, h);
         filtered = true;
-        if (path_advance(S, p.cur, p.color, p.prev_d, p.depth, p.st, g, J.max_path_len, nee, result, nee_here))
-            break;
+        const bool done = path_advance(S, p.cur, p.color, p.prev_d, p.depth, p.st, g, J.max_path_len, J.flags,
+                                       result, nee_here, p.mis_pdf, lr, has_lr);
+        if (has_lr) {
+            RayQ lq = make_rayq(lr.o, lr.d, S.tree.scene_mag);
+            lq.pf = pf;
+            const Hit lh = trace_closest<true, true>(S.tree, lq, lr.inside, lr.contact, stack, blockDim.x, stack_cap,
+                                                     err);
+            if (light_req_visible(S, lh, lr)) p.acc = p.acc + lr.contrib;
+        }
+        if (done) break;
     }
     if (nee_here) {
         ShadowReq sr;
@@ -360,6 +427,8 @@ __global__ void __launch_bounds__(128) k_wf_drain(const RenderScene* __restrict_
             if (nee_visible(h, sr.dist)) result = sr.contrib;
         }
     }
+    if (!legal(result)) result = mk(0, 0, 0);
+    result = result + p.acc;
     if (result.x != 0.f || result.y != 0.f || result.z != 0.f) film_add(J, p.pixel, result);
     const unsigned same = __match_any_sync(__activemask(), p.job);
     if ((threadIdx.x & 31u) == (unsigned)(__ffs(same) - 1))
@@ -420,9 +489,14 @@ __global__ void __launch_bounds__(128) k_wf_generate(const WfJob* __restrict__ j
             p.prev_d = mk(0, 0, 0);
             p.depth = 0;
             p.st.reset(p.cur.inside);
+            p.mis_pdf = 0.f;
+            p.acc = mk(0, 0, 0);
         }
         const uint32_t j = warp_append(&Y.counts[1], have, survivors);
-        if (have) wf_store(Y, j, p);
+        if (have) {
+            wf_store(Y, j, p);
+            if (jobs[jid].flags & WR_RENDER_NEE_MIS) wf_store_acc(Y, j, p);
+        }
     }
 }
 
@@ -458,7 +532,7 @@ const WfConfig& wf_config(const WfEngine* E) { return E->cfg; }
 
 static int alloc_side(wr_ctx* ctx, WfEngine* E, int k) {
     const size_t Q = E->cfg.capacity;
-    const size_t bytes = Q * (5 * sizeof(float4) + 3 * sizeof(int4)) + 256;
+    const size_t bytes = Q * (6 * sizeof(float4) + 3 * sizeof(int4)) + 256;
     WR_CUDA(ctx, E->side_mem[k].reserve(bytes));
     char* p = E->side_mem[k].as<char>();
     WfSide& S = E->side[k];
@@ -470,7 +544,8 @@ static int alloc_side(wr_ctx* ctx, WfEngine* E, int k) {
     S.misc = S.ids + Q;
     S.stk = S.misc + Q;
     S.a4 = reinterpret_cast<float4*>(S.stk + Q);
-    S.counts = reinterpret_cast<unsigned int*>(S.a4 + Q);
+    S.a5 = S.a4 + Q;
+    S.counts = reinterpret_cast<unsigned int*>(S.a5 + Q);
     WR_CUDA(ctx, cudaMemset(S.counts, 0, 2 * sizeof(unsigned int)));
     return WR_OK;
 }
@@ -504,12 +579,13 @@ int wf_engine_get(wr_ctx* ctx, const WfConfig& cfg, WfEngine** out) {
     E->grid_sort = ctx->num_sms * 4;
     {
         const size_t Q = cfg.capacity;
-        WR_CUDA(ctx, E->shadow_mem.reserve(Q * (3 * sizeof(float4) + sizeof(int4)) + 256));
+        WR_CUDA(ctx, E->shadow_mem.reserve(Q * (4 * sizeof(float4) + sizeof(int4)) + 256));
         char* p = E->shadow_mem.as<char>();
         E->shadow.o = reinterpret_cast<float4*>(p);
         E->shadow.d = E->shadow.o + Q;
         E->shadow.c = E->shadow.d + Q;
-        E->shadow.ids = reinterpret_cast<int4*>(E->shadow.c + Q);
+        E->shadow.r = E->shadow.c + Q;
+        E->shadow.ids = reinterpret_cast<int4*>(E->shadow.r + Q);
         E->shadow.count = reinterpret_cast<unsigned int*>(E->shadow.ids + Q);
         WR_CUDA(ctx, cudaMemset(E->shadow.count, 0, sizeof(unsigned int)));
     }
@@ -655,8 +731,8 @@ static void enqueue_iteration(WfEngine* E, int x, cudaStream_t s, cudaEvent_t* e
     k_wf_shade<<<E->grid_shade, E->cfg.shade_block, 0, s>>>(scenes, jobs, cnt, E->side[x], E->hits.as<int2>(),
                                                             E->side[y], E->shadow, E->sort, E->cfg.capacity);
     if (ev) cudaEventRecord(ev[2], s);
-    k_wf_shadow<<<E->grid_shadow, E->cfg.extend_block, E->smem_shadow, s>>>(scenes, jobs, E->shadow, E->stack_cap,
-                                                                           E->err_word.as<unsigned int>());
+    k_wf_shadow<<<E->grid_shadow, E->cfg.extend_block, E->smem_shadow, s>>>(scenes, jobs, E->shadow, E->side[y],
+                                                                           E->stack_cap, E->err_word.as<unsigned int>());
     if (ev) cudaEventRecord(ev[3], s);
     k_wf_generate<<<E->grid_gen, E->cfg.shade_block, 0, s>>>(jobs, E->order.as<int>(), cnt, E->side[y],
                                                              E->cfg.capacity);

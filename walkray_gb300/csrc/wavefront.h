@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <memory>
+#include <string>
 #include <vector>
 
 #include "render_launch.h"
@@ -28,6 +29,7 @@ namespace wr {
 struct RenderData;
 struct RenderDataView {  // what the engine needs from RenderData (render_api.cu)
     static const RenderScene& scene(const RenderData* rd);
+    static const std::string& unsupported(const RenderData* rd);  // non-empty: why the scene cannot render
 };
 
 struct WfJob {
@@ -56,7 +58,8 @@ struct WfSide {
     int4* ids;   // inside, contact, job, pixel
     int4* misc;  // sample, rng dim, depth | stack_n << 16, cnorm.z bits
     int4* stk;   // inside stack
-    float4* a4;  // direction of the ray before the current one (next-event estimation)
+    float4* a4;  // direction of the ray before the current one (next-event estimation), MIS density
+    float4* a5;  // light connections counted so far (WR_RENDER_NEE_MIS jobs only)
     unsigned int* counts;  // [0] survivors written by shade, [1] paths appended by generate
 };
 
@@ -72,11 +75,17 @@ struct WfSort {
 // shadow rays of next-event estimation, written by shade, traced by k_wf_shadow
 struct WfShadow {
     float4* o;    // origin, distance to the light sample
-    float4* d;    // direction
-    float4* c;    // contribution if visible
+    float4* d;    // direction, light object (int bits; WR_RENDER_NEE_MIS)
+    float4* c;    // contribution if visible, kind (int bits: WF_SHADOW_*)
+    float4* r;    // WF_SHADOW_MIS_DONE: the path's own result; target path slot (int bits)
     int4* ids;    // inside, contact, job, pixel
     unsigned int* count;
 };
+// what a visible shadow ray does: the reference's NEE adds its colour to the
+// film; a light connection of a path that goes on adds it to the path's
+// accumulator (slot `target` of the side shade wrote); one of a path that
+// ended adds it to the path's result, which goes to the film
+enum : int { WF_SHADOW_NEE = 0, WF_SHADOW_MIS_KEEP = 1, WF_SHADOW_MIS_DONE = 2 };
 
 struct WfConfig {
     uint32_t capacity = 1u << 24;  // paths in flight (16M x 128 B of state per side): a 1024^2 x 16-spp call at once

@@ -74,7 +74,7 @@ struct wr_ctx {
     wr::DeviceBuffer rays, hits, inside, contact;
     wr::DeviceBuffer scratch_words;  // counters / error flags
     wr::DeviceBuffer film;           // wr_render's image, kept between calls (no allocation per call)
-    bool trace_prune = false;
+    bool trace_prune = true;  // wr_trace_closest skips boxes beyond the closest hit (WR_CTX_EXACT_TRAVERSAL: never)
     int last_trace_blocks = 0;
     uint64_t kernel_launches = 0;  // kernels this library has launched on the context
     std::shared_ptr<void> serving;    // serving loop state (serve.cpp)

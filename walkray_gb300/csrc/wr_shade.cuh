@@ -240,6 +240,33 @@ __device__ __forceinline__ f3 phong_sample(f3 albedo, float power, f3 in, f3 N, 
     return rho * powf(dRW > 0.f ? dRW : 0.f, power);
 }
 
+// IsotropicPhong's BRDF with directions sampled about the mirror direction R
+// (WR_RENDER_PHONG_MIRROR): density (n+1)/(2 pi) (R.w)^n over the sphere, the
+// lobe's own shape, so f cos / pdf = albedo (n+2)/(n+1) cos stays bounded.
+// The BRDF is zero where R.w <= 0, and the density covers every direction
+// where it is not, so the expectation is the reference's; a sample below the
+// surface ends the path with zero radiance.  Same draws as phong_sample.
+__device__ __forceinline__ f3 phong_sample_mirror(f3 albedo, float power, f3 in, f3 N, PathRng& g, f3& out,
+                                                  float& pdf) {
+    const f3 R = mirror_dir(N, in);
+    f3 X, Y, Z;
+    frame_from_n(R, X, Y, Z);
+    const float a = g.next(), b = g.next();
+    const float t2 = powf(b, 1.f / (power + 1.f));
+    const float t3 = sqrtf(fmaxf(0.f, 1.f - t2 * t2));
+    float s, c;
+    sincosf(2.f * PI_F * a, &s, &c);
+    out = normalize(to_world(X, Y, Z, mk(s * t3, t2, c * t3)));
+    const float dR = fmaxf(dot(R, out), 0.f);
+    const float lobe = powf(dR, power);
+    pdf = (power + 1.f) * lobe * (INV_PI_F * 0.5f);
+    if (!(dot(out, N) > 0.f)) {
+        out = mk(0, 0, 0);
+        return mk(0, 0, 0);
+    }
+    return albedo * ((power + 2.f) * 0.5f * INV_PI_F * lobe);
+}
+
 // AnisotropicPhong::evalBSDF (anisotropicPhong.h:62-101), including the
 // reference's unparenthesised MAX in the specular denominator
 __device__ __forceinline__ f3 aniso_eval(const wr_object_desc* m, f3 in, f3 out, f3 N) {
@@ -397,7 +424,8 @@ __device__ __forceinline__ void set_contact(const RenderScene& S, PRay& out, int
 }
 
 // Diffuse / Glossy / AnisotropicGlossy (diffuseObj.h:34-57, glossyObj.h:39-62, anisotropicGlossyObj.h:54-68)
-__device__ __forceinline__ PRay scatter_surface(const RenderScene& S, int self, const PRay& in, PathRng& g) {
+__device__ __forceinline__ PRay scatter_surface(const RenderScene& S, int self, const PRay& in, PathRng& g,
+                                                bool mirror = false) {
     const wr_object_desc* m = &S.objs[self];
     PRay out = ray_default();
     out.o = in.o + in.d * in.idist;
@@ -417,6 +445,7 @@ __device__ __forceinline__ PRay scatter_surface(const RenderScene& S, int self, 
     if (albedo.z > p) p = albedo.z;
     if (g.next() < p) {
         if (type == WR_MAT_DIFFUSE) out.rad = diffuse_sample(albedo, N, g, out.d, out.dP);
+        else if (mirror) out.rad = phong_sample_mirror(albedo, __ldg(&m->power), in.d, N, g, out.d, out.dP);
         else out.rad = phong_sample(albedo, __ldg(&m->power), in.d, N, g, out.d, out.dP);
         out.dP *= p;
     } else {
@@ -856,7 +885,7 @@ static __device__ __noinline__ PRay scatter_heterogeneous_ref(const RenderScene&
 // RefMedia: heterogeneous media by the reference's own sampler.
 template <bool RefMedia = false>
 static __device__ __forceinline__ PRay scatter(const RenderScene& S, int self, const PRay& in, PathRng& g,
-                                            InsideStack& st) {
+                                            InsideStack& st, bool mirror = false) {
     PRay cur = in;
     float oP_scale = 1.f;
     int medium_hit = -1;  // the object a medium handed over to (photonType, homogeneousVolume.cpp:192-194)
@@ -868,7 +897,7 @@ static __device__ __forceinline__ PRay scatter(const RenderScene& S, int self, c
         switch (type) {
             case WR_MAT_DIFFUSE:
             case WR_MAT_GLOSSY:
-            case WR_MAT_ANISO: out = scatter_surface(S, self, cur, g); break;
+            case WR_MAT_ANISO: out = scatter_surface(S, self, cur, g, mirror); break;
             case WR_MAT_EMISSIVE: out = scatter_emissive(S, self, cur); break;
             case WR_MAT_REFLECTIVE: out = scatter_reflective(S, self, cur, g); break;
             case WR_MAT_REFRACTIVE:
@@ -1143,29 +1172,140 @@ __device__ __forceinline__ bool nee_visible(const Hit& h, float dist) {
     return h.slot < 0 || h.t - dist >= -EPS_F;
 }
 
+// ---------------------------------------------------------------------------
+// next-event estimation with multiple importance sampling (WR_RENDER_NEE_MIS)
+// ---------------------------------------------------------------------------
+// The surface materials whose scatter has a density to weigh against light
+// sampling: diffuse, isotropic and anisotropic Phong.
+__device__ __forceinline__ bool mis_material(uint32_t t) {
+    return t == WR_MAT_DIFFUSE || t == WR_MAT_GLOSSY || t == WR_MAT_ANISO;
+}
+
+// Solid-angle density with which scatter_surface of object `o` samples `out`
+// for the incoming direction `in` at normal N, Russian roulette left out
+// (diffuseBsdf.h:21-30, isotropicPhong.h:20-38 or the mirror lobe,
+// anisotropicPhongHalfVecSampler.h:39-56).  Used by both strategies' weights.
+__device__ __forceinline__ float bsdf_pdf(const RenderScene& S, int o, f3 in, f3 N, f3 out, bool mirror) {
+    const wr_object_desc* m = &S.objs[o];
+    const uint32_t t = __ldg(&m->type);
+    const float dn = dot(N, out);
+    if (!(dn > 0.f)) return 0.f;
+    if (t == WR_MAT_DIFFUSE) return dn * INV_PI_F;
+    if (t == WR_MAT_GLOSSY) {
+        const float power = __ldg(&m->power);
+        const float c = mirror ? dot(mirror_dir(N, in), out) : dn;
+        return c > 0.f ? (power + 1.f) * powf(c, power) * (INV_PI_F * 0.5f) : 0.f;
+    }
+    if (t == WR_MAT_ANISO) {
+        const f3 h = normalize(out - in);
+        const float ih = fabsf(dot(in, h));
+        return ih > 0.f ? aniso_half_pdf(__ldg(&m->nu), __ldg(&m->nv), N, h) / (4.f * ih) : 0.f;
+    }
+    return 0.f;
+}
+
+// Solid-angle density with which the light sampler picks the emitter point
+// a ray from a surface reaches at distance `dist` with cosine `cl` (the
+// sampler is uniform in area over all emitters: SurfaceSampler's
+// area-proportional object pick times the object's own uniform point).
+__device__ __forceinline__ float light_pdf(const RenderScene& S, int emitter, float dist, float cl) {
+    const float pa = __ldg(&S.pick_prob[emitter]) / __ldg(&S.obj_area[emitter]);
+    return pa > 0.f && cl != 0.f ? pa * dist * dist / fabsf(cl) : 0.f;
+}
+
+// A light-sample connection: traced from o along d; it counts when the
+// closest hit is the sampled emitter at (about) `dist`.
+struct LightReq {
+    f3 o, d;
+    float dist;
+    f3 contrib;  // the path's colour added when it counts (MIS-weighted)
+    int light, inside, contact;
+};
+
+__device__ __forceinline__ bool light_req_visible(const RenderScene& S, const Hit& h, const LightReq& lr) {
+    if (h.slot < 0) return false;
+    const int obj = (int)__float_as_uint(__ldg(&S.tree.tris[h.slot].v1.w));
+    return obj == lr.light && h.t >= lr.dist - fmaxf(EPS_F, 1e-4f * lr.dist);
+}
+
+// The light strategy at the surface vertex `cur` hits (object `self`, outside
+// media), whose arriving throughput is T: one light sample (6 draws), the
+// BSDF towards it, the geometry term and the power-heuristic weight against
+// the density with which the scatter could have sampled the same direction.
+__device__ __forceinline__ bool mis_light_request(const RenderScene& S, int self, const PRay& cur, f3 T, PathRng& g,
+                                                  bool mirror, LightReq& lr) {
+    if (S.nlights == 0) return false;
+    const PRay L = light_sample(S, g);
+    if (length(L.d) < 0.5f) return false;  // an emitter without triangles
+    const f3 x = cur.o + cur.d * cur.idist;
+    const f3 N = cur.inorm;
+    const f3 v = L.o - x;
+    const float dist = length(v);
+    if (!(dist > EPS_F)) return false;
+    const f3 wi = v * (1.f / dist);
+    const float cl = dot(wi, L.cnorm);
+    if (!(cl < 0.f)) return false;  // EmissiveObject emits against its normal only
+    PRay e = ray_default();
+    e.o = x;
+    e.d = wi;
+    e.contact = self;
+    e.cnorm = N;
+    e.inside = cur.inside;
+    const f3 f = eval_bsdf(S, cur.d, e);
+    if (f.x == 0.f && f.y == 0.f && f.z == 0.f) return false;
+    const float pl = L.oP * dist * dist / -cl;
+    const float pb = bsdf_pdf(S, self, cur.d, N, wi, mirror);
+    const float w = pl * pl / (pl * pl + pb * pb);
+    lr.contrib = vmul(vmul(T, f), L.rad) * (cos_term(S, e) * w / pl);
+    lr.o = x;
+    lr.d = wi;
+    lr.dist = dist;
+    lr.light = L.contact;
+    lr.inside = cur.inside;
+    lr.contact = self;
+    return legal(lr.contrib);
+}
+
 // One bounce of MCRenderer::samplePath (mcRenderer.cpp:25-56) for a path
 // whose current ray `cur` has its hit set: scatter, then either finish
 // (returns true, `result` = the path's colour before isLegalColor) or apply
 // cur's throughput factors (pathTracer.cpp:29-38) and make the scattered ray
 // current (returns false; it must be traced next, a miss ends with 0).
 //
-// With NEE (`nee`), a path that ends with zero radiance and no contact or
-// inside object on its last ray (it escaped, or was cut at the maximum
-// length, or was absorbed in a medium) is connected to a light from the
-// origin of the ray that closes it (the reference's endIndex rule,
+// With NEE (WR_RENDER_NEE in `flags`), a path that ends with zero radiance
+// and no contact or inside object on its last ray (it escaped, or was cut at
+// the maximum length, or was absorbed in a medium) is connected to a light
+// from the origin of the ray that closes it (the reference's endIndex rule,
 // pathTracer.cpp:40-41): `nee_here` is set, `cur` is that ray, `prev_d` the
 // direction before it and `color` the product of the earlier factors.  A
 // scattered ray that misses is the caller's case: the same connection from it.
+//
+// With WR_RENDER_NEE_MIS, a vertex on a diffuse / Phong surface outside media
+// also asks for a light connection (`has_lr`, `lr`: the caller traces it and
+// adds lr.contrib when light_req_visible), and an emitter reached straight
+// from such a vertex is weighted against the light strategy; `mis_pdf`
+// carries the scatter's density of the current ray (0: nothing to weigh).
 __device__ __forceinline__ bool path_advance(const RenderScene& S, PRay& cur, f3& color, f3& prev_d,
                                              uint32_t& depth, InsideStack& st, PathRng& g, uint32_t max_path_len,
-                                             bool nee, f3& result, bool& nee_here) {
+                                             uint32_t flags, f3& result, bool& nee_here, float& mis_pdf,
+                                             LightReq& lr, bool& has_lr) {
     nee_here = false;
+    has_lr = false;
+    const bool nee = (flags & WR_RENDER_NEE) != 0;
+    const bool mis = (flags & WR_RENDER_NEE_MIS) != 0;
+    const bool mirror = (flags & WR_RENDER_PHONG_MIRROR) != 0;
     const int self = cur.inside >= 0 ? cur.inside : cur.iobj;
     if (self < 0) {  // escaped eye ray: terminateRay carries zero radiance, endIndex 0 connects nothing
         result = mk(0, 0, 0);
         return true;
     }
-    PRay next = scatter(S, self, cur, g, st);
+    const uint32_t stype = obj_type(S, self);
+    const bool mis_vertex = mis && cur.inside < 0 && mis_material(stype);
+    if (mis_vertex) {
+        const f3 T = vmul(color * cos_term(S, cur), weight(cur));
+        has_lr = mis_light_request(S, self, cur, T, g, mirror, lr);
+    }
+    PRay next = scatter(S, self, cur, g, st, mirror);
     if (length(next.d) < 0.5f) {
         const bool zero = next.rad.x == 0.f && next.rad.y == 0.f && next.rad.z == 0.f;
         if (nee && zero) {
@@ -1177,6 +1317,11 @@ __device__ __forceinline__ bool path_advance(const RenderScene& S, PRay& cur, f3
         color = vmul(color, radiance_decay(S, cur, length(next.o - cur.o)));
         color = vmul(color, weight(cur));
         result = vmul(color, weight(next));
+        if (mis && mis_pdf > 0.f && stype == WR_MAT_EMISSIVE && cur.inside < 0 && !zero) {
+            // the emitter reached by the previous vertex's scatter: weigh against the light strategy
+            const float pl = light_pdf(S, self, cur.idist * length(cur.d), dot(cur.d, cur.inorm));
+            result = result * (mis_pdf * mis_pdf / (mis_pdf * mis_pdf + pl * pl));
+        }
         return true;
     }
     if (depth + 1 > max_path_len) {
@@ -1184,6 +1329,7 @@ __device__ __forceinline__ bool path_advance(const RenderScene& S, PRay& cur, f3
         nee_here = nee && depth >= 1;
         return true;
     }
+    mis_pdf = mis_vertex ? bsdf_pdf(S, self, cur.d, cur.inorm, next.d, mirror) : 0.f;
     st.set_top(next.inside);
     color = color * cos_term(S, cur);
     color = vmul(color, radiance_decay(S, cur, length(next.o - cur.o)));

@@ -30,11 +30,23 @@
 //    all six if that one fails.
 //    Rays must be finite; a NaN or infinite direction gets no hit here, as
 //    in the reference (its triangle test fails for it).
-//  * Optional pruning (PRUNE, used by the renderers): a child whose grown-box
-//    entry distance exceeds q.pf times the best hit (plus M) is skipped.  A
-//    triangle's hit lies inside its box, so this keeps the closest hit unless
-//    the triangle test's rounding puts a hit far from the triangle (a ray
-//    almost in the triangle's plane); off in wr_trace_closest.
+//    The shrunk distances are the grown ones moved by 2M|inv| per axis
+//    (q.sm: the grown near plane is M outside the box, the shrunk one M
+//    inside, so their distances differ by exactly 2M|inv|), one FP32
+//    addition each instead of a subtraction and a product: their rounding
+//    stays within ~4 eps (B + |o|) |inv|, far inside the margin.  A ray with
+//    a zero (or subnormal) direction component has a non-finite 2M|inv|; its
+//    q.sm is NaN, so its shrunk test never passes and every box it grazes is
+//    decided by the face test.
+//  * Optional pruning (PRUNE, used by the renderers and wr_trace_closest): a
+//    child whose grown-box entry distance exceeds q.pf times the best hit
+//    (plus M) is skipped.  A triangle lies inside its box (boxes are the
+//    bounds of their triangles' vertices), so its hit distance is at least
+//    the box's entry distance up to the triangle test's rounding, which is
+//    relative and bounded unless the ray grazes the triangle's plane (|n.d|
+//    small).  A hit accepted with |n.d| < 2^-5 |d| therefore switches pruning
+//    off for the rest of that ray (q.pf = inf): near-grazing rays see every
+//    box the reference sees.
 #pragma once
 
 #include "wr_device.cuh"
@@ -45,12 +57,15 @@ struct RayQ {
     f3 o, d, inv;
     // per axis, with s = +1 where the direction is positive (inv > 0), else -1:
     // gno = o + s M and gfo = o - s M.  (near corner - gno) * inv is the
-    // grown-box near distance, (near corner - gfo) * inv the shrunk one, and
-    // the far corner with the roles swapped.
-    f3 gno, gfo;
+    // grown-box near distance, (far corner - gfo) * inv the grown-box far
+    // one; the shrunk box's are those -/+ sm = 2 M |inv| (NaN: never sure).
+    f3 gno, gfo, sm;
     float M;      // box margin for this ray
     float pf;     // pruning: boxes entered beyond pf * (closest hit) + M are skipped
 };
+
+// below this |n.d| / |d| an accepted hit turns pruning off for its ray
+constexpr float GRAZE_COS = 0.03125f;
 
 __device__ __forceinline__ RayQ make_rayq(f3 o, f3 d, float scene_mag) {
     RayQ q;
@@ -65,6 +80,9 @@ __device__ __forceinline__ RayQ make_rayq(f3 o, f3 d, float scene_mag) {
     const float hi_x = o.x - q.M, hi_y = o.y - q.M, hi_z = o.z - q.M;
     q.gno = mk(q.inv.x > 0.f ? lo_x : hi_x, q.inv.y > 0.f ? lo_y : hi_y, q.inv.z > 0.f ? lo_z : hi_z);
     q.gfo = mk(q.inv.x > 0.f ? hi_x : lo_x, q.inv.y > 0.f ? hi_y : lo_y, q.inv.z > 0.f ? hi_z : lo_z);
+    const float m2 = 2.f * q.M;
+    q.sm = mk(m2 * fabsf(q.inv.x), m2 * fabsf(q.inv.y), m2 * fabsf(q.inv.z));
+    if (!(isfinite(q.sm.x) && isfinite(q.sm.y) && isfinite(q.sm.z))) q.sm = mk(NAN, NAN, NAN);
     q.pf = 1.001f;
     return q;
 }
@@ -150,9 +168,9 @@ __device__ __forceinline__ int box_classify(const Box& bx, const RayQ& q, float*
     const float gny = (cny - q.gno.y) * q.inv.y, gfy = (cfy - q.gfo.y) * q.inv.y;
     const float gnz = (cnz - q.gno.z) * q.inv.z, gfz = (cfz - q.gfo.z) * q.inv.z;
     // shrunk box (empty, so never "sure", when thinner than 2M)
-    const float snx = (cnx - q.gfo.x) * q.inv.x, sfx = (cfx - q.gno.x) * q.inv.x;
-    const float sny = (cny - q.gfo.y) * q.inv.y, sfy = (cfy - q.gno.y) * q.inv.y;
-    const float snz = (cnz - q.gfo.z) * q.inv.z, sfz = (cfz - q.gno.z) * q.inv.z;
+    const float snx = gnx + q.sm.x, sfx = gfx - q.sm.x;
+    const float sny = gny + q.sm.y, sfy = gfy - q.sm.y;
+    const float snz = gnz + q.sm.z, sfz = gfz - q.sm.z;
     const float T1 = fmaxf(gnx, fmaxf(gny, gnz)), U1 = fminf(gfx, fminf(gfy, gfz));
     const float T2 = fmaxf(snx, fmaxf(sny, snz)), U2 = fminf(sfx, fminf(sfy, sfz));
     *tnear = T1;
@@ -189,7 +207,7 @@ __device__ __forceinline__ void pair_pred(const Box& L, const Box& R, const RayQ
 // KDTree::intersect(ray, tri) geometric part (kdtree.cpp:279-301); returns
 // the distance or -1.  The edge-mask rejection is taken before the plane
 // distance (same result, less work).
-__device__ __forceinline__ float tri_test(f3 v0, f3 v1, f3 v2, const RayQ& q) {
+__device__ __forceinline__ float tri_test(f3 v0, f3 v1, f3 v2, const RayQ& q, float* dd_out = nullptr) {
     const f3 l0 = v1 - v0, l1 = v2 - v1, l2 = v0 - v2;
     const f3 r0 = v0 - q.o, r1 = v1 - q.o, r2 = v2 - q.o;
     const float s0 = dot(q.d, cross(l0, r0));
@@ -201,10 +219,16 @@ __device__ __forceinline__ float tri_test(f3 v0, f3 v1, f3 v2, const RayQ& q) {
     const f3 n = normalize(cross(l0, l1));
     const float od = dot(n, r2);
     const float dd = dot(n, q.d);
+    if (dd_out) *dd_out = dd;
     if (dd == 0.f) return -1.f;
     const float t = od / dd;
     if (t < 0.f) return -1.f;
     return t;
+}
+
+// pruning stays on only while the closest hit is not a near-grazing one
+__device__ __forceinline__ void graze_check(RayQ& q, float dd) {
+    if (fabsf(dd) < GRAZE_COS * length(q.d)) q.pf = __int_as_float(0x7f800000);
 }
 
 // Mesh::getWorldNormal without vertex normals (mesh.h:47-56)
@@ -230,39 +254,44 @@ struct Hit {
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 __device__ __forceinline__ uint4 ldg4u(const uint4* p) { return __ldg(p); }
 
-template <bool FILTERED>
-__device__ __forceinline__ void leaf_test(const DevTree& T, uint32_t first, uint32_t count, const RayQ& q, int inside,
+template <bool FILTERED, bool PRUNE>
+__device__ __forceinline__ void leaf_test(const DevTree& T, uint32_t first, uint32_t count, RayQ& q, int inside,
                                           int contact, Hit& h) {
     for (uint32_t k = 0; k < count; k++) {
         const int slot = (int)(first + k);
         const TriRec* tr = T.tris + slot;
         const float4 a = ldg4(&tr->v0), b = ldg4(&tr->v1), c = ldg4(&tr->v2);
         const f3 v0 = xyz(a), v1 = xyz(b), v2 = xyz(c);
-        const float t = tri_test(v0, v1, v2, q);
+        float dd;
+        const float t = tri_test(v0, v1, v2, q, &dd);
         if (t >= 0.f && (t < h.t || (t == h.t && slot > h.slot))) {
             if (FILTERED) {
                 if (!noself_legal(inside, contact, (int)__float_as_uint(b.w), q.d, face_normal(v0, v1, v2))) continue;
             }
             h.t = t;
             h.slot = slot;
+            if (PRUNE) graze_check(q, dd);
         }
     }
 }
 
 // The same with the filter chosen per ray (eye rays are traced without one)
-__device__ __forceinline__ void leaf_test_dyn(const TriRec* tris, uint32_t first, uint32_t count, const RayQ& q,
-                                              bool filt, int inside, int contact, Hit& h) {
+template <bool PRUNE>
+__device__ __forceinline__ void leaf_test_dyn(const TriRec* tris, uint32_t first, uint32_t count, RayQ& q, bool filt,
+                                              int inside, int contact, Hit& h) {
     for (uint32_t k = 0; k < count; k++) {
         const int slot = (int)(first + k);
         const TriRec* tr = tris + slot;
         const float4 a = ldg4(&tr->v0), b = ldg4(&tr->v1), c = ldg4(&tr->v2);
         const f3 v0 = xyz(a), v1 = xyz(b), v2 = xyz(c);
-        const float t = tri_test(v0, v1, v2, q);
+        float dd;
+        const float t = tri_test(v0, v1, v2, q, &dd);
         if (t >= 0.f && (t < h.t || (t == h.t && slot > h.slot))) {
             if (filt && !noself_legal(inside, contact, (int)__float_as_uint(b.w), q.d, face_normal(v0, v1, v2)))
                 continue;
             h.t = t;
             h.slot = slot;
+            if (PRUNE) graze_check(q, dd);
         }
     }
 }
@@ -271,15 +300,16 @@ __device__ __forceinline__ void leaf_test_dyn(const TriRec* tris, uint32_t first
 // at most `cap` of them (cap >= tree depth + 2 always suffices; a traversal
 // that would exceed it stops and sets bit 0 of *err instead of writing past).
 template <bool FILTERED, bool PRUNE>
-__device__ __forceinline__ Hit trace_closest(const DevTree& T, const RayQ& q, int inside, int contact, uint32_t* stack,
-                                             int stride, int cap, unsigned int* err) {
+__device__ __forceinline__ Hit trace_closest(const DevTree& T, const RayQ& q0, int inside, int contact,
+                                             uint32_t* stack, int stride, int cap, unsigned int* err) {
+    RayQ q = q0;
     Hit h;
     h.t = __int_as_float(0x7f800000);
     h.slot = -1;
     float tn;
     if (!box_pred(root_box(T), q, &tn)) return h;
     if (T.root_w1 & LEAF_FLAG) {
-        leaf_test<FILTERED>(T, T.root_w0, T.root_w1 & ~LEAF_FLAG, q, inside, contact, h);
+        leaf_test<FILTERED, PRUNE>(T, T.root_w0, T.root_w1 & ~LEAF_FLAG, q, inside, contact, h);
         return h;
     }
     int sp = 0;
@@ -304,7 +334,7 @@ __device__ __forceinline__ Hit trace_closest(const DevTree& T, const RayQ& q, in
         const bool ll = hl && (W.y & LEAF_FLAG), lr = hr && (W.w & LEAF_FLAG);
         for (int k = 0, nk = (int)ll + (int)lr; k < nk; k++) {
             const bool right = k == 1 || !ll;
-            leaf_test<FILTERED>(T, right ? W.z : W.x, (right ? W.w : W.y) & ~LEAF_FLAG, q, inside, contact, h);
+            leaf_test<FILTERED, PRUNE>(T, right ? W.z : W.x, (right ? W.w : W.y) & ~LEAF_FLAG, q, inside, contact, h);
         }
         hl = hl && !ll;
         hr = hr && !lr;

@@ -102,12 +102,12 @@ __device__ __forceinline__ void lane_step(TraceLane& L, uint32_t* stack, int str
 }
 
 // The postponed leaves of a lane, through one code path for the warp.
-template <bool STATS>
+template <bool PRUNE, bool STATS>
 __device__ __forceinline__ void lane_leaves(TraceLane& L) {
     for (int k = 0; k < L.npend; ++k) {
         const uint32_t first = k ? L.lf1 : L.lf0, count = k ? L.lc1 : L.lc0;
         if (STATS) L.n_tri += count;
-        leaf_test_dyn(L.tris, first, count, L.q, L.filt, L.inside, L.contact, L.h);
+        leaf_test_dyn<PRUNE>(L.tris, first, count, L.q, L.filt, L.inside, L.contact, L.h);
     }
     L.npend = 0;
 }
@@ -156,7 +156,7 @@ __device__ __forceinline__ void warp_trace(Src& src, uint64_t n, unsigned long l
         const bool pending = active && L.npend > 0;
         const unsigned sm = __ballot_sync(FULL, searching), pm = __ballot_sync(FULL, pending);
         if (pm && (sm == 0 || __popc(pm) >= tune.leaf_min)) {
-            if (pending) lane_leaves<STATS>(L);
+            if (pending) lane_leaves<PRUNE, STATS>(L);
         } else if (searching) {
             lane_step<PRUNE, STATS>(L, stack, stride, cap, err);
         }

@@ -6,7 +6,8 @@
 // on the GPU through the C ABI of libwalkray_gpu.so (include/walkray.h).
 //
 // This file is compiled inside a WalkRay source tree (it includes WalkRay's
-// headers); see INTEGRATION.md for the two lines that register it.
+// headers); registering it takes one include and one name branch in
+// Config::load (config.cpp:528-573).
 #pragma once
 
 #include <functional>
