@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define WR_ABI_VERSION 1u
+#define WR_ABI_VERSION 2u
 
 /* status codes */
 #define WR_OK 0
@@ -349,8 +349,13 @@ typedef uint64_t wr_req_id;
 typedef struct wr_serve_desc {
     uint64_t film_bytes; /* device memory for request films; 0 = a quarter of the context budget */
     uint32_t max_active; /* requests in flight at once; 0 = 64 */
-    uint32_t pad;
+    uint32_t flags;      /* WR_SERVE_* */
 } wr_serve_desc;
+/* Queue slots freed by finished paths go to the running requests in
+ * admission order (first come, first served) instead of in equal shares to
+ * every request with paths left (the default: a small request admitted
+ * behind a large one starts at once). */
+#define WR_SERVE_FIFO 1u
 
 typedef struct wr_request_desc {
     wr_scene_id scene;
@@ -395,13 +400,23 @@ typedef struct wr_wavefront_config {
                                 0 = default); both also apply to wr_trace_closest */
     int32_t drain_paths;     /* wr_render: once every path is generated and at most this many remain,
                                 finish them in one per-path kernel (0 = never) */
+    int32_t pixel_tile;      /* camera paths generated tile by tile, square tiles of this many pixels a
+                                side (0 = row by row); the image does not depend on it */
+    int32_t steps_per_turn;  /* traversal: steps a searching lane takes per turn of a warp's loop (1..8,
+                                0 = default 1); also applies to wr_trace_closest */
     double mpaths_per_s;     /* filled by wr_autotune */
 } wr_wavefront_config;
 
 int wr_set_wavefront_config(wr_ctx* ctx, const wr_wavefront_config* cfg);
 
-/* Times short wavefront renders (spp_per_trial samples per pixel) of `scene`
- * over a grid of configurations and keeps the fastest in the context. */
+/* Picks the wavefront configuration for `scene` by timing short renders
+ * (spp_per_trial samples per pixel, max_path_len) on the device: starting
+ * from the defaults, one dimension at a time -- paths in flight, traversal
+ * CTAs per SM, the warp loop's refill and leaf thresholds and steps per
+ * turn, the camera-path pixel tile, bounce iterations per graph launch --
+ * keeping each value that renders faster (coordinate descent).  The best
+ * configuration stays in the context; `best` gets it with its Mpaths/s.  No
+ * reference counterpart. */
 int wr_autotune(wr_ctx* ctx, wr_scene_id scene, uint32_t spp_per_trial, uint32_t max_path_len,
                 wr_wavefront_config* best);
 

@@ -23,7 +23,7 @@ def test_library_exports_declared_symbols(built):
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
     v = C.c_uint32()
-    assert lib.wr_get_abi_version(C.byref(v)) == 0 and v.value == 1
+    assert lib.wr_get_abi_version(C.byref(v)) == 0 and v.value == 2
 
 
 @pytest.mark.parametrize("name", ["cornell", "ico4", "mixed_l2", "media_small"])

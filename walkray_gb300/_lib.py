@@ -96,11 +96,13 @@ class wr_render_desc(C.Structure):
 
 class wr_wavefront_config(C.Structure):
     _fields_ = [("capacity", C.c_uint32), ("extend_block", C.c_int32), ("shade_block", C.c_int32),
-                ("ctas_per_sm", C.c_int32), ("iters_per_graph", C.c_int32), ("refill_min", C.c_int32), ("leaf_min", C.c_int32), ("drain_paths", C.c_int32), ("mpaths_per_s", C.c_double)]
+                ("ctas_per_sm", C.c_int32), ("iters_per_graph", C.c_int32), ("refill_min", C.c_int32),
+                ("leaf_min", C.c_int32), ("drain_paths", C.c_int32), ("pixel_tile", C.c_int32),
+                ("steps_per_turn", C.c_int32), ("mpaths_per_s", C.c_double)]
 
 
 class wr_serve_desc(C.Structure):
-    _fields_ = [("film_bytes", C.c_uint64), ("max_active", C.c_uint32), ("pad", C.c_uint32)]
+    _fields_ = [("film_bytes", C.c_uint64), ("max_active", C.c_uint32), ("flags", C.c_uint32)]
 
 
 class wr_request_desc(C.Structure):
@@ -127,6 +129,7 @@ WR_RENDER_EXACT_TRAVERSAL = 2
 WR_RENDER_NEE_MIS = 4
 WR_RENDER_PHONG_MIRROR = 8
 WR_CTX_EXACT_TRAVERSAL = 1
+WR_SERVE_FIFO = 1
 
 HIT_DTYPE = np.dtype([("tri", "<u4"), ("t", "<f4"), ("b1", "<f4"), ("b2", "<f4")])
 

@@ -172,12 +172,14 @@ class Context:
 
     def set_wavefront_config(self, capacity: int, extend_block: int = 128, shade_block: int = 128,
                              ctas_per_sm: int = 0, iters_per_graph: int = 4, refill_min: int = 0,
-                             leaf_min: int = 0, drain_paths: int = 0) -> None:
-        """Queue sizes and block shapes of the wavefront renderer; refill_min and
-        leaf_min (0 = defaults) tune the warp traversal loop of both the
-        extend stage and trace_closest."""
+                             leaf_min: int = 0, drain_paths: int = 0, pixel_tile: int = 0,
+                             steps_per_turn: int = 0) -> None:
+        """Queue sizes and block shapes of the wavefront renderer; refill_min,
+        leaf_min and steps_per_turn (0 = defaults) tune the warp traversal
+        loop of both the extend stage and trace_closest; pixel_tile orders
+        camera paths by square pixel tiles (0 = rows)."""
         c = L.wr_wavefront_config(capacity, extend_block, shade_block, ctas_per_sm, iters_per_graph, refill_min,
-                                  leaf_min, drain_paths, 0.0)
+                                  leaf_min, drain_paths, pixel_tile, steps_per_turn, 0.0)
         self._check(self.lib.wr_set_wavefront_config(self.h, C.byref(c)))
 
     def autotune(self, sid: int, spp_per_trial: int, max_path_len: int) -> dict:
@@ -223,9 +225,11 @@ class Server:
     """The serving loop of a Context (wr_serve_start ... wr_serve_stop):
     requests admitted by film memory, their paths sharing the wavefront queues."""
 
-    def __init__(self, ctx: Context, film_bytes: int = 0, max_active: int = 0):
+    def __init__(self, ctx: Context, film_bytes: int = 0, max_active: int = 0, fifo: bool = False):
+        """`fifo`: queue slots go to the requests in admission order instead
+        of in equal shares (WR_SERVE_FIFO)."""
         self.ctx = ctx
-        d = L.wr_serve_desc(film_bytes, max_active, 0)
+        d = L.wr_serve_desc(film_bytes, max_active, L.WR_SERVE_FIFO if fifo else 0)
         ctx._check(ctx.lib.wr_serve_start(ctx.h, C.byref(d)))
         self.sizes: dict[int, tuple[int, int]] = {}
 

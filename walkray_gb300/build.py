@@ -4,10 +4,19 @@ the oracle programs.
     python -m walkray_gb300.build            # library + oracle
     python -m walkray_gb300.build --lib      # library only
 
-Every translation unit is compiled by nvcc in parallel; kernels use
-``-fmad=false`` (no contraction) with IEEE division and square root, host code
-``-ffp-contract=off``, so that traversal arithmetic is bit-identical to the
-reference's FP32 code on both x86-64 and aarch64 hosts.
+Every translation unit is compiled by nvcc in parallel, with IEEE division
+and square root.  The traversal code whose results must equal the
+reference's FP32 bit for bit (box face test, triangle test, face normals,
+NoSelfCondition) spells every product and sum as an unfused round-to-nearest
+intrinsic (wr_device.cuh: add_x, mul_x, ...), which no compiler setting
+contracts, so the path tracer's translation units are compiled with
+contraction into fused multiply-adds (-fmad=true).  The bidirectional /
+VCM / photon-mapping unit (bpt.cu) is not: its estimators keep or drop
+merges and photons by the last bit of hit points against the light points'
+bounding box and the hash grid, as the reference's unfused FP32 does, and
+contraction moved those decisions far enough to shift its images off the
+reference's (measured: photon mapping on the Cornell box 4 % brighter).
+Host code uses -ffp-contract=off, on x86-64 and aarch64 alike.
 """
 from __future__ import annotations
 
@@ -23,6 +32,7 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libwalkray_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+UNFUSED = {"bpt.cu"}  # translation units compiled without contraction (see the module docstring)
 
 
 def _nvcc() -> str:
@@ -39,19 +49,25 @@ def _sources():
 def _compile(src: str, nvcc: str) -> str:
     out = os.path.join(OBJ, src.rsplit(".", 1)[0] + ".o")
     path = os.path.join(CSRC, src)
-    deps = [path] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
-    deps.append(os.path.join(ROOT, "include", "walkray.h"))
-    if os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(d) for d in deps):
-        return out
     host = "-Xcompiler=-fPIC,-fopenmp,-ffp-contract=off,-O3"
     if src.endswith(".cu"):
-        cmd = [nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
+        fmad = "-fmad=false" if src in UNFUSED else "-fmad=true"
+        cmd = [nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", fmad, "-prec-div=true", "-prec-sqrt=true",
                host, "-c", path, "-o", out]
     else:
         cmd = [nvcc, "-std=c++17", "-O3", host, "-c", path, "-o", out]
+    # an object is current when it is newer than its sources and was built by the same command
+    stamp = out + ".cmd"
+    deps = [path] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
+    deps.append(os.path.join(ROOT, "include", "walkray.h"))
+    if (os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(d) for d in deps)
+            and os.path.exists(stamp) and open(stamp).read() == " ".join(cmd)):
+        return out
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+    with open(stamp, "w") as f:
+        f.write(" ".join(cmd))
     return out
 
 

@@ -333,6 +333,7 @@ WfConfig wf_tuned_config(wr_ctx* ctx) {
     if (ctx->wf_iters) c.iters_per_graph = ctx->wf_iters;
     c.trace = trace_tune_of(ctx);
     c.drain_paths = ctx->wf_drain_paths;
+    c.pixel_tile = ctx->wf_pixel_tile;
     return c;
 }
 

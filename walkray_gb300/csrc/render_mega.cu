@@ -8,7 +8,7 @@
 
 namespace wr {
 
-template <bool STATS>
+template <bool STATS, bool MIS>
 __global__ void __launch_bounds__(128) k_megakernel(RenderScene S, RenderParams P, float* __restrict__ film,
                                                       float* __restrict__ film2, unsigned int* __restrict__ err) {
     extern __shared__ uint32_t s_stack[];
@@ -44,9 +44,9 @@ __global__ void __launch_bounds__(128) k_megakernel(RenderScene S, RenderParams 
             }
             set_hit(S, cur, h);
             filtered = true;
-            const bool done = path_advance(S, cur, color, prev_d, depth, st, g, P.max_path_len, P.flags, result,
-                                           nee_here, mis_pdf, lr, has_lr);
-            if (has_lr) {  // the light connection of WR_RENDER_NEE_MIS, traced inline
+            const bool done = path_advance<MIS>(S, cur, color, prev_d, depth, st, g, P.max_path_len, P.flags,
+                                                result, nee_here, mis_pdf, lr, has_lr);
+            if (MIS && has_lr) {  // the light connection of WR_RENDER_NEE_MIS, traced inline
                 RayQ lq = make_rayq(lr.o, lr.d, S.tree.scene_mag);
                 lq.pf = pf;
                 const Hit lh =
@@ -89,7 +89,9 @@ cudaError_t launch_megakernel(const RenderScene& S, const RenderParams& P, float
     const size_t smem = (size_t)P.stack_cap * block * sizeof(uint32_t);
     const uint32_t npix = S.cam.width * S.cam.height;
     const int grid = (int)((npix + block - 1) / block);
-    auto kern = film2 ? k_megakernel<true> : k_megakernel<false>;
+    const bool mis = (P.flags & WR_RENDER_NEE_MIS) != 0;
+    auto kern = film2 ? (mis ? k_megakernel<true, true> : k_megakernel<true, false>)
+                      : (mis ? k_megakernel<false, true> : k_megakernel<false, false>);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;

@@ -5,7 +5,10 @@
 // One host thread owns the wavefront engine while serving.  Each turn it
 // (1) admits queued requests in FIFO order while a job slot is free and the
 // request's FP32 film fits in the serving film arena, (2) replays the
-// captured bounce loop once, (3) reads the per-job path counters and retires
+// captured bounce loop once -- its generate stage shares the queue slots that
+// finished paths free among the running requests (k_wf_plan: equal shares,
+// or admission order with WR_SERVE_FIFO) -- (3) reads the per-job path
+// counters and retires
 // every request whose paths have all reached its film (copy to the host,
 // free the arena block and the slot).  New requests therefore join while
 // older ones run, and their paths share the same queues; a request's image
@@ -266,6 +269,7 @@ int wr_serve_start(wr_ctx* ctx, const wr_serve_desc* desc) {
         WR_CUDA(ctx, cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
         int rc = wf_engine_get(ctx, wf_tuned_config(ctx), &S->E);
         if (rc != WR_OK) return rc;
+        if ((rc = wf_set_equal_share(ctx, S->E, !(desc && (desc->flags & WR_SERVE_FIFO)))) != WR_OK) return rc;
         // start from an empty job table and empty queues
         std::vector<WfSlotUpdate> clear;
         for (uint32_t k = 0; k < wf_max_jobs(); k++) {

@@ -28,9 +28,17 @@ struct WfPath {
     f3 acc;         // light connections counted so far (WR_RENDER_NEE_MIS)
 };
 
+__device__ __forceinline__ int4 as_i4(float4 v) {
+    return make_int4(__float_as_int(v.x), __float_as_int(v.y), __float_as_int(v.z), __float_as_int(v.w));
+}
+__device__ __forceinline__ float4 as_f4(int4 v) {
+    return make_float4(__int_as_float(v.x), __int_as_float(v.y), __int_as_float(v.z), __int_as_float(v.w));
+}
+
 __device__ __forceinline__ void wf_load(const WfSide& X, uint32_t i, WfPath& p) {
-    const float4 a0 = X.a0[i], a1 = X.a1[i], a2 = X.a2[i], a3 = X.a3[i];
-    const int4 ids = X.ids[i], misc = X.misc[i], stk = X.stk[i];
+    const float4* r = X.rec + (size_t)WF_REC * i;
+    const float4 a0 = r[WF_O], a1 = r[WF_D], a2 = r[WF_RAD], a3 = r[WF_COL];
+    const int4 ids = as_i4(r[WF_IDS]), misc = as_i4(r[WF_MISC]), stk = as_i4(r[WF_STK]);
     p.cur = ray_default();
     p.cur.o = mk(a0.x, a0.y, a0.z);
     p.cur.oP = a0.w;
@@ -51,7 +59,7 @@ __device__ __forceinline__ void wf_load(const WfSide& X, uint32_t i, WfPath& p) 
     p.st.v1 = stk.y;
     p.st.v2 = stk.z;
     p.st.v3 = stk.w;
-    const float4 a4 = X.a4[i];
+    const float4 a4 = r[WF_PREV];
     p.prev_d = mk(a4.x, a4.y, a4.z);
     p.mis_pdf = a4.w;
     p.acc = mk(0, 0, 0);
@@ -63,15 +71,16 @@ __device__ __forceinline__ void wf_load_acc(const WfSide& X, uint32_t i, WfPath&
 }
 
 __device__ __forceinline__ void wf_store(const WfSide& Y, uint32_t j, const WfPath& p) {
-    Y.a0[j] = make_float4(p.cur.o.x, p.cur.o.y, p.cur.o.z, p.cur.oP);
-    Y.a1[j] = make_float4(p.cur.d.x, p.cur.d.y, p.cur.d.z, p.cur.dP);
-    Y.a2[j] = make_float4(p.cur.rad.x, p.cur.rad.y, p.cur.rad.z, p.cur.cnorm.x);
-    Y.a3[j] = make_float4(p.color.x, p.color.y, p.color.z, p.cur.cnorm.y);
-    Y.ids[j] = make_int4(p.cur.inside, p.cur.contact, p.job, (int)p.pixel);
-    Y.misc[j] = make_int4((int)p.sample, (int)p.dim, (int)(p.depth | ((uint32_t)p.st.n << 16)),
-                          __float_as_int(p.cur.cnorm.z));
-    Y.stk[j] = make_int4(p.st.v0, p.st.v1, p.st.v2, p.st.v3);
-    Y.a4[j] = make_float4(p.prev_d.x, p.prev_d.y, p.prev_d.z, p.mis_pdf);
+    float4* r = Y.rec + (size_t)WF_REC * j;
+    r[WF_O] = make_float4(p.cur.o.x, p.cur.o.y, p.cur.o.z, p.cur.oP);
+    r[WF_D] = make_float4(p.cur.d.x, p.cur.d.y, p.cur.d.z, p.cur.dP);
+    r[WF_IDS] = as_f4(make_int4(p.cur.inside, p.cur.contact, p.job, (int)p.pixel));
+    r[WF_MISC] = as_f4(make_int4((int)p.sample, (int)p.dim, (int)(p.depth | ((uint32_t)p.st.n << 16)),
+                                 __float_as_int(p.cur.cnorm.z)));
+    r[WF_RAD] = make_float4(p.cur.rad.x, p.cur.rad.y, p.cur.rad.z, p.cur.cnorm.x);
+    r[WF_COL] = make_float4(p.color.x, p.color.y, p.color.z, p.cur.cnorm.y);
+    r[WF_STK] = as_f4(make_int4(p.st.v0, p.st.v1, p.st.v2, p.st.v3));
+    r[WF_PREV] = make_float4(p.prev_d.x, p.prev_d.y, p.prev_d.z, p.mis_pdf);
 }
 
 __device__ __forceinline__ void wf_store_acc(const WfSide& Y, uint32_t j, const WfPath& p) {
@@ -116,7 +125,7 @@ __global__ void __launch_bounds__(256) k_wf_sort(const RenderScene* __restrict__
         if (valid) {
             const int slot = hits[i].x;
             if (slot >= 0) {
-                const int4 ids = X.ids[i];
+                const int4 ids = as_i4(X.rec[(size_t)WF_REC * i + WF_IDS]);
                 const RenderScene& S = scenes[jobs[ids.z].scene];
                 const int self = ids.x >= 0 ? ids.x : (int)__float_as_uint(__ldg(&S.tree.tris[slot].v1.w));
                 key = 1 + (int)obj_type(S, self);
@@ -206,8 +215,9 @@ struct ExtendSrc {
     unsigned long long n_rays, n_box, n_tri;  // this thread's work counts (profiling launches)
 
     __device__ __forceinline__ void load(uint64_t id, TraceLane& L, uint32_t* stack, int stride) {
-        const float4 a0 = X.a0[id], a1 = X.a1[id];
-        const int4 ids = X.ids[id];
+        const float4* r = X.rec + (size_t)WF_REC * id;
+        const float4 a0 = r[WF_O], a1 = r[WF_D];
+        const int4 ids = as_i4(r[WF_IDS]);
         const WfJob& J = jobs[ids.z];
         const DevTree& T = scenes[J.scene].tree;
         L.pairs = T.pairs;
@@ -267,7 +277,10 @@ static ExtendKernel extend_kernel(int ctas_per_sm, bool stats) {
     return stats ? k_wf_extend<true, 0> : k_wf_extend<false, 0>;
 }
 
-// shade: one bounce per path; survivors compacted into Y, finished paths to the film
+// shade: one bounce per path; survivors compacted into Y, finished paths to
+// the film.  MIS: compiled with the WR_RENDER_NEE_MIS code (launched while a
+// job with that flag is in the table).
+template <bool MIS>
 __global__ void __launch_bounds__(128, 4) k_wf_shade(const RenderScene* __restrict__ scenes,
                                                     const WfJob* __restrict__ jobs,
                                                     WfJobCounters* __restrict__ counters, WfSide X,
@@ -304,7 +317,7 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade(const RenderScene* __restri
             wf_load(X, i, p);
             const WfJob& J = jobs[p.job];
             const RenderScene& S = scenes[J.scene];
-            mis = (J.flags & WR_RENDER_NEE_MIS) != 0;
+            mis = MIS && (J.flags & WR_RENDER_NEE_MIS) != 0;
             if (mis) wf_load_acc(X, i, p);
             const int2 hv = hits[i];
             Hit h;
@@ -319,8 +332,8 @@ __global__ void __launch_bounds__(128, 4) k_wf_shade(const RenderScene* __restri
                 nee_here = nee;
             } else {
                 set_hit(S, p.cur, h);
-                done = path_advance(S, p.cur, p.color, p.prev_d, p.depth, p.st, g, J.max_path_len, J.flags, result,
-                                    nee_here, p.mis_pdf, lr, has_lr);
+                done = path_advance<MIS>(S, p.cur, p.color, p.prev_d, p.depth, p.st, g, J.max_path_len, J.flags,
+                                         result, nee_here, p.mis_pdf, lr, has_lr);
             }
             if (nee_here) shadow = nee_prepare(S, p.cur, p.prev_d, p.color, g, sr);
             p.dim = g.dim;
@@ -406,8 +419,8 @@ __global__ void __launch_bounds__(128) k_wf_drain(const RenderScene* __restrict_
         }
         set_hit(S, p.cur, h);
         filtered = true;
-        const bool done = path_advance(S, p.cur, p.color, p.prev_d, p.depth, p.st, g, J.max_path_len, J.flags,
-                                       result, nee_here, p.mis_pdf, lr, has_lr);
+        const bool done = path_advance<true>(S, p.cur, p.color, p.prev_d, p.depth, p.st, g, J.max_path_len,
+                                             J.flags, result, nee_here, p.mis_pdf, lr, has_lr);
         if (has_lr) {
             RayQ lq = make_rayq(lr.o, lr.d, S.tree.scene_mag);
             lq.pf = pf;
@@ -435,68 +448,139 @@ __global__ void __launch_bounds__(128) k_wf_drain(const RenderScene* __restrict_
         atomicAdd(&counters[p.job].finished, (unsigned long long)__popc(same));
 }
 
-// generate: new camera paths into the free slots of Y, from the job slots
-// listed in `order` (admission order); the list lives in device memory so the
-// captured graph does not change when jobs come and go
-__global__ void __launch_bounds__(128) k_wf_generate(const WfJob* __restrict__ jobs, const int* __restrict__ order,
-                                                       WfJobCounters* __restrict__ counters, WfSide Y,
-                                                       uint32_t capacity) {
-    const int njobs = order[0];
+// plan: how the free slots of Y are shared out among the jobs this turn.
+// One block, one thread per listed job (`order`: admission order).  Each job
+// with paths left gets an equal share of the free slots (processor sharing:
+// a small request admitted behind a large one starts at once), capped by what
+// it has left; slots nobody's share used go to the jobs in admission order.
+// With `equal_share` off, every slot goes in admission order (first come,
+// first served).  The plan reserves each job's index range [first, first +
+// quota) by advancing its claim counter; the generate kernel then maps queue
+// position t to a job and a path index without atomics.  Which paths a job
+// renders does not depend on the plan, only when.
+__device__ __forceinline__ unsigned long long block_excl_scan(unsigned long long v, unsigned long long* buf) {
+    const int k = threadIdx.x;
+    buf[k] = v;
+    __syncthreads();
+    for (int d = 1; d < (int)blockDim.x; d <<= 1) {
+        const unsigned long long add = k >= d ? buf[k - d] : 0ull;
+        __syncthreads();
+        buf[k] += add;
+        __syncthreads();
+    }
+    const unsigned long long incl = buf[k];
+    __syncthreads();
+    return incl - v;
+}
+
+__global__ void __launch_bounds__(WF_MAX_JOBS) k_wf_plan(const WfJob* __restrict__ jobs, const int* __restrict__ order,
+                                                          WfJobCounters* __restrict__ counters, WfSide Y,
+                                                          uint32_t capacity, int equal_share, WfPlan P) {
+    __shared__ unsigned long long buf[WF_MAX_JOBS];
+    __shared__ unsigned long long s_total_q;
+    const int n = order[0];
+    const int k = threadIdx.x;
     const uint32_t survivors = Y.counts[0];
-    const uint32_t free_slots = capacity > survivors ? capacity - survivors : 0;
-    const uint32_t step = gridDim.x * blockDim.x;
-    const unsigned lane = threadIdx.x & 31u;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < free_slots; base += step) {
-        const bool want = base + threadIdx.x < free_slots;
-        bool have = false;
-        int jid = -1;
-        unsigned long long idx = 0;
-        unsigned need = __ballot_sync(0xffffffffu, want);
-        for (int k = 0; k < njobs && need; k++) {
-            const int j = order[1 + k];
-            const WfJob& J = jobs[j];
-            // one lane reads the claim counter so that the skip decision is warp-uniform
-            unsigned long long cl = 0;
-            if (lane == 0) cl = *(volatile unsigned long long*)&counters[j].claimed;
-            cl = __shfl_sync(0xffffffffu, cl, 0);
-            if (!J.active || cl >= J.total) continue;
-            const int leader = __ffs(need) - 1;
-            unsigned long long b = 0;
-            if ((int)lane == leader) b = atomicAdd(&counters[j].claimed, (unsigned long long)__popc(need));
-            b = __shfl_sync(0xffffffffu, b, leader);
-            if ((need >> lane) & 1u) {
-                const unsigned long long mine = b + __popc(need & ((1u << lane) - 1u));
-                if (mine < J.total) {
-                    have = true;
-                    jid = j;
-                    idx = mine;
-                }
-            }
-            need = __ballot_sync(0xffffffffu, want && !have);
+    const unsigned long long free_slots = capacity > survivors ? capacity - survivors : 0u;
+    int j = -1;
+    unsigned long long rem = 0, claimed = 0;
+    if (k < n) {
+        j = order[1 + k];
+        const WfJob& J = jobs[j];
+        claimed = counters[j].claimed;
+        rem = (J.active && claimed < J.total) ? J.total - claimed : 0ull;
+    }
+    const int active = __syncthreads_count(rem > 0);
+    const unsigned long long share = (equal_share && active) ? free_slots / (unsigned long long)active : 0ull;
+    const unsigned long long q = rem < share ? rem : share;
+    const unsigned long long q_before = block_excl_scan(q, buf);
+    if (k == (int)blockDim.x - 1) s_total_q = q_before + q;
+    __syncthreads();
+    const unsigned long long leftover = free_slots - s_total_q;
+    unsigned long long need = rem - q;
+    need = need < free_slots ? need : free_slots;
+    const unsigned long long need_before = block_excl_scan(need, buf);
+    unsigned long long extra = leftover > need_before ? leftover - need_before : 0ull;
+    extra = extra < need ? extra : need;
+    const unsigned long long quota = q + extra;
+    const unsigned long long off = block_excl_scan(quota, buf);
+    if (k < n) {
+        P.slot[k] = j;
+        P.first[k] = claimed;
+        P.off[k] = (uint32_t)off;
+        if (quota) counters[j].claimed = claimed + quota;
+    }
+    if (k == n - 1 || (n == 0 && k == 0)) {
+        const uint32_t total = n ? (uint32_t)(off + quota) : 0u;
+        P.off[n] = total;
+        *P.n = n;
+        Y.counts[1] = total;
+    }
+}
+
+// Pixel of the k-th camera path of a sample when paths are generated tile by
+// tile: bands of `tile` rows, each cut into tiles of `tile` columns (the last
+// band and the last tile of a band may be smaller), rows within a tile.  A
+// bijection of [0, W*H); tile 0 is row order.  Neighbouring queue entries
+// then hold neighbouring pixels, whose first bounces visit the same nodes.
+__device__ __forceinline__ uint32_t tile_pixel(uint32_t k, uint32_t W, uint32_t H, uint32_t tile) {
+    if (tile == 0 || tile >= W) return k;
+    const uint32_t band = k / (W * tile);
+    const uint32_t y0 = band * tile;
+    const uint32_t bh = min(tile, H - y0);  // rows in this band
+    const uint32_t r = k - band * W * tile;
+    const uint32_t tc = r / (tile * bh);     // tile column (the last one may be narrower)
+    const uint32_t x0 = tc * tile;
+    const uint32_t tw = min(tile, W - x0);
+    const uint32_t q = r - tc * tile * bh;
+    return (y0 + q / tw) * W + x0 + q % tw;
+}
+
+// generate: new camera paths into the free slots of Y as the plan shares
+// them out: queue position survivors + t belongs to the job whose planned
+// range holds t; the list lives in device memory so the captured graph does
+// not change when jobs come and go
+__global__ void __launch_bounds__(128) k_wf_generate(const WfJob* __restrict__ jobs, WfPlan P, WfSide Y) {
+    __shared__ uint32_t s_off[WF_MAX_JOBS + 1];
+    __shared__ int s_slot[WF_MAX_JOBS];
+    __shared__ unsigned long long s_first[WF_MAX_JOBS];
+    const int n = *P.n;
+    for (int k = threadIdx.x; k <= n; k += blockDim.x) {
+        s_off[k] = P.off[k];
+        if (k < n) {
+            s_slot[k] = P.slot[k];
+            s_first[k] = P.first[k];
         }
-        if (!__any_sync(0xffffffffu, have)) break;  // every job fully handed out
+    }
+    __syncthreads();
+    const uint32_t total = s_off[n];
+    const uint32_t survivors = Y.counts[0];
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        int lo = 0, hi = n - 1;  // the last k with s_off[k] <= t (its range is not empty)
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_off[mid] <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        const int jid = s_slot[lo];
+        const unsigned long long idx = s_first[lo] + (t - s_off[lo]);
+        const WfJob& J = jobs[jid];
         WfPath p;
-        if (have) {
-            const WfJob& J = jobs[jid];
-            p.job = jid;
-            p.pixel = (uint32_t)(idx % J.npix);
-            p.sample = J.s0 + (uint32_t)(idx / J.npix);
-            PathRng g;
-            g.init(J.seed, p.pixel, p.sample);
-            p.cur = camera_ray(J.cam, p.pixel, g);
-            p.dim = g.dim;
-            p.color = mk(1, 1, 1);
-            p.prev_d = mk(0, 0, 0);
-            p.depth = 0;
-            p.st.reset(p.cur.inside);
-            p.mis_pdf = 0.f;
-            p.acc = mk(0, 0, 0);
-        }
-        const uint32_t j = warp_append(&Y.counts[1], have, survivors);
-        if (have) {
-            wf_store(Y, j, p);
-            if (jobs[jid].flags & WR_RENDER_NEE_MIS) wf_store_acc(Y, j, p);
-        }
+        p.job = jid;
+        p.pixel = tile_pixel((uint32_t)(idx % J.npix), J.cam.width, J.cam.height, J.tile);
+        p.sample = J.s0 + (uint32_t)(idx / J.npix);
+        PathRng g;
+        g.init(J.seed, p.pixel, p.sample);
+        p.cur = camera_ray(J.cam, p.pixel, g);
+        p.dim = g.dim;
+        p.color = mk(1, 1, 1);
+        p.prev_d = mk(0, 0, 0);
+        p.depth = 0;
+        p.st.reset(p.cur.inside);
+        p.mis_pdf = 0.f;
+        p.acc = mk(0, 0, 0);
+        wf_store(Y, survivors + t, p);
+        if (J.flags & WR_RENDER_NEE_MIS) wf_store_acc(Y, survivors + t, p);
     }
 }
 
@@ -505,8 +589,10 @@ __global__ void __launch_bounds__(128) k_wf_generate(const WfJob* __restrict__ j
 // ---------------------------------------------------------------------------
 struct WfEngine {
     WfConfig cfg;
-    DeviceBuffer side_mem[2], hits, scenes, jobs, order, counters, work, err_word, shadow_mem, sort_mem;
+    DeviceBuffer side_mem[2], hits, scenes, jobs, order, counters, work, err_word, shadow_mem, sort_mem, plan_mem;
     WfSide side[2];
+    WfPlan plan{};
+    int equal_share = 1;  // the plan's policy (captured into the graph)
     WfShadow shadow{};
     WfSort sort{};
     int grid_sort = 0;
@@ -521,6 +607,7 @@ struct WfEngine {
     size_t smem_extend = 0;
     cudaGraphExec_t graph = nullptr;
     int graph_stack = -1;
+    bool mis_any = false;  // a job in the table has WR_RENDER_NEE_MIS: the shade stage with that code
     WfJobCounters* host_counters = nullptr;  // pinned
     ~WfEngine() {
         if (graph) cudaGraphExecDestroy(graph);
@@ -532,19 +619,12 @@ const WfConfig& wf_config(const WfEngine* E) { return E->cfg; }
 
 static int alloc_side(wr_ctx* ctx, WfEngine* E, int k) {
     const size_t Q = E->cfg.capacity;
-    const size_t bytes = Q * (6 * sizeof(float4) + 3 * sizeof(int4)) + 256;
+    const size_t bytes = Q * (WF_REC + 1) * sizeof(float4) + 256;
     WR_CUDA(ctx, E->side_mem[k].reserve(bytes));
     char* p = E->side_mem[k].as<char>();
     WfSide& S = E->side[k];
-    S.a0 = reinterpret_cast<float4*>(p);
-    S.a1 = S.a0 + Q;
-    S.a2 = S.a1 + Q;
-    S.a3 = S.a2 + Q;
-    S.ids = reinterpret_cast<int4*>(S.a3 + Q);
-    S.misc = S.ids + Q;
-    S.stk = S.misc + Q;
-    S.a4 = reinterpret_cast<float4*>(S.stk + Q);
-    S.a5 = S.a4 + Q;
+    S.rec = reinterpret_cast<float4*>(p);
+    S.a5 = S.rec + (size_t)WF_REC * Q;
     S.counts = reinterpret_cast<unsigned int*>(S.a5 + Q);
     WR_CUDA(ctx, cudaMemset(S.counts, 0, 2 * sizeof(unsigned int)));
     return WR_OK;
@@ -556,8 +636,10 @@ int wf_engine_get(wr_ctx* ctx, const WfConfig& cfg, WfEngine** out) {
     if (cur && cur->cfg.capacity == cfg.capacity && cur->cfg.extend_block == cfg.extend_block &&
         cur->cfg.shade_block == cfg.shade_block && cur->cfg.ctas_per_sm == cfg.ctas_per_sm &&
         cur->cfg.iters_per_graph == cfg.iters_per_graph && cur->cfg.trace.refill_min == cfg.trace.refill_min &&
+        cur->cfg.trace.steps == cfg.trace.steps &&
         cur->cfg.trace.leaf_min == cfg.trace.leaf_min) {
         cur->cfg.drain_paths = cfg.drain_paths;  // host-side only
+        cur->cfg.pixel_tile = cfg.pixel_tile;    // a job field, set when jobs are written
         *out = cur;
         return WR_OK;
     }
@@ -594,6 +676,12 @@ int wf_engine_get(wr_ctx* ctx, const WfConfig& cfg, WfEngine** out) {
     WR_CUDA(ctx, cudaMemset(E->jobs.p, 0, sizeof(WfJob) * WF_MAX_JOBS));
     WR_CUDA(ctx, E->order.reserve(sizeof(int) * (WF_MAX_JOBS + 1)));
     WR_CUDA(ctx, cudaMemset(E->order.p, 0, sizeof(int) * (WF_MAX_JOBS + 1)));
+    WR_CUDA(ctx, E->plan_mem.reserve(sizeof(unsigned long long) * WF_MAX_JOBS + sizeof(int) * WF_MAX_JOBS +
+                                     sizeof(uint32_t) * (WF_MAX_JOBS + 1) + 64));
+    E->plan.first = E->plan_mem.as<unsigned long long>();
+    E->plan.slot = reinterpret_cast<int*>(E->plan.first + WF_MAX_JOBS);
+    E->plan.off = reinterpret_cast<uint32_t*>(E->plan.slot + WF_MAX_JOBS);
+    E->plan.n = reinterpret_cast<int*>(E->plan.off + WF_MAX_JOBS + 1);
     WR_CUDA(ctx, E->counters.reserve(sizeof(WfJobCounters) * WF_MAX_JOBS));
     WR_CUDA(ctx, cudaMemset(E->counters.p, 0, sizeof(WfJobCounters) * WF_MAX_JOBS));
     WR_CUDA(ctx, E->work.reserve(sizeof(unsigned long long)));
@@ -605,7 +693,7 @@ int wf_engine_get(wr_ctx* ctx, const WfConfig& cfg, WfEngine** out) {
     E->order_host.assign(1, 0);
     // persistent grids from the occupancy calculator
     int per_sm = 0;
-    WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_shade, cfg.shade_block, 0));
+    WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_shade<false>, cfg.shade_block, 0));
     if (cfg.ctas_per_sm > 0) per_sm = std::min(per_sm, cfg.ctas_per_sm);
     E->grid_shade = ctx->num_sms * std::max(1, per_sm);
     WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_generate, cfg.shade_block, 0));
@@ -655,6 +743,7 @@ int wf_update_jobs(wr_ctx* ctx, WfEngine* E, const std::vector<WfSlotUpdate>& up
     for (const WfSlotUpdate& u : updates) {
         if (u.slot < 0 || u.slot >= (int)WF_MAX_JOBS) return set_error(ctx, WR_ERR_INTERNAL, "bad job slot");
         WfJob j = u.jh.job;
+        j.tile = (uint32_t)std::max(0, E->cfg.pixel_tile);
         if (u.jh.rd) {
             int rc = scene_slot(ctx, E, u.jh.rd, &j.scene);
             if (rc != WR_OK) return rc;
@@ -705,6 +794,18 @@ int wf_update_jobs(wr_ctx* ctx, WfEngine* E, const std::vector<WfSlotUpdate>& up
             E->grid_shadow = ctx->num_sms * std::max(1, per_sm);
         }
     }
+    // the shade stage compiled with the light-connection code only while a job needs it
+    bool mis_any = false;
+    for (int slot : order)
+        if (E->job_tab[slot].active && (E->job_tab[slot].flags & WR_RENDER_NEE_MIS)) mis_any = true;
+    if (mis_any != E->mis_any) {
+        E->mis_any = mis_any;
+        if (E->graph) {
+            WR_CUDA(ctx, cudaStreamSynchronize(s));
+            cudaGraphExecDestroy(E->graph);
+            E->graph = nullptr;
+        }
+    }
     E->order_host.assign(1, (int)order.size());
     E->order_host.insert(E->order_host.end(), order.begin(), order.end());
     WR_CUDA(ctx, cudaMemcpyAsync(E->order.p, E->order_host.data(), sizeof(int) * E->order_host.size(),
@@ -728,14 +829,15 @@ static void enqueue_iteration(WfEngine* E, int x, cudaStream_t s, cudaEvent_t* e
         E->err_word.as<unsigned int>(), stats);
     if (ev) cudaEventRecord(ev[1], s);
     k_wf_sort<<<E->grid_sort, 256, 0, s>>>(scenes, jobs, E->side[x], E->hits.as<int2>(), E->sort, E->cfg.capacity);
-    k_wf_shade<<<E->grid_shade, E->cfg.shade_block, 0, s>>>(scenes, jobs, cnt, E->side[x], E->hits.as<int2>(),
+    (E->mis_any ? k_wf_shade<true> : k_wf_shade<false>)<<<E->grid_shade, E->cfg.shade_block, 0, s>>>(scenes, jobs, cnt, E->side[x], E->hits.as<int2>(),
                                                             E->side[y], E->shadow, E->sort, E->cfg.capacity);
     if (ev) cudaEventRecord(ev[2], s);
     k_wf_shadow<<<E->grid_shadow, E->cfg.extend_block, E->smem_shadow, s>>>(scenes, jobs, E->shadow, E->side[y],
                                                                            E->stack_cap, E->err_word.as<unsigned int>());
     if (ev) cudaEventRecord(ev[3], s);
-    k_wf_generate<<<E->grid_gen, E->cfg.shade_block, 0, s>>>(jobs, E->order.as<int>(), cnt, E->side[y],
-                                                             E->cfg.capacity);
+    k_wf_plan<<<1, WF_MAX_JOBS, 0, s>>>(jobs, E->order.as<int>(), cnt, E->side[y], E->cfg.capacity, E->equal_share,
+                                        E->plan);
+    k_wf_generate<<<E->grid_gen, E->cfg.shade_block, 0, s>>>(jobs, E->plan, E->side[y]);
     if (ev) cudaEventRecord(ev[4], s);
 }
 
@@ -770,7 +872,7 @@ int profile_wavefront(wr_ctx* ctx, RenderData& rd, const RenderParams& P, uint32
     uint32_t queued = 0;  // rays waiting in side x
     for (uint64_t it = 0;; it++) {
         enqueue_iteration(E, x, s, ev, st.as<unsigned long long>());
-        ctx->kernel_launches += 6;
+        ctx->kernel_launches += 7;
         x = 1 - x;
         WR_CUDA(ctx, cudaEventSynchronize(ev[4]));
         float a = 0, b = 0, cc = 0, d = 0;
@@ -856,7 +958,7 @@ int wf_launch(wr_ctx* ctx, WfEngine* E, cudaStream_t s) {
         E->graph_stack = E->stack_cap;
     }
     WR_CUDA(ctx, cudaGraphLaunch(E->graph, s));
-    ctx->kernel_launches += 6ull * 2 * E->cfg.iters_per_graph;  // reset, extend, sort, shade, shadow, generate
+    ctx->kernel_launches += 7ull * 2 * E->cfg.iters_per_graph;  // reset, extend, sort, shade, shadow, plan, generate
     return WR_OK;
 }
 
@@ -891,6 +993,18 @@ int wf_drain(wr_ctx* ctx, WfEngine* E, int side, uint32_t n, cudaStream_t s) {
 int wf_error_word(wr_ctx* ctx, WfEngine* E, unsigned int* herr, cudaStream_t s) {
     WR_CUDA(ctx, cudaMemcpyAsync(herr, E->err_word.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, s));
     WR_CUDA(ctx, cudaStreamSynchronize(s));
+    return WR_OK;
+}
+
+int wf_set_equal_share(wr_ctx* ctx, WfEngine* E, bool on) {
+    (void)ctx;
+    if (E->equal_share != (int)on) {
+        E->equal_share = on;
+        if (E->graph) {  // the policy is a kernel argument of the captured loop
+            cudaGraphExecDestroy(E->graph);
+            E->graph = nullptr;
+        }
+    }
     return WR_OK;
 }
 

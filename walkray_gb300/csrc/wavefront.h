@@ -39,6 +39,7 @@ struct WfJob {
     uint64_t seed;
     uint32_t s0, spp, max_path_len, flags;
     uint32_t npix;
+    uint32_t tile;             // camera paths in pixel tiles of this side (0: by rows)
     unsigned long long total;  // npix * spp paths
     float* film;
     float* film2;
@@ -49,17 +50,24 @@ struct WfJobCounters {
     unsigned long long finished;  // paths whose colour reached the film
 };
 
-// structure-of-arrays path state, one ping-pong side
+// path state, one ping-pong side: one 128-byte record (a cache line) per
+// path, so that the shade stage, which reads the queue in material-bucket
+// order, fetches each path's state as whole lines; the extend stage reads
+// its first 48 bytes (origin, direction, ids)
+enum : int {
+    WF_O = 0,     // o.xyz, oP
+    WF_D = 1,     // d.xyz, dP
+    WF_IDS = 2,   // inside, contact, job, pixel (int bits)
+    WF_MISC = 3,  // sample, rng dim, depth | stack_n << 16, cnorm.z bits
+    WF_RAD = 4,   // rad.xyz, cnorm.x
+    WF_COL = 5,   // color.xyz, cnorm.y
+    WF_STK = 6,   // inside stack (int bits)
+    WF_PREV = 7,  // direction of the ray before the current one (next-event estimation), MIS density
+    WF_REC = 8    // float4 per record
+};
 struct WfSide {
-    float4* a0;  // o.xyz, oP
-    float4* a1;  // d.xyz, dP
-    float4* a2;  // rad.xyz, cnorm.x
-    float4* a3;  // color.xyz, cnorm.y
-    int4* ids;   // inside, contact, job, pixel
-    int4* misc;  // sample, rng dim, depth | stack_n << 16, cnorm.z bits
-    int4* stk;   // inside stack
-    float4* a4;  // direction of the ray before the current one (next-event estimation), MIS density
-    float4* a5;  // light connections counted so far (WR_RENDER_NEE_MIS jobs only)
+    float4* rec;  // WF_REC float4 per path
+    float4* a5;   // light connections counted so far (WR_RENDER_NEE_MIS jobs only)
     unsigned int* counts;  // [0] survivors written by shade, [1] paths appended by generate
 };
 
@@ -95,10 +103,21 @@ struct WfConfig {
     int iters_per_graph = 4;       // ping-pong pairs per graph launch
     TraceTune trace = default_trace_tune();  // warp traversal loop of the extend stage
     int drain_paths = 0;           // per-path finish of a render's last paths at most this many (0 = never)
+    int pixel_tile = 0;            // generate camera paths tile by tile, tiles of this side (0: by rows)
 
     uint32_t drain_threshold() const {
         return drain_paths > 0 ? (uint32_t)drain_paths : 0u;
     }
+};
+
+// the share-out of free queue slots among jobs for one generate stage
+// (k_wf_plan): entry k is job slot slot[k] with path indices
+// [first[k], first[k] + off[k+1] - off[k]) at queue positions off[k]..
+struct WfPlan {
+    int* slot;
+    unsigned long long* first;
+    uint32_t* off;  // n + 1 offsets
+    int* n;
 };
 
 struct WfEngine;
@@ -134,6 +153,9 @@ int wf_read_counters(wr_ctx* ctx, WfEngine* E, std::vector<WfJobCounters>& out, 
 int wf_drain(wr_ctx* ctx, WfEngine* E, int side, uint32_t n, cudaStream_t s);
 int wf_error_word(wr_ctx* ctx, WfEngine* E, unsigned int* herr, cudaStream_t s);
 int wf_reset_queues(wr_ctx* ctx, WfEngine* E, cudaStream_t s);
+// free queue slots shared equally among the jobs with paths left (default)
+// or handed out in admission order
+int wf_set_equal_share(wr_ctx* ctx, WfEngine* E, bool on);
 const WfConfig& wf_config(const WfEngine* E);
 int wf_set_config(wr_ctx* ctx, const WfConfig& cfg);
 WfConfig wf_tuned_config(wr_ctx* ctx);

@@ -84,7 +84,9 @@ struct wr_ctx {
     uint32_t wf_capacity = 0;
     int wf_extend_block = 0, wf_shade_block = 0, wf_ctas_per_sm = 0, wf_iters = 0;
     int trace_refill_min = 0, trace_leaf_min = 0;  // warp traversal loop (0 = defaults)
+    int trace_steps = 0;                            // traversal steps per turn of the warp loop (0 = default)
     int wf_drain_paths = 0;                          // drain threshold of wr_render (0 = never)
+    int wf_pixel_tile = 0;                           // camera paths generated tile by tile (0 = by rows)
 };
 
 namespace wr {
@@ -99,6 +101,7 @@ inline TraceTune trace_tune_of(const wr_ctx* ctx) {
     TraceTune t = default_trace_tune();
     if (ctx->trace_refill_min) t.refill_min = ctx->trace_refill_min;
     if (ctx->trace_leaf_min) t.leaf_min = ctx->trace_leaf_min;
+    if (ctx->trace_steps) t.steps = ctx->trace_steps;
     return t;
 }
 }  // namespace wr

@@ -57,8 +57,9 @@ struct DevTree {
 struct TraceTune {
     int refill_min;  // refill idle lanes once at least this many are idle (or none is busy)
     int leaf_min;    // lanes holding postponed leaves that start the warp's leaf phase
+    int steps;       // traversal steps a searching lane takes per turn of the warp loop (1..8)
 };
-inline TraceTune default_trace_tune() { return TraceTune{8, 8}; }  // fastest of a sweep on GB300
+inline TraceTune default_trace_tune() { return TraceTune{8, 8, 1}; }  // fastest of a sweep on GB300
 
 struct f3 {
     float x, y, z;
@@ -93,6 +94,43 @@ __host__ __device__ __forceinline__ f3 normalize(f3 a) {
     return a;
 }
 __host__ __device__ __forceinline__ f3 xyz(float4 v) { return mk(v.x, v.y, v.z); }
+
+// The same operations with every product and sum rounded on its own, for the
+// traversal code whose results must equal the reference's FP32 bit for bit
+// (box face test, triangle test, face normals, NoSelfCondition): these are
+// never contracted into fused multiply-adds, whatever the compiler's -fmad
+// setting, so the rest of the device code may be compiled with contraction.
+#ifdef __CUDA_ARCH__
+__device__ __forceinline__ float add_x(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float sub_x(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float mul_x(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float div_x(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float sqrt_x(float a) { return __fsqrt_rn(a); }
+#else
+inline float add_x(float a, float b) { return a + b; }
+inline float sub_x(float a, float b) { return a - b; }
+inline float mul_x(float a, float b) { return a * b; }
+inline float div_x(float a, float b) { return a / b; }
+inline float sqrt_x(float a) { return sqrtf(a); }
+#endif
+__host__ __device__ __forceinline__ f3 sub3_x(f3 a, f3 b) { return mk(sub_x(a.x, b.x), sub_x(a.y, b.y), sub_x(a.z, b.z)); }
+// nvVector.h:501-506 order, unfused
+__host__ __device__ __forceinline__ float dot_x(f3 a, f3 b) {
+    float r = 0.f;
+    r = add_x(r, mul_x(a.x, b.x));
+    r = add_x(r, mul_x(a.y, b.y));
+    r = add_x(r, mul_x(a.z, b.z));
+    return r;
+}
+__host__ __device__ __forceinline__ f3 cross_x(f3 l, f3 r) {
+    return mk(sub_x(mul_x(l.y, r.z), mul_x(l.z, r.y)), sub_x(mul_x(l.z, r.x), mul_x(l.x, r.z)),
+              sub_x(mul_x(l.x, r.y), mul_x(l.y, r.x)));
+}
+__host__ __device__ __forceinline__ f3 normalize_x(f3 a) {
+    const float r = sqrt_x(dot_x(a, a));
+    if (r > 0.f) a = mk(div_x(a.x, r), div_x(a.y, r), div_x(a.z, r));
+    return a;
+}
 
 // ---------------------------------------------------------------------------
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).  Draw `dim` of

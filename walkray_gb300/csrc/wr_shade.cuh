@@ -1281,10 +1281,14 @@ __device__ __forceinline__ bool mis_light_request(const RenderScene& S, int self
 // scattered ray that misses is the caller's case: the same connection from it.
 //
 // With WR_RENDER_NEE_MIS, a vertex on a diffuse / Phong surface outside media
-// also asks for a light connection (`has_lr`, `lr`: the caller traces it and
-// adds lr.contrib when light_req_visible), and an emitter reached straight
-// from such a vertex is weighted against the light strategy; `mis_pdf`
-// carries the scatter's density of the current ray (0: nothing to weigh).
+// whose scattered ray may still be traced (depth + 1 <= max_path_len) also
+// asks for a light connection (`has_lr`, `lr`: the caller traces it and adds
+// lr.contrib when light_req_visible), and an emitter reached straight from
+// such a vertex is weighted against the light strategy; `mis_pdf` carries
+// the scatter's density of the current ray (0: nothing to weigh).
+// MIS_CODE: compiled with the WR_RENDER_NEE_MIS code (kernels that never see
+// the flag leave it out, which keeps their register count down).
+template <bool MIS_CODE>
 __device__ __forceinline__ bool path_advance(const RenderScene& S, PRay& cur, f3& color, f3& prev_d,
                                              uint32_t& depth, InsideStack& st, PathRng& g, uint32_t max_path_len,
                                              uint32_t flags, f3& result, bool& nee_here, float& mis_pdf,
@@ -1292,7 +1296,7 @@ __device__ __forceinline__ bool path_advance(const RenderScene& S, PRay& cur, f3
     nee_here = false;
     has_lr = false;
     const bool nee = (flags & WR_RENDER_NEE) != 0;
-    const bool mis = (flags & WR_RENDER_NEE_MIS) != 0;
+    const bool mis = MIS_CODE && (flags & WR_RENDER_NEE_MIS) != 0;
     const bool mirror = (flags & WR_RENDER_PHONG_MIRROR) != 0;
     const int self = cur.inside >= 0 ? cur.inside : cur.iobj;
     if (self < 0) {  // escaped eye ray: terminateRay carries zero radiance, endIndex 0 connects nothing
@@ -1300,7 +1304,9 @@ __device__ __forceinline__ bool path_advance(const RenderScene& S, PRay& cur, f3
         return true;
     }
     const uint32_t stype = obj_type(S, self);
-    const bool mis_vertex = mis && cur.inside < 0 && mis_material(stype);
+    // a light connection from this vertex is a path one segment longer, which
+    // the reference only has while its scattered ray may still be traced
+    const bool mis_vertex = mis && cur.inside < 0 && mis_material(stype) && depth + 1 <= max_path_len;
     if (mis_vertex) {
         const f3 T = vmul(color * cos_term(S, cur), weight(cur));
         has_lr = mis_light_request(S, self, cur, T, g, mirror, lr);

@@ -104,9 +104,9 @@ __device__ __forceinline__ bool face_pass(const Box& bx, const RayQ& q) {
     const float dA = c_<A>(q.d);
     if (dA == 0.f) return false;
     const float plane = I < 3 ? lo_<A>(bx) : hi_<A>(bx);
-    const float dist = (plane - c_<A>(q.o)) / dA;
-    const float pb = c_<B>(q.o) + dist * c_<B>(q.d);
-    const float pc = c_<C>(q.o) + dist * c_<C>(q.d);
+    const float dist = div_x(sub_x(plane, c_<A>(q.o)), dA);
+    const float pb = add_x(c_<B>(q.o), mul_x(dist, c_<B>(q.d)));
+    const float pc = add_x(c_<C>(q.o), mul_x(dist, c_<C>(q.d)));
     return dist >= 0.f && lo_<B>(bx) <= pb && hi_<B>(bx) >= pb && lo_<C>(bx) <= pc && hi_<C>(bx) >= pc;
 }
 
@@ -131,9 +131,9 @@ __device__ __forceinline__ bool face_pass_sel(int a, bool hi, const Box& bx, con
     const float loC = pick3(c, bx.lx, bx.ly, bx.lz), hiC = pick3(c, bx.hx, bx.hy, bx.hz);
     // a zero direction component skips the face (kdtree.cpp:51); the division
     // is still evaluated so that every lane runs the same instructions
-    const float dist = (plane - oA) / dA;
-    const float pb = oB + dist * dB;
-    const float pc = oC + dist * dC;
+    const float dist = div_x(sub_x(plane, oA), dA);
+    const float pb = add_x(oB, mul_x(dist, dB));
+    const float pc = add_x(oC, mul_x(dist, dC));
     return (dA != 0.f) & (dist >= 0.f) & (loB <= pb) & (hiB >= pb) & (loC <= pc) & (hiC >= pc);
 }
 
@@ -208,20 +208,20 @@ __device__ __forceinline__ void pair_pred(const Box& L, const Box& R, const RayQ
 // the distance or -1.  The edge-mask rejection is taken before the plane
 // distance (same result, less work).
 __device__ __forceinline__ float tri_test(f3 v0, f3 v1, f3 v2, const RayQ& q, float* dd_out = nullptr) {
-    const f3 l0 = v1 - v0, l1 = v2 - v1, l2 = v0 - v2;
-    const f3 r0 = v0 - q.o, r1 = v1 - q.o, r2 = v2 - q.o;
-    const float s0 = dot(q.d, cross(l0, r0));
-    const float s1 = dot(q.d, cross(l1, r1));
-    const float s2 = dot(q.d, cross(l2, r2));
+    const f3 l0 = sub3_x(v1, v0), l1 = sub3_x(v2, v1), l2 = sub3_x(v0, v2);
+    const f3 r0 = sub3_x(v0, q.o), r1 = sub3_x(v1, q.o), r2 = sub3_x(v2, q.o);
+    const float s0 = dot_x(q.d, cross_x(l0, r0));
+    const float s1 = dot_x(q.d, cross_x(l1, r1));
+    const float s2 = dot_x(q.d, cross_x(l2, r2));
     const bool pos = s0 >= 0.f && s1 >= 0.f && s2 >= 0.f;
     const bool neg = s0 <= 0.f && s1 <= 0.f && s2 <= 0.f;
     if (!pos && !neg) return -1.f;
-    const f3 n = normalize(cross(l0, l1));
-    const float od = dot(n, r2);
-    const float dd = dot(n, q.d);
+    const f3 n = normalize_x(cross_x(l0, l1));
+    const float od = dot_x(n, r2);
+    const float dd = dot_x(n, q.d);
     if (dd_out) *dd_out = dd;
     if (dd == 0.f) return -1.f;
-    const float t = od / dd;
+    const float t = div_x(od, dd);
     if (t < 0.f) return -1.f;
     return t;
 }
@@ -232,11 +232,13 @@ __device__ __forceinline__ void graze_check(RayQ& q, float dd) {
 }
 
 // Mesh::getWorldNormal without vertex normals (mesh.h:47-56)
-__device__ __forceinline__ f3 face_normal(f3 v0, f3 v1, f3 v2) { return normalize(cross(v1 - v0, v2 - v0)); }
+__device__ __forceinline__ f3 face_normal(f3 v0, f3 v1, f3 v2) {
+    return normalize_x(cross_x(sub3_x(v1, v0), sub3_x(v2, v0)));
+}
 
 // NoSelfCondition::legal (noself.cpp:13-20); object ids, -1 = none
 __device__ __forceinline__ bool noself_legal(int inside, int contact, int hit_obj, f3 dir, f3 fn) {
-    const float d = dot(dir, fn);
+    const float d = dot_x(dir, fn);
     const bool in = d <= 0.f, out = d >= 0.f;
     if (inside == contact) return !(in && contact == hit_obj);
     return !(out && inside != hit_obj);

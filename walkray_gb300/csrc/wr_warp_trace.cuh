@@ -116,8 +116,8 @@ __device__ __forceinline__ void lane_leaves(TraceLane& L) {
 // starts at 0).  Every lane of the warp must call it.  Each turn the warp
 // does one thing for the lanes it concerns: tests the postponed leaves (once
 // `leaf_min` lanes hold some, or no lane is left searching) or takes one
-// traversal step; lanes that finish store their hit, and idle lanes refill
-// once `refill_min` of them are idle.
+// traversal step (or up to `steps` of them); lanes that finish store their
+// hit, and idle lanes refill once `refill_min` of them are idle.
 template <bool PRUNE, bool STATS, class Src>
 __device__ __forceinline__ void warp_trace(Src& src, uint64_t n, unsigned long long* counter, TraceTune tune,
                                            uint32_t* stack, int stride, int cap, unsigned int* err) {
@@ -158,7 +158,12 @@ __device__ __forceinline__ void warp_trace(Src& src, uint64_t n, unsigned long l
         if (pm && (sm == 0 || __popc(pm) >= tune.leaf_min)) {
             if (pending) lane_leaves<PRUNE, STATS>(L);
         } else if (searching) {
+            // up to tune.steps steps before the warp looks at its lanes again:
+            // fewer ballots per step, at the price of lanes that reach leaves
+            // early waiting for the others
             lane_step<PRUNE, STATS>(L, stack, stride, cap, err);
+            for (int k = 1; k < tune.steps && L.npend == 0 && L.sp > 0; ++k)
+                lane_step<PRUNE, STATS>(L, stack, stride, cap, err);
         }
         if (active && L.sp == 0 && L.npend == 0) {
             src.store(id, L);
