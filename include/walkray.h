@@ -263,6 +263,20 @@ typedef struct wr_render_desc {
  * the W*H*3 mean image (p = y*W + x, row 0 at the top), host buffer. */
 int wr_render(wr_ctx* ctx, wr_scene_id scene, const wr_render_desc* desc, float* rgb_out);
 
+/* PathTracer::renderPixels (pathTracer.cpp:15-73) refines its image one
+ * sample per pixel at a time and shows / saves the running mean after each
+ * (Film::setBuffer, savePFM); without an <iter> in the configuration its
+ * spp is INT_MAX (config.cpp:534) and it runs until stopped.  This entry
+ * point renders the same way in chunks of at most chunk_spp samples per
+ * pixel (0 = about 16M paths per chunk): after each chunk rgb_out (host,
+ * W*H*3) holds the mean of the samples so far and progress(user, rgb_out,
+ * spp_done) is called (progress may be NULL); a nonzero return stops the
+ * render there.  *spp_done (may be NULL) gets the samples rendered.  The
+ * samples are those of one wr_render of desc->spp samples. */
+typedef int (*wr_progress_fn)(void* user, const float* rgb, uint32_t spp_done);
+int wr_render_progressive(wr_ctx* ctx, wr_scene_id scene, const wr_render_desc* desc, uint32_t chunk_spp,
+                          float* rgb_out, wr_progress_fn progress, void* user, uint32_t* spp_done);
+
 /* Adds the desc->spp samples starting at desc->spp_offset to a device film:
  * d_sum[3p+c] += colour, d_sumsq (may be NULL) += colour^2.  Enqueued on
  * `stream` (cudaStream_t; NULL = the context's stream), asynchronous. */

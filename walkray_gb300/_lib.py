@@ -174,7 +174,12 @@ _SIGS = {
     "wr_rng_draws": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p,
                                C.c_void_p]),
     "wr_render_noalloc_status": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint)]),
+    "wr_render_progressive": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(wr_render_desc), C.c_uint32, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.POINTER(C.c_uint32)]),
 }
+
+# int (*)(void* user, const float* rgb, uint32_t spp_done)
+PROGRESS_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_float), C.c_uint32)
 
 _lib = None
 

@@ -139,6 +139,24 @@ class Context:
         self._check(self.lib.wr_render(self.h, sid, C.byref(d), L.ptr(out)))
         return out
 
+    def render_progressive(self, sid: int, spp: int, max_path_len: int, seed: int = 1, mode: str = "wavefront",
+                           chunk_spp: int = 0, progress=None, nee: bool = False, flags: int = 0):
+        """wr_render_progressive: the running mean after every chunk of
+        samples; `progress(image, spp_done)` may return True to stop.
+        Returns (image, spp_done)."""
+        w, h = self._camera_size(sid)
+        out = np.empty((h, w, 3), np.float32)
+
+        def cb(user, rgb, done):
+            return 1 if (progress is not None and progress(out, int(done))) else 0
+
+        fn = L.PROGRESS_FN(cb)
+        d = L.wr_render_desc(spp, max_path_len, seed, MODES[mode], _flags(nee, False) | flags, 0, 0)
+        done = C.c_uint32()
+        self._check(self.lib.wr_render_progressive(self.h, sid, C.byref(d), chunk_spp, L.ptr(out), fn, None,
+                                                   C.byref(done)))
+        return out, done.value
+
     def render_device(self, sid: int, spp: int, max_path_len: int, d_sum: int, d_sumsq: int = 0, seed: int = 1,
                       mode: str = "megakernel", nee: bool = False, spp_offset: int = 0, stream: int = 0,
                       exact: bool = False, radius: float = 0.0, flags: int = 0) -> None:

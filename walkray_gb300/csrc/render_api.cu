@@ -316,6 +316,58 @@ int wr_render(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, float* rg
     }
 }
 
+// out = sum * s (grid-stride)
+__global__ void k_scale_to(const float* __restrict__ a, float* __restrict__ out, size_t n, float s) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = a[i] * s;
+}
+
+int wr_render_progressive(wr_ctx* ctx, wr_scene_id id, const wr_render_desc* desc, uint32_t chunk_spp,
+                          float* rgb_out, wr_progress_fn progress, void* user, uint32_t* spp_done) {
+    if (!ctx || !desc || !rgb_out) return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "null argument");
+    if (spp_done) *spp_done = 0;
+    SceneGPU* sc = find_scene(ctx, id);
+    if (!sc) return set_error(ctx, WR_ERR_NOT_FOUND, "no such scene");
+    try {
+        WR_CUDA(ctx, cudaSetDevice(ctx->device));
+        const size_t npix = (size_t)sc->camera.width * sc->camera.height, n = 3 * npix;
+        if (chunk_spp == 0) chunk_spp = (uint32_t)std::max<size_t>(1, (16ull << 20) / std::max<size_t>(1, npix));
+        // the running sum stays on the device between chunks; the mean of the
+        // samples so far is taken into a second buffer and copied out
+        DeviceBuffer& film = ctx->film;
+        WR_CUDA(ctx, film.reserve(sizeof(float) * std::max<size_t>(2 * n, 1)));
+        float* sum = film.as<float>();
+        float* mean = sum + n;
+        cudaStream_t s = ctx->stream;
+        unsigned int* err = reinterpret_cast<unsigned int*>(ctx->scratch_words.as<unsigned long long>() + 1);
+        WR_CUDA(ctx, cudaMemsetAsync(err, 0, sizeof(unsigned int), s));
+        WR_CUDA(ctx, cudaMemsetAsync(sum, 0, sizeof(float) * n, s));
+        uint32_t done = 0;
+        while (done < desc->spp) {
+            wr_render_desc d = *desc;
+            d.spp_offset = desc->spp_offset + done;
+            d.spp = std::min<uint32_t>(chunk_spp, desc->spp - done);
+            int rc = wr_render_device(ctx, id, &d, sum, nullptr, s);
+            if (rc != WR_OK) return rc;
+            done += d.spp;
+            k_scale_to<<<(unsigned)std::min<size_t>((n + 255) / 256, 65535), 256, 0, s>>>(sum, mean, n,
+                                                                                       1.0f / (float)done);
+            WR_CUDA(ctx, cudaGetLastError());
+            ctx->kernel_launches++;
+            WR_CUDA(ctx, cudaMemcpyAsync(rgb_out, mean, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+            unsigned int herr = 0;
+            WR_CUDA(ctx, cudaMemcpyAsync(&herr, err, sizeof herr, cudaMemcpyDeviceToHost, s));
+            WR_CUDA(ctx, cudaStreamSynchronize(s));
+            if (herr) return set_error(ctx, WR_ERR_INTERNAL, "traversal stack overflow");
+            if (spp_done) *spp_done = done;
+            if (progress && progress(user, rgb_out, done) != 0) break;
+        }
+        return WR_OK;
+    } catch (const std::exception& ex) {
+        return set_error(ctx, WR_ERR_INTERNAL, ex.what());
+    }
+}
+
 }  // extern "C"
 
 namespace wr {

@@ -136,8 +136,33 @@ GpuPathTracer::~GpuPathTracer() {
     if (ctx) wr_ctx_destroy(ctx);
 }
 
+bool GpuPathTracer::uploadSceneFile() {
+    wr_scene_file* f = nullptr;
+    char err[512] = {0};
+    if (wr_scene_file_load(sceneFile.c_str(), &f, err, sizeof err) != WR_OK) {
+        std::cerr << "GpuPathTracer: " << err << std::endl;
+        return false;
+    }
+    wr_scene_desc desc;
+    wr_scene_file_settings settings;
+    bool ok = wr_scene_file_get(f, &desc, &settings) == WR_OK;
+    if (ok && desc.num_objects != engine->scene.objects.size()) {
+        std::cerr << "GpuPathTracer: the scene file has " << desc.num_objects << " objects, the scene "
+                  << engine->scene.objects.size() << std::endl;
+        ok = false;
+    }
+    if (ok && wr_scene_upload(ctx, &desc, &sceneId) != WR_OK) {
+        std::cerr << "GpuPathTracer: " << wr_last_error(ctx) << std::endl;
+        ok = false;
+    }
+    wr_scene_file_free(f);
+    uploaded = ok;
+    return ok;
+}
+
 bool GpuPathTracer::uploadScene() {
     if (uploaded) return true;
+    if (!sceneFile.empty()) return uploadSceneFile();
     Scene& sc = engine->scene;
     std::vector<wr_object_desc> objs(sc.objects.size());
     std::vector<float> verts;
@@ -190,6 +215,8 @@ bool GpuPathTracer::uploadScene() {
     desc.camera.width = (uint32_t)c.mResolution.x;
     desc.camera.height = (uint32_t)c.mResolution.y;
     desc.camera.image_plane_dist = c.mImagePlaneDist;
+    desc.camera.lens_radius = lens[0];
+    desc.camera.focal_dist = lens[1];
     if (wr_scene_upload(ctx, &desc, &sceneId) != WR_OK) {
         std::cerr << "GpuPathTracer: " << wr_last_error(ctx) << std::endl;
         return false;
@@ -198,9 +225,29 @@ bool GpuPathTracer::uploadScene() {
     return true;
 }
 
+namespace {
+
+struct ProgressCtx {
+    GpuPathTracer::Progress* hook;
+    Camera* camera;
+    std::string pfm;
+    std::vector<vec3f>* img;
+};
+
+// after every chunk: the film and its PFM as the reference updates them
+// after every iteration (pathTracer.cpp:67-70), then the caller's hook
+int on_chunk(void* user, const float*, uint32_t done) {
+    ProgressCtx* p = static_cast<ProgressCtx*>(user);
+    p->camera->mFilm.setBuffer(*p->img);
+    p->camera->mFilm.savePFM(p->pfm);
+    return (*p->hook && (*p->hook)(*p->img, done)) ? 1 : 0;
+}
+
+}  // namespace
+
 std::vector<vec3f> GpuPathTracer::renderPixels() {
     if (!ctx || !uploadScene()) return std::vector<vec3f>();
-    const Camera& c = engine->scene.mCamera;
+    Camera& c = engine->scene.mCamera;
     const size_t n = (size_t)c.mResolution.x * (size_t)c.mResolution.y;
     std::vector<vec3f> img(n);
     wr_render_desc d;
@@ -210,9 +257,11 @@ std::vector<vec3f> GpuPathTracer::renderPixels() {
     d.seed = seed;
     d.mode = mode;
     d.radius = mergeRadius;
-    d.flags = useNextEventEstimation ? WR_RENDER_NEE : 0u;
+    d.flags = (useNextEventEstimation ? WR_RENDER_NEE : 0u) | extraFlags;
     static_assert(sizeof(vec3f) == 3 * sizeof(float), "vec3f must be three packed floats");
-    if (wr_render(ctx, sceneId, &d, &img[0].x) != WR_OK) {
+    ProgressCtx pc{&progress, &c, name + engine->scene.name + ".pfm", &img};
+    uint32_t done = 0;
+    if (wr_render_progressive(ctx, sceneId, &d, 0, &img[0].x, on_chunk, &pc, &done) != WR_OK) {
         std::cerr << "GpuPathTracer: " << wr_last_error(ctx) << std::endl;
         return std::vector<vec3f>();
     }
