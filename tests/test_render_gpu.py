@@ -333,3 +333,56 @@ def test_scene_file_renders_through_both_renderers(ctx):
     o = wr_oracle.SceneOracle(s).render(64, n, seed=70, flags=wr_oracle.DELTA)[0].reshape(h_, w_, 3) / 64
     assert m.mean() > 0 and abs(m.mean() / o.mean() - 1) < 5e-3, (m.mean(), o.mean())
     ctx.release(sid)
+
+
+def test_autotuner_pick_renders_the_same_image(ctx):
+    """wr_autotune's coordinate descent starts from the shipped defaults
+    (2^24 paths in flight, 6 traversal CTAs per SM, refill / leaf 8, one step
+    per turn, rows) and keeps a value only if it is faster; its pick --
+    whatever it is -- renders the image the defaults render (only the order
+    of the FP32 film additions differs), and the camera-path pixel tile, an
+    order of work only, leaves the image alone."""
+    s = make_golden.golden_scenes()["mixed_l2"]
+    sid = ctx.upload(s)
+    want = ctx.render(sid, 8, 16, seed=12, mode="wavefront")
+    try:
+        best = ctx.autotune(sid, 4, 16)
+        assert best["capacity"] in (1 << 22, 1 << 23, 1 << 24)
+        assert best["ctas_per_sm"] in (6, 8) and best["pixel_tile"] in (0, 8, 16, 32)
+        assert best["steps_per_turn"] in (1, 2, 4)
+        assert best["mpaths_per_s"] > 0
+        got = ctx.render(sid, 8, 16, seed=12, mode="wavefront")
+        assert np.allclose(got, want, rtol=1e-4, atol=1e-5), np.abs(got - want).max()
+        for tile in (8, 13, 32):
+            ctx.set_wavefront_config(capacity=1 << 16, pixel_tile=tile)
+            got = ctx.render(sid, 8, 16, seed=12, mode="wavefront")
+            assert np.allclose(got, want, rtol=1e-4, atol=1e-5), (tile, np.abs(got - want).max())
+    finally:
+        ctx.set_wavefront_config(capacity=1 << 24)
+    ctx.release(sid)
+
+
+def test_progressive_render_refines_like_the_reference(ctx):
+    """wr_render_progressive: the running mean after every chunk (the
+    reference's per-iteration film update, pathTracer.cpp:15-73), a stop from
+    the progress callback, and in the end the image of one wr_render of the
+    same samples."""
+    s = make_golden.golden_scenes()["cornell"]
+    sid = ctx.upload(s)
+    seen = []
+
+    def progress(img, done):
+        seen.append((done, img.copy()))
+        return False
+
+    img, done = ctx.render_progressive(sid, 40, 8, seed=21, chunk_spp=16, progress=progress)
+    assert done == 40 and [d for d, _ in seen] == [16, 32, 40]
+    want = ctx.render(sid, 40, 8, seed=21, mode="wavefront")
+    assert np.allclose(img, want, rtol=1e-4, atol=1e-5), np.abs(img - want).max()
+    first = ctx.render(sid, 16, 8, seed=21, mode="wavefront")
+    assert np.allclose(seen[0][1], first, rtol=1e-4, atol=1e-5)
+    # a stop after the second chunk: the mean of 32 samples
+    img2, done2 = ctx.render_progressive(sid, 1 << 30, 8, seed=21, chunk_spp=16, progress=lambda im, d: d >= 32)
+    assert done2 == 32
+    assert np.allclose(img2, ctx.render(sid, 32, 8, seed=21, mode="wavefront"), rtol=1e-4, atol=1e-5)
+    ctx.release(sid)

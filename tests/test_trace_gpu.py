@@ -63,15 +63,16 @@ def test_filtered_trace_matches_reference_golden(ctx):
     ctx.release(sid)
 
 
-@pytest.mark.parametrize("refill_min,leaf_min", [(1, 1), (32, 32), (4, 3)])
-def test_traversal_loop_settings_do_not_change_hits(ctx, refill_min, leaf_min):
-    """The warp loop's refill threshold and leaf postponement change only the
-    order of work: filtered hits stay equal to the reference's."""
+@pytest.mark.parametrize("refill_min,leaf_min,steps", [(1, 1, 1), (32, 32, 1), (4, 3, 1), (8, 8, 2), (4, 8, 8)])
+def test_traversal_loop_settings_do_not_change_hits(ctx, refill_min, leaf_min, steps):
+    """The warp loop's refill threshold, leaf postponement and steps per turn
+    change only the order of work: filtered hits stay equal to the
+    reference's."""
     s = make_golden.golden_scenes()["mixed_l2"]
     g = np.load(os.path.join(GOLDEN, "trace_filtered.npz"))
     rays, ids = make_golden.filtered_rays(s, 32768, seed=5)
     sid = ctx.upload(s)
-    ctx.set_wavefront_config(capacity=1 << 24, refill_min=refill_min, leaf_min=leaf_min)
+    ctx.set_wavefront_config(capacity=1 << 24, refill_min=refill_min, leaf_min=leaf_min, steps_per_turn=steps)
     try:
         h = ctx.trace_closest(sid, rays, ids[:, 0], ids[:, 1])
     finally:

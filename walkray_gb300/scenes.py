@@ -569,6 +569,31 @@ def cornell_fog(width=256, height=256, ior=1.0) -> Scene:
     return s
 
 
+def phong_dome(width=16, height=16, power=100.0, albedo=0.8, elevation_deg=30.0, fov=4.0, aniso=None) -> Scene:
+    """One isotropic Phong plane (y = 0, 60 x 60, exponent `power`, grey
+    albedo) inside an emissive sphere of radius 50 and radiance 1 facing
+    inwards, seen by a narrow camera `elevation_deg` above the plane: every
+    pixel shows the plane, and a path of length 2 (plane, then sphere) gives
+    the Phong BRDF's directional albedo at the pixel's incidence angle --
+    a value fixed by the BRDF alone, against which any sampler of it can be
+    checked by numerical integration.  `aniso` = (rs, rd, nu, nv) makes the
+    plane anisotropic Phong instead (AnisotropicGlossyObject)."""
+    s = Scene("phong_dome")
+    g = 30.0
+    plane = quad((-g, 0, -g), (-g, 0, g), (g, 0, g), (g, 0, -g), (0, 1, 0))
+    if aniso is None:
+        s.add(MAT_GLOSSY, *plane, albedo=(albedo, albedo, albedo), power=float(power))
+    else:
+        rs, rd, nu, nv = aniso
+        s.add(MAT_ANISO, *plane, rs=(rs, rs, rs), rd=(rd, rd, rd), nu=float(nu), nv=float(nv))
+    V, F = icosphere(4)
+    s.add(MAT_EMISSIVE, (V * 50.0).astype(np.float32), F[:, ::-1].copy(), emission=(1.0, 1.0, 1.0))
+    e = math.radians(elevation_deg)
+    pos = (0.0, 3.0 * math.sin(e), -3.0 * math.cos(e))
+    s.camera = Camera.from_fov(pos, (0.0, 0.0, 0.0), (0, 1, 0), width, height, fov)
+    return s
+
+
 def save_rays(path: str, rays: np.ndarray) -> None:
     rays = np.ascontiguousarray(rays, np.float32)
     with open(path, "wb") as fh:
