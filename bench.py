@@ -1,18 +1,28 @@
 #!/usr/bin/env python3
 """Benchmark driver.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload pt|kd]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload pt|kd|serve|relmse|bpt]
 
 Prints ONE JSON line (rank 0).  Workloads:
 
-  pt  (default) path tracing of the mixed-material scene: 25 displaced
-      level-5 icospheres (512,006 triangles) on a ground plane, 40 % diffuse /
-      40 % isotropic Phong / 20 % refractive, two area lights, 1024x1024, max
-      path length 16.  One step = one sample per pixel (1,048,576 paths)
-      through the wavefront renderer.  Metric: Mpaths/s (the megakernel's
-      Mpaths/s and the time to relMSE 1e-3 of both are reported beside it).
+  pt  (default) path tracing of the mixed-material scene as configured: 25
+      displaced level-5 icospheres (512,006 triangles) on a ground plane,
+      40 % diffuse / 40 % isotropic Phong / 20 % refractive, two area lights,
+      1024x1024 at 256 samples per pixel, max path length 16.  One step = one
+      wr_render_device call of the whole configuration (268,435,456 paths)
+      through the wavefront renderer with the reference's estimator, in the
+      configuration wr_autotune picks first.  Metric: Mpaths/s.  Beside it:
+      the plain megakernel on the same call, the time to relMSE 1e-3 of both
+      renderers with the reference's estimator and with the low-variance one
+      (NEE with MIS + mirror-lobe Phong), the extend stage's roofline, and --
+      unless --no-extras -- the kd microbenchmark (key "kd") and a short
+      serving stream (key "serve").
   kd  closest-hit microbenchmark: level-8 displaced icosphere (1,310,720
       triangles), 2^24 rays; one step = all rays.  Metric: Mrays/s.
+  serve  a seeded Poisson stream of render requests through the serving
+      loop: p50 / p99 latency, slowdowns and Mpaths/s.
+  relmse relMSE of each path-tracing configuration at its own spp against a
+      converged image (configuration 0: the reference's 16,384-spp CPU image).
   bpt bidirectional path tracing (WR_MODE_BIDIRECTIONAL) of the Cornell box,
       256x256, max path length 8; one step = one render call of 16 samples
       per pixel (1,048,576 eye + light sub-path pairs, all connections).
@@ -58,7 +68,7 @@ RAY_IO_BYTES, BOX_BYTES, TRI_BYTES = 40, 32, 52
 KD_BYTES_PER_RAY = RAY_IO_BYTES + KD_BOX_TESTS * BOX_BYTES + KD_TRI_TESTS * TRI_BYTES
 
 PT_SIZE, PT_DEPTH, PT_SEED = 1024, 16, 7
-PT_SPP = 16  # samples per pixel per step (one render call)
+PT_SPP = 256  # samples per pixel per step: one render call of the whole configuration
 METRIC_PT = "Mpaths/s (wavefront path tracing, 1024^2 mixed-material scene; time-to-relMSE 1e-3 beside it)"
 
 
@@ -211,42 +221,61 @@ def cpu_baseline_pt(scene, rows: int, threads: int):
                       f"WalkRay's PathTracer restated in C (oracle), {threads} OpenMP threads, tree build excluded"}
 
 
+def time_to_relmse(ctx, sid, flags, ms_per_spp):
+    """Time to relMSE 1e-3 of one estimator: per-pixel variance from 64 spp
+    (sum and sum of squares) against R, an independent 256-spp image of the
+    low-variance estimator (the least noisy reference at hand; an unbiased
+    estimator's MSE is its variance, so relMSE(n spp) = rel_1spp / n)."""
+    from walkray_gb300.api import LOW_VARIANCE
+
+    ref = ctx.render(sid, 256, PT_DEPTH, seed=99, mode="wavefront", flags=LOW_VARIANCE).astype(np.float64)
+    s1, s2 = ctx.render_stats(sid, 64, PT_DEPTH, seed=11, mode="wavefront", flags=flags)
+    rel1, top_share = relmse_per_sample(s1, s2, 64, ref)
+    spp_needed = rel1 / 1e-3
+    out = {"spp_needed": round(spp_needed, 1), "relmse_1spp": round(rel1, 5),
+           "share_of_top_0.1pct_entries": round(top_share, 4)}
+    for k, v in ms_per_spp.items():
+        out[k + "_s"] = round(spp_needed * v / 1e3, 3)
+    return out
+
+
 def run_pt(args, world, rank, local):
     import torch
 
-    from walkray_gb300.api import Context
+    from walkray_gb300.api import LOW_VARIANCE, Context
 
     torch.cuda.set_device(local)
     scene = pt_scene()
     npix = PT_SIZE * PT_SIZE
     ctx = Context(device=local)
     sid = ctx.upload(scene)
-    tuned = ctx.autotune(sid, 1, PT_DEPTH) if args.tune else None
+    tuned = ctx.autotune(sid, 16, PT_DEPTH) if not args.no_tune else None
     stream = torch.cuda.Stream()
     film = torch.zeros(npix * 3, dtype=torch.float32, device="cuda")
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
     seed = 1000 + rank
+    mk_steps = max(1, min(args.steps, args.mk_steps))
 
-    def step_mode(mode):
+    def step_mode(mode, flags=0):
         return lambda i: ctx.render_device(sid, PT_SPP, PT_DEPTH, film.data_ptr(), seed=seed, mode=mode,
-                                           spp_offset=i * PT_SPP, stream=stream.cuda_stream)
+                                           spp_offset=i * PT_SPP, stream=stream.cuda_stream, flags=flags)
 
     with torch.cuda.stream(stream):
         for i in range(args.warmup):
             step_mode("wavefront")(i)
-            step_mode("megakernel")(i)
+        step_mode("megakernel")(0)
     torch.cuda.synchronize()
     barrier(world)
     with ClockSampler(local) as clk:
         l0 = launches(ctx)
         ms = timed_steps(step_mode("wavefront"), args.steps, stream, flush)
         n_launch = launches(ctx) - l0
-        ms_mk = timed_steps(step_mode("megakernel"), args.steps, stream, flush)
+        ms_mk = timed_steps(step_mode("megakernel"), mk_steps, stream, flush)
     ms_max = allreduce(world, ms, "max")
     paths = float(npix * PT_SPP * args.steps)
     units = allreduce(world, paths, "sum")
     value = units / (ms_max / 1e3) / 1e6
-    mk_value = allreduce(world, paths, "sum") / (allreduce(world, ms_mk, "max") / 1e3) / 1e6
+    mk_value = allreduce(world, float(npix * PT_SPP * mk_steps), "sum") / (allreduce(world, ms_mk, "max") / 1e3) / 1e6
 
     # e2e: wr_render returning the image to the host, PT_SPP samples per pixel per step
     barrier(world)
@@ -261,20 +290,25 @@ def run_pt(args, world, rank, local):
         "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
         "config": {"workload": "pt: 25 displaced level-5 icospheres (512,006 tris) on a ground plane, 40% diffuse / "
-                               f"40% Phong / 20% refractive, two area lights, 1024x1024, max depth 16, {PT_SPP} spp "
-                               "per step (one render call)",
+                               f"40% Phong / 20% refractive, two area lights, {PT_SIZE}x{PT_SIZE}, max depth 16, "
+                               f"{PT_SPP} spp per step (one render call), the reference's estimator",
                    "renderer": "wavefront (generate/extend/shade/shadow queues, CUDA-graph bounce loop)",
                    "l2": "flushed (512 MiB write) before every step", "parallelism": f"replicas x{world}"},
         "e2e": {"value": round(e2e, 2), "unit": "Mpaths/s", "h2d_bytes_per_step": 256 + 4 * 257,
                 "d2h_bytes_per_step": npix * 12},
-        "megakernel": {"value": round(mk_value, 2), "unit": "Mpaths/s", "ms_per_step": round(ms_mk / args.steps, 3)},
+        "megakernel": {"value": round(mk_value, 2), "unit": "Mpaths/s", "ms_per_step": round(ms_mk / mk_steps, 3),
+                       "steps": mk_steps},
         "paths_per_step": npix * PT_SPP,
         "wavefront_over_megakernel": round(value / mk_value, 3),
         "gpu_launches": int(n_launch), "clocks": clk.summary(),
     }
     if tuned:
         line["config"]["autotuned"] = {k: tuned[k] for k in ("capacity", "extend_block", "shade_block",
-                                                             "ctas_per_sm", "iters_per_graph")}
+                                                             "ctas_per_sm", "iters_per_graph", "refill_min",
+                                                             "leaf_min", "steps_per_turn", "pixel_tile")}
+        line["config"]["autotuned"]["trial_mpaths_per_s"] = round(tuned["mpaths_per_s"], 1)
+        line["config"]["autotuned"]["how"] = ("wr_autotune: coordinate descent from the defaults, 16-spp trial "
+                                              "renders of this scene")
     if rank == 0 and not args.quick:
         # roofline of the dominant kernel (the extend / traversal stage), from a
         # profiled render of one step.  Algorithmic bytes count the reference's
@@ -304,22 +338,29 @@ def run_pt(args, world, rank, local):
             "rays_per_step": prof["rays"], "iterations": prof["iterations"],
             "rays_per_s_extend": round(prof["rays"] / (prof["ms_extend"] / 1e3) / 1e6, 1),
         }
-        # time to relMSE 1e-3: per-pixel variance from 64 spp (sum and sum of
-        # squares), R = an independent 256-spp image; an n-spp image has
-        # relMSE = rel_1spp / n, so n = rel_1spp / 1e-3
-        ref = ctx.render(sid, 256, PT_DEPTH, seed=99, mode="wavefront").astype(np.float64)
-        s1, s2 = ctx.render_stats(sid, 64, PT_DEPTH, seed=11, mode="wavefront")
-        rel1, top_share = relmse_per_sample(s1, s2, 64, ref)
-        spp_needed = rel1 / 1e-3
-        ms_per_spp, ms_per_spp_mk = ms / args.steps / PT_SPP, ms_mk / args.steps / PT_SPP
-        line["time_to_relmse_1e-3"] = {
-            "wavefront_s": round(spp_needed * ms_per_spp / 1e3, 3),
-            "megakernel_s": round(spp_needed * ms_per_spp_mk / 1e3, 3),
-            "spp_needed": round(spp_needed, 1), "relmse_1spp": round(rel1, 4),
-            "share_of_top_0.1pct_entries": round(top_share, 4),
-            "formula": "mean((I-R)^2/(R^2+1e-2)) = mean(Var/(R^2+1e-2))/spp; Var per pixel from 64 spp "
-                       "(sum, sum of squares), R = independent 256-spp wavefront image",
-        }
+        # time to relMSE 1e-3 with the reference's estimator and with the
+        # low-variance one; each estimator's own throughput on both renderers
+        lv_steps = max(1, min(3, args.steps))
+        with torch.cuda.stream(stream):
+            step_mode("wavefront", LOW_VARIANCE)(0)
+            step_mode("megakernel", LOW_VARIANCE)(0)
+        ms_lv = timed_steps(step_mode("wavefront", LOW_VARIANCE), lv_steps, stream, flush)
+        ms_lv_mk = timed_steps(step_mode("megakernel", LOW_VARIANCE), lv_steps, stream, flush)
+        per = {"reference_estimator": {"wavefront": ms / args.steps / PT_SPP,
+                                       "megakernel": ms_mk / mk_steps / PT_SPP},
+               "low_variance_estimator": {"wavefront": ms_lv / lv_steps / PT_SPP,
+                                          "megakernel": ms_lv_mk / lv_steps / PT_SPP}}
+        ttr = {}
+        for name, f in (("reference_estimator", 0), ("low_variance_estimator", LOW_VARIANCE)):
+            ttr[name] = time_to_relmse(ctx, sid, f, per[name])
+            ttr[name]["mpaths_per_s"] = {k: round(npix / v / 1e3, 2) for k, v in per[name].items()}
+        ttr["formula"] = ("relMSE = mean((I-R)^2/(R^2+1e-2)) = mean(Var/(R^2+1e-2))/spp for an unbiased estimator; "
+                          "Var per pixel from 64 spp (sum, sum of squares), R = independent 256-spp wavefront image "
+                          "with the low-variance estimator; time = spp needed x measured ms per spp")
+        ttr["low_variance"] = "WR_RENDER_NEE_MIS | WR_RENDER_PHONG_MIRROR (same expectation as the reference's)"
+        ttr["plain_megakernel_reference_estimator_over_wavefront_low_variance"] = round(
+            ttr["reference_estimator"]["megakernel_s"] / ttr["low_variance_estimator"]["wavefront_s"], 1)
+        line["time_to_relmse_1e-3"] = ttr
         if world == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_pt(scene, args.cpu_rows or 64, os.cpu_count() or 1)
     ctx.close()
@@ -509,17 +550,29 @@ def run_stream(srv, sids, depths, stream):
     return [st[r] for r in rids]
 
 
-def serve_stats(stream, st):
+def serve_stats(stream, st, alone=None):
+    """Latency = finish - submit on the library's clock.  `alone` (per
+    request, seconds): the time the request's paths take on an idle GPU at
+    its scene's throughput; slowdown = latency / alone (processor sharing
+    at load rho gives about 1 / (1 - rho) to every request)."""
     lat = np.array([s["finish_s"] - s["submit_s"] for s in st])
     wait = np.array([s["admit_s"] - s["submit_s"] for s in st])
     paths = sum(s["paths_total"] for s in st)
     span = max(s["finish_s"] for s in st) - min(s["submit_s"] for s in st)
-    return {"requests": len(st), "p50_s": round(float(np.percentile(lat, 50)), 4),
-            "p99_s": round(float(np.percentile(lat, 99)), 4),
-            "p99_over_p50": round(float(np.percentile(lat, 99) / np.percentile(lat, 50)), 3),
-            "admission_wait_p50_s": round(float(np.percentile(wait, 50)), 4),
-            "mpaths_per_s": round(paths / span / 1e6, 2), "paths": int(paths), "makespan_s": round(span, 3),
-            "offered_mpaths_per_s": round(paths / (stream[-1][0] if stream else 1.0) / 1e6, 2)}
+    out = {"requests": len(st), "p50_s": round(float(np.percentile(lat, 50)), 4),
+           "p99_s": round(float(np.percentile(lat, 99)), 4),
+           "p99_over_p50": round(float(np.percentile(lat, 99) / np.percentile(lat, 50)), 3),
+           "mean_s": round(float(lat.mean()), 4),
+           "admission_wait_p50_s": round(float(np.percentile(wait, 50)), 4),
+           "mpaths_per_s": round(paths / span / 1e6, 2), "paths": int(paths), "makespan_s": round(span, 3),
+           "offered_mpaths_per_s": round(paths / (stream[-1][0] if stream else 1.0) / 1e6, 2)}
+    if alone is not None:
+        sd = lat / np.maximum(np.asarray(alone), 1e-4)
+        out["slowdown_p50"] = round(float(np.percentile(sd, 50)), 3)
+        out["slowdown_p99"] = round(float(np.percentile(sd, 99)), 3)
+        a = np.asarray(alone)
+        out["alone_p99_over_p50"] = round(float(np.percentile(a, 99) / np.percentile(a, 50)), 2)
+    return out
 
 
 def run_serve(args, world, rank, local):
@@ -545,26 +598,49 @@ def run_serve(args, world, rank, local):
                 var = np.maximum(s2 / 16 - (s1 / 16) ** 2, 0) * 16 / 15
                 rel1[(k, side)] = float(np.mean(var / (ref ** 2 + 1e-2)))
                 ctx.release(sid)
-    srv = Server(ctx, film_bytes=2 << 30, max_active=64)
-    # warm-up: one small request per scene
-    run_stream(srv, sids, depths, [(0.0, k, 128, 16) for k in range(3)])
+    # each scene's throughput alone (a 512^2 x 64-spp render), for the slowdowns
+    thr = []
+    for k, (name, sc, d) in enumerate(scenes):
+        sid = ctx.upload(scene_at(sc, 512))
+        ctx.render(sid, 4, d, seed=1, mode="wavefront")
+        t0 = time.perf_counter()
+        ctx.render(sid, 64, d, seed=2, mode="wavefront")
+        thr.append(512 * 512 * 64 / (time.perf_counter() - t0))
+        ctx.release(sid)
+
+    def alone(stream):
+        return [side * side * spp / thr[k] for (_, k, side, spp) in stream]
+
     seconds = args.serve_seconds
     legs = {}
     stream = serve_stream(seconds, SERVE_RATE, seed=2024 + rank)
+    srv = Server(ctx, film_bytes=2 << 30, max_active=64)
+    run_stream(srv, sids, depths, [(0.0, k, 128, 16) for k in range(3)])  # warm-up: one small request per scene
     with ClockSampler(local) as clk:
         st = run_stream(srv, sids, depths, stream)
-    legs["stream"] = serve_stats(stream, st)
+    legs["stream"] = serve_stats(stream, st, alone(stream))
+    legs["stream"]["slot_policy"] = "equal shares"
     if rel1:
         rr = [rel1[(k, side)] / spp for (_, k, side, spp) in stream]
         legs["stream"]["relmse_per_request"] = {"p50": float(np.percentile(rr, 50)), "max": float(max(rr))}
     # the same stream slowed to 60 % of the sustained throughput: latency without a backlog
     load = legs["stream"]["offered_mpaths_per_s"] / max(1e-9, legs["stream"]["mpaths_per_s"])
+    f = load / 0.6
+    slow = [(t * f, k, side, spp) for (t, k, side, spp) in stream]
     if load > 0.6 and not args.quick:
-        f = load / 0.6
-        st2 = run_stream(srv, sids, depths, [(t * f, k, side, spp) for (t, k, side, spp) in stream])
-        legs["stream_at_60pct_load"] = serve_stats([(t * f, *x) for (t, *x) in stream], st2)
+        st2 = run_stream(srv, sids, depths, slow)
+        legs["stream_at_60pct_load"] = serve_stats(slow, st2, alone(slow))
         legs["stream_at_60pct_load"]["rate_req_per_s"] = round(SERVE_RATE / f, 3)
+        legs["stream_at_60pct_load"]["slot_policy"] = "equal shares"
     srv.stop()
+    if load > 0.6 and not args.quick and args.workload == "serve":
+        fifo = Server(ctx, film_bytes=2 << 30, max_active=64, fifo=True)
+        run_stream(fifo, sids, depths, [(0.0, k, 128, 16) for k in range(3)])
+        st3 = run_stream(fifo, sids, depths, slow)
+        fifo.stop()
+        legs["stream_at_60pct_load_fifo"] = serve_stats(slow, st3, alone(slow))
+        legs["stream_at_60pct_load_fifo"]["rate_req_per_s"] = round(SERVE_RATE / f, 3)
+        legs["stream_at_60pct_load_fifo"]["slot_policy"] = "admission order (WR_SERVE_FIFO)"
     ctx.close()
     main_leg = legs["stream"]
     line = {
@@ -575,6 +651,7 @@ def run_serve(args, world, rank, local):
                                "mixed-material (depth 16) and media (depth 24) scenes, resolution "
                                "U{128^2..1024^2}, spp U{16,64,256}", "parallelism": f"replicas x{world}"},
         "p50_s": main_leg["p50_s"], "p99_s": main_leg["p99_s"], "legs": legs, "clocks": clk.summary(),
+        "scene_mpaths_per_s_alone": [round(x / 1e6, 1) for x in thr],
         "relmse_formula": "mean((I-R)^2/(R^2+1e-2)) = mean(Var/(R^2+1e-2))/spp, Var from 16 spp per pixel, "
                           "R = independent 64-spp image",
     }
@@ -615,7 +692,7 @@ def run_relmse(args, world, rank, local):
     import torch
 
     from walkray_gb300 import scenes as S
-    from walkray_gb300.api import Context
+    from walkray_gb300.api import LOW_VARIANCE, Context
 
     torch.cuda.set_device(local)
     ctx = Context(device=local)
@@ -624,22 +701,32 @@ def run_relmse(args, world, rank, local):
         scene = build(S)
         sid = ctx.upload(scene)
         conv_spp = args.converged_spp or CONVERGED_SPP
-        acc = None
-        t0 = time.perf_counter()
-        for k in range(conv_spp // CONVERGED_PASS):
-            img = ctx.render(sid, CONVERGED_PASS, depth, seed=7000 + k, mode="wavefront").astype(np.float64)
-            acc = img if acc is None else acc + img
-        conv = acc / (conv_spp // CONVERGED_PASS)
-        t_conv = time.perf_counter() - t0
-        row = {"spp": spp, "max_depth": depth, "converged_spp": conv_spp, "converged_s": round(t_conv, 2)}
-        for mode in ("wavefront", "megakernel"):
-            ctx.render(sid, 1, depth, seed=5, mode=mode)  # warm
-            torch.cuda.synchronize()
+        c0 = os.path.join(ROOT, "tests", "golden", "c0_ref.npz")
+        if name == "cornell_256x256" and os.path.exists(c0):
+            # configuration 0: the reference's own CPU renders (256 x 64 spp, FP64 sums)
+            g = np.load(c0)
+            conv = g["mean"].astype(np.float64)
+            row = {"spp": spp, "max_depth": depth, "converged_spp": int(g["renders"]) * int(g["spp"]),
+                   "converged": "CPU: 256 renders of WalkRay's PathTracer (64 spp each), FP64 mean (c0_ref.npz)"}
+        else:
+            acc = None
             t0 = time.perf_counter()
-            img = ctx.render(sid, spp, depth, seed=1, mode=mode).astype(np.float64)
-            dt = time.perf_counter() - t0
-            row[mode] = {"relmse": round(relmse(img, conv), 6), "seconds": round(dt, 4),
-                         "mpaths_per_s": round(img.shape[0] * img.shape[1] * spp / dt / 1e6, 2)}
+            for k in range(conv_spp // CONVERGED_PASS):
+                img = ctx.render(sid, CONVERGED_PASS, depth, seed=7000 + k, mode="wavefront").astype(np.float64)
+                acc = img if acc is None else acc + img
+            conv = acc / (conv_spp // CONVERGED_PASS)
+            row = {"spp": spp, "max_depth": depth, "converged_spp": conv_spp,
+                   "converged_s": round(time.perf_counter() - t0, 2),
+                   "converged": f"GPU: {conv_spp}-spp wavefront render, FP64 sum of {CONVERGED_PASS}-spp passes"}
+        for est, flags in (("", 0), ("_low_variance", LOW_VARIANCE)):
+            for mode in ("wavefront", "megakernel"):
+                ctx.render(sid, 1, depth, seed=5, mode=mode, flags=flags)  # warm
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                img = ctx.render(sid, spp, depth, seed=1, mode=mode, flags=flags).astype(np.float64)
+                dt = time.perf_counter() - t0
+                row[mode + est] = {"relmse": round(relmse(img, conv), 6), "seconds": round(dt, 4),
+                                   "mpaths_per_s": round(img.shape[0] * img.shape[1] * spp / dt / 1e6, 2)}
         # the variance part alone: relMSE of the image against itself rendered again
         b = ctx.render(sid, spp, depth, seed=2, mode="wavefront").astype(np.float64)
         a = ctx.render(sid, spp, depth, seed=1, mode="wavefront").astype(np.float64)
@@ -650,9 +737,11 @@ def run_relmse(args, world, rank, local):
     return {"metric": "relMSE at each configuration's spp vs a converged image", "value": None,
             "unit": "relMSE", "n_gpus": world, "higher_is_better": False, "dtype": "f32",
             "data": "synthetic (seeded scene generators)", "configs": out,
-            "formula": "mean over pixels and channels of (I-R)^2/(R^2+1e-2); R = 16,384-spp wavefront render "
-                       "accumulated in FP64 from 256-spp FP32 passes (seeds 7000+), I = one render at the "
-                       "configuration's spp (seed 1); times are wall-clock through wr_render (host image)"}
+            "formula": "mean over pixels and channels of (I-R)^2/(R^2+1e-2); R per configuration (row 'converged'): "
+                       "configuration 0 the reference's 16,384-spp CPU image, the others a 16,384-spp GPU render "
+                       "accumulated in FP64; I = one render at the configuration's spp (seed 1), with the "
+                       "reference's estimator and with the low-variance one; times are wall-clock through "
+                       "wr_render (host image)"}
 
 
 # ---------------------------------------------------------------------------
@@ -780,7 +869,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["pt", "kd", "serve", "relmse", "bpt"], default=os.environ.get("WR_BENCH_WORKLOAD", "pt"))
-    ap.add_argument("--tune", action="store_true", help="run the wavefront autotuner first (pt)")
+    ap.add_argument("--no-tune", action="store_true", help="pt: skip the wavefront autotuner (defaults instead)")
     ap.add_argument("--quick", action="store_true", help="skip the roofline profile, relMSE and CPU legs (pt)")
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--cpu-rows", type=int, default=0)
@@ -788,6 +877,8 @@ def main():
     ap.add_argument("--kd-rays", type=int, default=1 << 24, help="rays per step (kd); smaller for ncu captures")
     ap.add_argument("--kd-exact", action="store_true", help="kd: visit every box the reference visits (no pruning)")
     ap.add_argument("--pt-spp", type=int, default=PT_SPP, help="samples per pixel per step (pt)")
+    ap.add_argument("--mk-steps", type=int, default=5, help="timed megakernel steps beside the pt line (at most --steps)")
+    ap.add_argument("--no-extras", action="store_true", help="pt: leave out the kd and serving legs")
     ap.add_argument("--pt-size", type=int, default=PT_SIZE, help="image side (pt); smaller for ncu captures")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window of the request stream (serve)")
     ap.add_argument("--converged-spp", type=int, default=0, help="spp of the converged image (relmse)")
@@ -813,6 +904,16 @@ def main():
     build.build_lib()
     run = {"pt": run_pt, "kd": run_kd, "serve": run_serve, "relmse": run_relmse, "bpt": run_bpt}[args.workload]
     line = run(args, world, rank, local)
+    if args.workload == "pt" and world == 1 and not args.no_extras:
+        # the kd microbenchmark and a short serving stream in the same run
+        kd = run_kd(args, world, rank, local)
+        line["kd"] = {k: kd[k] for k in ("metric", "value", "unit", "ms_per_step", "e2e", "roofline", "config",
+                                         "gpu_launches", "clocks") if k in kd}
+        if "cpu_baseline" in kd:
+            line["kd"]["cpu_baseline"] = kd["cpu_baseline"]
+        sv = run_serve(args, world, rank, local)
+        line["serve"] = {k: sv[k] for k in sv if k not in ("n_gpus", "steps", "warmup", "higher_is_better",
+                                                            "scaling", "vs_baseline", "dtype", "data")}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
