@@ -59,7 +59,9 @@ struct TraceTune {
     int leaf_min;    // lanes holding postponed leaves that start the warp's leaf phase
     int steps;       // traversal steps a searching lane takes per turn of the warp loop (1..8)
 };
-inline TraceTune default_trace_tune() { return TraceTune{8, 8, 1}; }  // fastest of a sweep on GB300
+// fastest of sweeps on GB300: kd workload 4333 Mrays/s with one step per
+// turn, 4567 with four (2: 4246, 3: 4436)
+inline TraceTune default_trace_tune() { return TraceTune{8, 8, 4}; }
 
 struct f3 {
     float x, y, z;
