@@ -552,9 +552,10 @@ def run_stream(srv, sids, depths, stream):
 
 def serve_stats(stream, st, alone=None):
     """Latency = finish - submit on the library's clock.  `alone` (per
-    request, seconds): the time the request's paths take on an idle GPU at
-    its scene's throughput; slowdown = latency / alone (processor sharing
-    at load rho gives about 1 / (1 - rho) to every request)."""
+    request, seconds): its latency on an idle loop (the scene's latency
+    floor plus its paths at the scene's throughput); slowdown = latency /
+    alone (processor sharing at load rho gives about 1 / (1 - rho) to every
+    request)."""
     lat = np.array([s["finish_s"] - s["submit_s"] for s in st])
     wait = np.array([s["admit_s"] - s["submit_s"] for s in st])
     paths = sum(s["paths_total"] for s in st)
@@ -608,14 +609,22 @@ def run_serve(args, world, rank, local):
         thr.append(512 * 512 * 64 / (time.perf_counter() - t0))
         ctx.release(sid)
 
-    def alone(stream):
-        return [side * side * spp / thr[k] for (_, k, side, spp) in stream]
-
     seconds = args.serve_seconds
     legs = {}
     stream = serve_stream(seconds, SERVE_RATE, seed=2024 + rank)
     srv = Server(ctx, film_bytes=2 << 30, max_active=64)
     run_stream(srv, sids, depths, [(0.0, k, 128, 16) for k in range(3)])  # warm-up: one small request per scene
+    # the latency floor of each scene: its smallest request (128^2 x 16 spp) alone on the idle loop
+    # (a path's bounces are graph replays, whatever the request's size)
+    floor = []
+    for k in range(3):
+        lat = [(lambda s: s["finish_s"] - s["submit_s"])(run_stream(srv, sids, depths, [(0.0, k, 128, 16)])[0])
+               for _ in range(3)]
+        floor.append(float(np.median(lat)))
+
+    def alone(stream):
+        return [floor[k] + max(0, side * side * spp - 128 * 128 * 16) / thr[k] for (_, k, side, spp) in stream]
+
     with ClockSampler(local) as clk:
         st = run_stream(srv, sids, depths, stream)
     legs["stream"] = serve_stats(stream, st, alone(stream))
@@ -652,6 +661,9 @@ def run_serve(args, world, rank, local):
                                "U{128^2..1024^2}, spp U{16,64,256}", "parallelism": f"replicas x{world}"},
         "p50_s": main_leg["p50_s"], "p99_s": main_leg["p99_s"], "legs": legs, "clocks": clk.summary(),
         "scene_mpaths_per_s_alone": [round(x / 1e6, 1) for x in thr],
+        "scene_latency_floor_s": [round(x, 4) for x in floor],
+        "slowdown": "latency / alone, alone = the scene's latency floor + the request's further paths at the "
+                    "scene's throughput alone",
         "relmse_formula": "mean((I-R)^2/(R^2+1e-2)) = mean(Var/(R^2+1e-2))/spp, Var from 16 spp per pixel, "
                           "R = independent 64-spp image",
     }
