@@ -417,7 +417,7 @@ typedef struct wr_wavefront_config {
     int32_t pixel_tile;      /* camera paths generated tile by tile, square tiles of this many pixels a
                                 side (0 = row by row); the image does not depend on it */
     int32_t steps_per_turn;  /* traversal: steps a searching lane takes per turn of a warp's loop (1..8,
-                                0 = default 4); also applies to wr_trace_closest */
+                                0 = default 6); also applies to wr_trace_closest */
     double mpaths_per_s;     /* filled by wr_autotune */
 } wr_wavefront_config;
 

@@ -2,7 +2,7 @@
 // timing short renders on the device, and keeps the fastest in the context
 // for later wavefront renders.  The search is coordinate descent from the
 // shipped defaults (2^24 paths in flight, the 6-CTA extend variant, refill
-// and leaf thresholds 8, four traversal steps per turn, rows, 4 iteration
+// and leaf thresholds 8, six traversal steps per turn, rows, 4 iteration
 // pairs per graph launch): each dimension in turn tries its candidate values
 // with the others held at the best so far, and keeps a value only if it
 // renders faster.
@@ -70,11 +70,11 @@ int wr_autotune(wr_ctx* ctx, wr_scene_id scene, uint32_t spp_per_trial, uint32_t
         return (double)n / 3 * spp_per_trial / (ms * 1e-3) / 1e6;
     };
     // the shipped defaults, then one dimension at a time
-    wr_wavefront_config top{1u << 24, 128, 128, 6, 4, 8, 8, 0, 0, 4, 0.0};
+    wr_wavefront_config top{1u << 24, 128, 128, 6, 4, 8, 8, 0, 0, 6, 0.0};
     double top_rate = trial(top);
     enum { CAP, CTAS, REFILL, LEAF, STEPS, TILE, ITERS, NDIM };
     const std::vector<int> values[NDIM] = {
-        {1 << 22, 1 << 23, 1 << 24}, {6, 8}, {4, 8, 16}, {4, 8, 16}, {1, 2, 4, 8}, {0, 8, 16, 32}, {2, 4, 8}};
+        {1 << 22, 1 << 23, 1 << 24}, {6, 8}, {4, 8, 16}, {4, 8, 16}, {1, 2, 4, 6, 8}, {0, 8, 16, 32}, {2, 4, 8}};
     for (int dim = 0; dim < NDIM; dim++) {
         for (int v : values[dim]) {
             wr_wavefront_config c = top;

@@ -59,9 +59,9 @@ struct TraceTune {
     int leaf_min;    // lanes holding postponed leaves that start the warp's leaf phase
     int steps;       // traversal steps a searching lane takes per turn of the warp loop (1..8)
 };
-// fastest of sweeps on GB300: kd workload 4333 Mrays/s with one step per
-// turn, 4567 with four (2: 4246, 3: 4436)
-inline TraceTune default_trace_tune() { return TraceTune{8, 8, 4}; }
+// fastest of sweeps on GB300, kd workload: 4349 Mrays/s with one step per
+// turn, 4568 with four, 4699 with six, 4673 with eight
+inline TraceTune default_trace_tune() { return TraceTune{8, 8, 6}; }
 
 struct f3 {
     float x, y, z;
