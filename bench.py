@@ -612,6 +612,8 @@ def run_serve(args, world, rank, local):
     seconds = args.serve_seconds
     legs = {}
     stream = serve_stream(seconds, SERVE_RATE, seed=2024 + rank)
+    if args.serve_capacity:  # paths in flight of the shared queues (default 2^24)
+        ctx.set_wavefront_config(capacity=args.serve_capacity)
     srv = Server(ctx, film_bytes=2 << 30, max_active=64)
     run_stream(srv, sids, depths, [(0.0, k, 128, 16) for k in range(3)])  # warm-up: one small request per scene
     # the latency floor of each scene: its smallest request (128^2 x 16 spp) alone on the idle loop
@@ -660,6 +662,7 @@ def run_serve(args, world, rank, local):
                                "mixed-material (depth 16) and media (depth 24) scenes, resolution "
                                "U{128^2..1024^2}, spp U{16,64,256}", "parallelism": f"replicas x{world}"},
         "p50_s": main_leg["p50_s"], "p99_s": main_leg["p99_s"], "legs": legs, "clocks": clk.summary(),
+        "queue_capacity": args.serve_capacity or (1 << 24),
         "scene_mpaths_per_s_alone": [round(x / 1e6, 1) for x in thr],
         "scene_latency_floor_s": [round(x, 4) for x in floor],
         "slowdown": "latency / alone, alone = the scene's latency floor + the request's further paths at the "
@@ -893,6 +896,7 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="pt: leave out the kd and serving legs")
     ap.add_argument("--pt-size", type=int, default=PT_SIZE, help="image side (pt); smaller for ncu captures")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window of the request stream (serve)")
+    ap.add_argument("--serve-capacity", type=int, default=0, help="serve: paths in flight of the queues (0 = 2^24)")
     ap.add_argument("--converged-spp", type=int, default=0, help="spp of the converged image (relmse)")
     args = ap.parse_args()
     globals()["PT_SIZE"] = args.pt_size

@@ -404,7 +404,7 @@ typedef struct wr_wavefront_config {
     uint32_t capacity;       /* paths in flight (queue length) */
     int32_t extend_block;    /* threads per CTA of the traversal stage (32..128) */
     int32_t shade_block;     /* threads per CTA of the shade / generate stages (32..128) */
-    int32_t ctas_per_sm;     /* traversal kernels compiled for at least 1-5, 6-7 or 8+ resident CTAs
+    int32_t ctas_per_sm;     /* traversal kernels compiled for at least 1-5, 6, 7 or 8+ resident CTAs
                                 per SM (fewer registers per thread as it grows), launched with at most
                                 that many; 0 = tuned defaults (6 for rendering, 8 for
                                 wr_trace_closest); also applies to wr_trace_closest */

@@ -74,7 +74,7 @@ int wr_autotune(wr_ctx* ctx, wr_scene_id scene, uint32_t spp_per_trial, uint32_t
     double top_rate = trial(top);
     enum { CAP, CTAS, REFILL, LEAF, STEPS, TILE, ITERS, NDIM };
     const std::vector<int> values[NDIM] = {
-        {1 << 22, 1 << 23, 1 << 24}, {6, 8}, {4, 8, 16}, {4, 8, 16}, {1, 2, 4, 6, 8}, {0, 8, 16, 32}, {2, 4, 8}};
+        {1 << 22, 1 << 23, 1 << 24}, {6, 7, 8}, {4, 8, 16}, {4, 8, 16}, {1, 2, 4, 6, 8}, {0, 8, 16, 32}, {2, 4, 8}};
     for (int dim = 0; dim < NDIM; dim++) {
         for (int v : values[dim]) {
             wr_wavefront_config c = top;

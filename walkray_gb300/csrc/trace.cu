@@ -74,6 +74,7 @@ cudaError_t launch_trace_closest(const DevTree& T, const float* d_rays, uint64_t
     void (*kern)(DevTree, const float*, uint64_t, const int32_t*, const int32_t*, wr_hit*, unsigned long long*, int,
                  TraceTune, unsigned int*) =
         variant >= 8   ? (prune ? k_trace_closest<true, 8> : k_trace_closest<false, 8>)
+        : variant >= 7 ? (prune ? k_trace_closest<true, 7> : k_trace_closest<false, 7>)
         : variant >= 6 ? (prune ? k_trace_closest<true, 6> : k_trace_closest<false, 6>)
                            : (prune ? k_trace_closest<true, 0> : k_trace_closest<false, 0>);
     if (smem > 48 * 1024) {

@@ -273,6 +273,7 @@ using ExtendKernel = void (*)(const RenderScene*, const WfJob*, WfSide, int2*, u
 static ExtendKernel extend_kernel(int ctas_per_sm, bool stats) {
     if (ctas_per_sm == 0) ctas_per_sm = 6;
     if (ctas_per_sm >= 8) return stats ? k_wf_extend<true, 8> : k_wf_extend<false, 8>;
+    if (ctas_per_sm >= 7) return stats ? k_wf_extend<true, 7> : k_wf_extend<false, 7>;
     if (ctas_per_sm >= 6) return stats ? k_wf_extend<true, 6> : k_wf_extend<false, 6>;
     return stats ? k_wf_extend<true, 0> : k_wf_extend<false, 0>;
 }
