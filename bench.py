@@ -726,13 +726,17 @@ def run_relmse(args, world, rank, local):
         else:
             acc = None
             t0 = time.perf_counter()
+            # the low-variance estimator converges far faster to the same expectation (the
+            # reference's Phong estimator has infinite variance on the mixed scene)
             for k in range(conv_spp // CONVERGED_PASS):
-                img = ctx.render(sid, CONVERGED_PASS, depth, seed=7000 + k, mode="wavefront").astype(np.float64)
+                img = ctx.render(sid, CONVERGED_PASS, depth, seed=7000 + k, mode="wavefront",
+                                 flags=LOW_VARIANCE).astype(np.float64)
                 acc = img if acc is None else acc + img
             conv = acc / (conv_spp // CONVERGED_PASS)
             row = {"spp": spp, "max_depth": depth, "converged_spp": conv_spp,
                    "converged_s": round(time.perf_counter() - t0, 2),
-                   "converged": f"GPU: {conv_spp}-spp wavefront render, FP64 sum of {CONVERGED_PASS}-spp passes"}
+                   "converged": f"GPU: {conv_spp}-spp wavefront render with the low-variance estimator, FP64 sum "
+                                f"of {CONVERGED_PASS}-spp passes"}
         for est, flags in (("", 0), ("_low_variance", LOW_VARIANCE)):
             for mode in ("wavefront", "megakernel"):
                 ctx.render(sid, 1, depth, seed=5, mode=mode, flags=flags)  # warm
@@ -754,7 +758,7 @@ def run_relmse(args, world, rank, local):
             "data": "synthetic (seeded scene generators)", "configs": out,
             "formula": "mean over pixels and channels of (I-R)^2/(R^2+1e-2); R per configuration (row 'converged'): "
                        "configuration 0 the reference's 16,384-spp CPU image, the others a 16,384-spp GPU render "
-                       "accumulated in FP64; I = one render at the configuration's spp (seed 1), with the "
+                       "with the low-variance estimator accumulated in FP64; I = one render at the configuration's spp (seed 1), with the "
                        "reference's estimator and with the low-variance one; times are wall-clock through "
                        "wr_render (host image)"}
 
