@@ -406,7 +406,7 @@ typedef struct wr_wavefront_config {
     int32_t shade_block;     /* threads per CTA of the shade / generate stages (32..128) */
     int32_t ctas_per_sm;     /* traversal kernels compiled for at least 1-5, 6, 7 or 8+ resident CTAs
                                 per SM (fewer registers per thread as it grows), launched with at most
-                                that many; 0 = tuned defaults (6 for rendering, 8 for
+                                that many; 0 = tuned defaults (6 for rendering, 7 for
                                 wr_trace_closest); also applies to wr_trace_closest */
     int32_t iters_per_graph; /* bounce-loop iterations (pairs) per CUDA-graph launch */
     int32_t refill_min;      /* traversal: idle lanes of a warp that trigger a ray refill (1..32, 0 = default) */

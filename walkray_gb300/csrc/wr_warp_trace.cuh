@@ -38,10 +38,6 @@ struct TraceLane {
     uint32_t n_box, n_tri;        // work counters (profiling only)
 };
 
-__device__ __forceinline__ void prefetch_l1(const void* p) {
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
-}
-
 // Starts a ray: the root's box test; the root pair goes on the stack, or a
 // root leaf is postponed.
 __device__ __forceinline__ void lane_start(TraceLane& L, const Box& root, uint32_t w0, uint32_t w1, uint32_t* stack,
@@ -94,23 +90,15 @@ __device__ __forceinline__ void lane_step(TraceLane& L, uint32_t* stack, int str
         L.sp = 0;
         return;
     }
-    uint32_t next = 0xffffffffu;  // the pair the next step pops
     if (hl && hr) {
         const bool lnear = tl <= tr;
         stack[(L.sp++) * stride] = lnear ? W.z : W.x;
         stack[(L.sp++) * stride] = lnear ? W.x : W.z;
-        next = lnear ? W.x : W.z;
     } else if (hl) {
         stack[(L.sp++) * stride] = W.x;
-        next = W.x;
     } else if (hr) {
         stack[(L.sp++) * stride] = W.z;
-        next = W.z;
     }
-    // start the next pair's and the postponed leaf's loads into L1 now: a
-    // hint, no registers held, the result is unchanged
-    if (next != 0xffffffffu) prefetch_l1(L.pairs + next);
-    if (L.npend) prefetch_l1(L.tris + L.lf0);
 }
 
 // The postponed leaves of a lane, through one code path for the warp.
