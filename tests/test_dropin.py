@@ -1,8 +1,8 @@
 """The C++ drop-in renderer (walkray_gb300/host/gpuPathTracer.*) compiled
 against WalkRay's own headers, and its reading of WalkRay's material objects
 (wrDefaultDescribe) checked against the scene descriptions.  Needs a
-WalkRay source tree named by the environment variable WR_REFERENCE_DIR;
-skipped without one."""
+WalkRay source tree (the environment variable WR_REFERENCE_DIR, else the
+oracle Makefile's default); skipped without one."""
 import os
 import subprocess
 
@@ -11,15 +11,16 @@ import pytest
 
 import make_golden
 from walkray_gb300 import scenes as S
+from walkray_gb300.build import reference_dir
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("WR_REFERENCE_DIR", "")
+REF = reference_dir()
 
 
 @pytest.fixture(scope="module")
 def dropin(built):
     if not REF or not os.path.isfile(os.path.join(REF, "kdtree.cpp")):
-        pytest.skip("WR_REFERENCE_DIR does not name a WalkRay source tree")
+        pytest.skip("no WalkRay source tree (WR_REFERENCE_DIR)")
     subprocess.run(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle"), "dropin", f"REF={REF}"], check=True)
     return os.path.join(ROOT, "oracle", "_ref", "wr_ref_dropin")
 

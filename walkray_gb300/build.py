@@ -89,15 +89,28 @@ def build_lib(verbose: bool = False) -> str:
     return LIB
 
 
+def reference_dir() -> str:
+    """The WalkRay source tree the oracle's reference harness compiles: the
+    environment variable WR_REFERENCE_DIR, else the oracle Makefile's default
+    when that tree is present; "" when there is none (as on a machine that
+    only runs the prebuilt library)."""
+    ref = os.environ.get("WR_REFERENCE_DIR", "")
+    if not ref:
+        r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref-dir"],
+                           capture_output=True, text=True)
+        ref = r.stdout.strip() if r.returncode == 0 else ""
+    return ref if ref and os.path.isfile(os.path.join(ref, "kdtree.cpp")) else ""
+
+
 def build_oracle(verbose: bool = False) -> None:
-    """The C restatement always; the reference harness too when the
-    environment variable WR_REFERENCE_DIR names a WalkRay source tree."""
+    """The C restatement always; the reference harness too when a WalkRay
+    source tree is present (reference_dir)."""
     odir = os.path.join(ROOT, "oracle")
     r = subprocess.run(["make", "-s", "-C", odir, "port"], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
-    ref = os.environ.get("WR_REFERENCE_DIR", "")
-    if ref and os.path.isfile(os.path.join(ref, "kdtree.cpp")):
+    ref = reference_dir()
+    if ref:
         r = subprocess.run(["make", "-s", "-j8", "-C", odir, "ref", f"REF={ref}"], capture_output=True, text=True)
         if r.returncode != 0 and verbose:
             print("reference harness not built:", r.stderr[-2000:])
