@@ -20,7 +20,8 @@ Prints ONE JSON line (rank 0).  Workloads:
   kd  closest-hit microbenchmark: level-8 displaced icosphere (1,310,720
       triangles), 2^24 rays; one step = all rays.  Metric: Mrays/s.
   serve  a seeded Poisson stream of render requests through the serving
-      loop: p50 / p99 latency, slowdowns and Mpaths/s.
+      loop (20 requests/s for 60 s; 10 s inside the default line): p50 / p99
+      latency, slowdowns and Mpaths/s, at that rate and slowed to 60 % load.
   relmse relMSE of each path-tracing configuration at its own spp against a
       converged image (configuration 0: the reference's 16,384-spp CPU image).
   bpt bidirectional path tracing (WR_MODE_BIDIRECTIONAL) of the Cornell box,
@@ -609,7 +610,7 @@ def run_serve(args, world, rank, local):
         thr.append(512 * 512 * 64 / (time.perf_counter() - t0))
         ctx.release(sid)
 
-    seconds = args.serve_seconds
+    seconds = args.serve_seconds or (60.0 if args.workload == "serve" else 10.0)
     legs = {}
     stream = serve_stream(seconds, SERVE_RATE, seed=2024 + rank)
     if args.serve_capacity:  # paths in flight of the shared queues (default 2^24)
@@ -899,7 +900,8 @@ def main():
     ap.add_argument("--mk-steps", type=int, default=5, help="timed megakernel steps beside the pt line (at most --steps)")
     ap.add_argument("--no-extras", action="store_true", help="pt: leave out the kd and serving legs")
     ap.add_argument("--pt-size", type=int, default=PT_SIZE, help="image side (pt); smaller for ncu captures")
-    ap.add_argument("--serve-seconds", type=float, default=10.0, help="arrival window of the request stream (serve)")
+    ap.add_argument("--serve-seconds", type=float, default=0.0,
+                    help="arrival window of the request stream (0 = 60 s for --workload serve, 10 s in the pt line)")
     ap.add_argument("--serve-capacity", type=int, default=0, help="serve: paths in flight of the queues (0 = 2^24)")
     ap.add_argument("--converged-spp", type=int, default=0, help="spp of the converged image (relmse)")
     args = ap.parse_args()
