@@ -613,9 +613,8 @@ def run_serve(args, world, rank, local):
     seconds = args.serve_seconds or (60.0 if args.workload == "serve" else 10.0)
     legs = {}
     stream = serve_stream(seconds, SERVE_RATE, seed=2024 + rank)
-    if args.serve_capacity:  # paths in flight of the shared queues (default 2^24)
-        ctx.set_wavefront_config(capacity=args.serve_capacity)
-    srv = Server(ctx, film_bytes=2 << 30, max_active=64)
+    pif = args.serve_capacity  # queue length while serving; 0 = the library's default (2^22)
+    srv = Server(ctx, film_bytes=2 << 30, max_active=64, paths_in_flight=pif)
     run_stream(srv, sids, depths, [(0.0, k, 128, 16) for k in range(3)])  # warm-up: one small request per scene
     # the latency floor of each scene: its smallest request (128^2 x 16 spp) alone on the idle loop
     # (a path's bounces are graph replays, whatever the request's size)
@@ -646,7 +645,7 @@ def run_serve(args, world, rank, local):
         legs["stream_at_60pct_load"]["slot_policy"] = "equal shares"
     srv.stop()
     if load > 0.6 and not args.quick and args.workload == "serve":
-        fifo = Server(ctx, film_bytes=2 << 30, max_active=64, fifo=True)
+        fifo = Server(ctx, film_bytes=2 << 30, max_active=64, fifo=True, paths_in_flight=pif)
         run_stream(fifo, sids, depths, [(0.0, k, 128, 16) for k in range(3)])
         st3 = run_stream(fifo, sids, depths, slow)
         fifo.stop()
@@ -663,7 +662,7 @@ def run_serve(args, world, rank, local):
                                "mixed-material (depth 16) and media (depth 24) scenes, resolution "
                                "U{128^2..1024^2}, spp U{16,64,256}", "parallelism": f"replicas x{world}"},
         "p50_s": main_leg["p50_s"], "p99_s": main_leg["p99_s"], "legs": legs, "clocks": clk.summary(),
-        "queue_capacity": args.serve_capacity or (1 << 24),
+        "queue_capacity": args.serve_capacity or (1 << 22),
         "scene_mpaths_per_s_alone": [round(x / 1e6, 1) for x in thr],
         "scene_latency_floor_s": [round(x, 4) for x in floor],
         "slowdown": "latency / alone, alone = the scene's latency floor + the request's further paths at the "
@@ -902,7 +901,8 @@ def main():
     ap.add_argument("--pt-size", type=int, default=PT_SIZE, help="image side (pt); smaller for ncu captures")
     ap.add_argument("--serve-seconds", type=float, default=0.0,
                     help="arrival window of the request stream (0 = 60 s for --workload serve, 10 s in the pt line)")
-    ap.add_argument("--serve-capacity", type=int, default=0, help="serve: paths in flight of the queues (0 = 2^24)")
+    ap.add_argument("--serve-capacity", type=int, default=0,
+                    help="serve: queue length while serving (wr_serve_desc.paths_in_flight; 0 = 2^22)")
     ap.add_argument("--converged-spp", type=int, default=0, help="spp of the converged image (relmse)")
     args = ap.parse_args()
     globals()["PT_SIZE"] = args.pt_size

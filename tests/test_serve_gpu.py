@@ -71,6 +71,32 @@ def test_serving_image_matches_wr_render(sctx):
     assert np.allclose(img, ref, rtol=1e-4, atol=1e-5)
 
 
+@pytest.mark.parametrize("paths", [4096, 1 << 16])
+def test_queue_length_does_not_change_images(sctx, paths):
+    """wr_serve_desc.paths_in_flight sets the serving queue's length (a
+    request's paths then pass through it in many more rounds); the images
+    stay those of wr_render, and lengths outside 1024 .. 2^25 are refused."""
+    ctx, ids = sctx
+    srv = Server(ctx, paths_in_flight=paths)
+    try:
+        rids = [srv.submit(ids[name], w, h, spp, d, seed) for name, w, h, spp, d, seed in MIX[:3]]
+        srv.wait(rids)
+        imgs = [srv.fetch(r) for r in rids]
+    finally:
+        srv.stop()
+    for (name, w, h, spp, d, seed), img in zip(MIX[:3], imgs):
+        srv1 = Server(ctx)
+        try:
+            r = srv1.submit(ids[name], w, h, spp, d, seed)
+            srv1.wait([r])
+            ref = srv1.fetch(r)
+        finally:
+            srv1.stop()
+        assert np.allclose(img, ref, rtol=1e-4, atol=1e-5), (name, np.abs(img - ref).max())
+    with pytest.raises(RuntimeError):
+        Server(ctx, paths_in_flight=512)
+
+
 def test_admission_waits_for_film_memory(sctx):
     """A film arena with room for about two 128x128 films: requests queue,
     are admitted as memory frees, and all finish in submission order of

@@ -102,7 +102,8 @@ class wr_wavefront_config(C.Structure):
 
 
 class wr_serve_desc(C.Structure):
-    _fields_ = [("film_bytes", C.c_uint64), ("max_active", C.c_uint32), ("flags", C.c_uint32)]
+    _fields_ = [("film_bytes", C.c_uint64), ("max_active", C.c_uint32), ("flags", C.c_uint32),
+                ("paths_in_flight", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class wr_request_desc(C.Structure):

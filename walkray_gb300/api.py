@@ -243,11 +243,13 @@ class Server:
     """The serving loop of a Context (wr_serve_start ... wr_serve_stop):
     requests admitted by film memory, their paths sharing the wavefront queues."""
 
-    def __init__(self, ctx: Context, film_bytes: int = 0, max_active: int = 0, fifo: bool = False):
+    def __init__(self, ctx: Context, film_bytes: int = 0, max_active: int = 0, fifo: bool = False,
+                 paths_in_flight: int = 0):
         """`fifo`: queue slots go to the requests in admission order instead
-        of in equal shares (WR_SERVE_FIFO)."""
+        of in equal shares (WR_SERVE_FIFO); `paths_in_flight`: the queue
+        length while serving (0 = 2^22, WR_SERVE_DEFAULT_PATHS)."""
         self.ctx = ctx
-        d = L.wr_serve_desc(film_bytes, max_active, L.WR_SERVE_FIFO if fifo else 0)
+        d = L.wr_serve_desc(film_bytes, max_active, L.WR_SERVE_FIFO if fifo else 0, paths_in_flight, 0)
         ctx._check(ctx.lib.wr_serve_start(ctx.h, C.byref(d)))
         self.sizes: dict[int, tuple[int, int]] = {}
 

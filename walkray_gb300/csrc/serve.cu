@@ -10,7 +10,9 @@
 // or admission order with WR_SERVE_FIFO) -- (3) reads the per-job path
 // counters and retires
 // every request whose paths have all reached its film (copy to the host,
-// free the arena block and the slot).  New requests therefore join while
+// free the arena block and the slot).  The serving queue is shorter than the
+// renderer's (wr_serve_desc.paths_in_flight, 2^22 by default): a request's
+// every bounce waits for one pass of the loop over the whole queue.  New requests therefore join while
 // older ones run, and their paths share the same queues; a request's image
 // depends only on its own seed, not on what else is in flight.
 #include <algorithm>
@@ -267,7 +269,13 @@ int wr_serve_start(wr_ctx* ctx, const wr_serve_desc* desc) {
         WR_CUDA(ctx, S->arena_mem.reserve(film));
         S->arena.init(S->arena_mem.as<char>(), film);
         WR_CUDA(ctx, cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
-        int rc = wf_engine_get(ctx, wf_tuned_config(ctx), &S->E);
+        const uint32_t pif = desc && desc->paths_in_flight ? desc->paths_in_flight : WR_SERVE_DEFAULT_PATHS;
+        if (pif < 1024 || pif > (1u << 25) || (desc && desc->reserved))
+            return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "paths_in_flight must be 1024 .. 2^25, reserved 0");
+        // the serving queue: no longer than the renderer's
+        WfConfig cfg = wf_tuned_config(ctx);
+        cfg.capacity = std::min(cfg.capacity, pif);
+        int rc = wf_engine_get(ctx, cfg, &S->E);
         if (rc != WR_OK) return rc;
         if ((rc = wf_set_equal_share(ctx, S->E, !(desc && (desc->flags & WR_SERVE_FIFO)))) != WR_OK) return rc;
         // start from an empty job table and empty queues
