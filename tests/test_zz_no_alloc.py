@@ -3,8 +3,9 @@ memory while they render (real-time loops that avoid cudaMalloc / cudaFree
 because they can stall the device, applications whose device memory belongs
 to their own pool).  Through the C ABI it must give the image wr_render gives,
 on two calls in a row (the shared film array keeps the previous call's
-contents and must be cleared by each call), report a clean traversal status
-through wr_render_noalloc_status, reject images larger than its fixed film,
+contents and must be cleared by each call) without the device's free memory
+moving between them, report a clean traversal status through
+wr_render_noalloc_status, reject images larger than its fixed film,
 refuse scenes whose rendering tables were never built and scenes wr_render
 itself refuses.  Collected last on purpose (file name)."""
 import ctypes as C
@@ -46,6 +47,7 @@ def test_noalloc_matches_wr_render_twice(built):
         assert fn(ctx.h, sid, C.byref(d), C.c_void_p(out.data_ptr()), None) == 8
         ref = ctx.render(sid, 16, 8, seed=5, mode="megakernel")
         stream = torch.cuda.current_stream()
+        free = []
         for _ in range(2):
             out.fill_(-1.0)
             rc = fn(ctx.h, sid, C.byref(d), C.c_void_p(out.data_ptr()), C.c_void_p(stream.cuda_stream))
@@ -56,6 +58,10 @@ def test_noalloc_matches_wr_render_twice(built):
             word = C.c_uint(12345)
             assert _status(ctx.lib)(ctx.h, C.c_void_p(stream.cuda_stream), C.byref(word)) == 0
             assert word.value == 0
+            torch.cuda.synchronize()
+            free.append(torch.cuda.mem_get_info()[0])
+        # the first call may load its kernels' code; the second allocates nothing
+        assert free[0] == free[1], free
         # a different image through the same film after a larger one
         d2 = L.wr_render_desc(4, 8, 6, 0, 0, 0, 0)
         ref2 = ctx.render(sid, 4, 8, seed=6, mode="megakernel")
