@@ -613,7 +613,7 @@ def run_serve(args, world, rank, local):
     seconds = args.serve_seconds or (60.0 if args.workload == "serve" else 10.0)
     legs = {}
     stream = serve_stream(seconds, SERVE_RATE, seed=2024 + rank)
-    pif = args.serve_capacity  # queue length while serving; 0 = the library's default (2^22)
+    pif = args.serve_capacity  # queue length while nobody waits for admission; 0 = the library's default (2^22)
     srv = Server(ctx, film_bytes=2 << 30, max_active=64, paths_in_flight=pif)
     run_stream(srv, sids, depths, [(0.0, k, 128, 16) for k in range(3)])  # warm-up: one small request per scene
     # the latency floor of each scene: its smallest request (128^2 x 16 spp) alone on the idle loop
@@ -662,7 +662,8 @@ def run_serve(args, world, rank, local):
                                "mixed-material (depth 16) and media (depth 24) scenes, resolution "
                                "U{128^2..1024^2}, spp U{16,64,256}", "parallelism": f"replicas x{world}"},
         "p50_s": main_leg["p50_s"], "p99_s": main_leg["p99_s"], "legs": legs, "clocks": clk.summary(),
-        "queue_capacity": args.serve_capacity or (1 << 22),
+        "queue_paths": {"no_request_waiting": args.serve_capacity or (1 << 22),
+                        "requests_waiting": "the wavefront capacity (2^24 unless configured)"},
         "scene_mpaths_per_s_alone": [round(x / 1e6, 1) for x in thr],
         "scene_latency_floor_s": [round(x, 4) for x in floor],
         "slowdown": "latency / alone, alone = the scene's latency floor + the request's further paths at the "
@@ -902,7 +903,7 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=0.0,
                     help="arrival window of the request stream (0 = 60 s for --workload serve, 10 s in the pt line)")
     ap.add_argument("--serve-capacity", type=int, default=0,
-                    help="serve: queue length while serving (wr_serve_desc.paths_in_flight; 0 = 2^22)")
+                    help="serve: queue length while no request waits (wr_serve_desc.paths_in_flight; 0 = 2^22)")
     ap.add_argument("--converged-spp", type=int, default=0, help="spp of the converged image (relmse)")
     args = ap.parse_args()
     globals()["PT_SIZE"] = args.pt_size

@@ -364,14 +364,15 @@ typedef struct wr_serve_desc {
     uint64_t film_bytes;      /* device memory for request films; 0 = a quarter of the context budget */
     uint32_t max_active;      /* requests in flight at once; 0 = 64 */
     uint32_t flags;           /* WR_SERVE_* */
-    uint32_t paths_in_flight; /* queue length while serving (1024 .. 2^25, at most the wavefront
-                                 configuration's capacity); 0 = WR_SERVE_DEFAULT_PATHS */
+    uint32_t paths_in_flight; /* queue length while no request waits for admission (1024 .. 2^25,
+                                 at most the wavefront configuration's capacity, which the queue
+                                 holds while requests wait); 0 = WR_SERVE_DEFAULT_PATHS */
     uint32_t reserved;        /* 0 */
 } wr_serve_desc;
 /* Every bounce of a request's paths waits for one pass of the bounce loop over
  * the whole queue, so a shorter queue than the renderer's 2^24 cuts the
- * latency of small requests; on GB300 2^22 paths keep 98 % of the
- * throughput. */
+ * latency of small requests; on GB300 2^22 paths keep 97 % of the
+ * throughput, and a saturated loop (requests waiting) uses the full queue. */
 #define WR_SERVE_DEFAULT_PATHS 4194304u
 /* Queue slots freed by finished paths go to the running requests in
  * admission order (first come, first served) instead of in equal shares to

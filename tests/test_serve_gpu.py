@@ -73,9 +73,10 @@ def test_serving_image_matches_wr_render(sctx):
 
 @pytest.mark.parametrize("paths", [4096, 1 << 16])
 def test_queue_length_does_not_change_images(sctx, paths):
-    """wr_serve_desc.paths_in_flight sets the serving queue's length (a
-    request's paths then pass through it in many more rounds); the images
-    stay those of wr_render, and lengths outside 1024 .. 2^25 are refused."""
+    """wr_serve_desc.paths_in_flight sets the serving queue's length while no
+    request waits for admission (a request's paths then pass through it in
+    many more rounds); the images stay the same, and lengths outside
+    1024 .. 2^25 are refused."""
     ctx, ids = sctx
     srv = Server(ctx, paths_in_flight=paths)
     try:

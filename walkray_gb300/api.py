@@ -247,7 +247,8 @@ class Server:
                  paths_in_flight: int = 0):
         """`fifo`: queue slots go to the requests in admission order instead
         of in equal shares (WR_SERVE_FIFO); `paths_in_flight`: the queue
-        length while serving (0 = 2^22, WR_SERVE_DEFAULT_PATHS)."""
+        length while no request waits for admission (0 = 2^22,
+        WR_SERVE_DEFAULT_PATHS; the full capacity while requests wait)."""
         self.ctx = ctx
         d = L.wr_serve_desc(film_bytes, max_active, L.WR_SERVE_FIFO if fifo else 0, paths_in_flight, 0)
         ctx._check(ctx.lib.wr_serve_start(ctx.h, C.byref(d)))

@@ -10,9 +10,12 @@
 // or admission order with WR_SERVE_FIFO) -- (3) reads the per-job path
 // counters and retires
 // every request whose paths have all reached its film (copy to the host,
-// free the arena block and the slot).  The serving queue is shorter than the
-// renderer's (wr_serve_desc.paths_in_flight, 2^22 by default): a request's
-// every bounce waits for one pass of the loop over the whole queue.  New requests therefore join while
+// free the arena block and the slot).  The queue length adapts to the load:
+// while no request waits for admission it holds wr_serve_desc.paths_in_flight
+// paths (2^22 by default), because every bounce of a request waits for one
+// pass of the loop over the whole queue and a short queue keeps small
+// requests fast; while requests wait (the loop is saturated) it holds the
+// renderer's full capacity, which gives the most paths per second.  New requests therefore join while
 // older ones run, and their paths share the same queues; a request's image
 // depends only on its own seed, not on what else is in flight.
 #include <algorithm>
@@ -102,6 +105,7 @@ struct Server {
     std::vector<wr_req_id> slot_owner;
     std::vector<int> order;  // active slots in admission order
     uint32_t max_active = 64;
+    uint32_t short_queue = WR_SERVE_DEFAULT_PATHS;  // queue length while nobody waits for admission
     DeviceBuffer arena_mem;
     Arena arena;
     std::chrono::steady_clock::time_point t0;
@@ -130,6 +134,7 @@ struct Server {
             std::vector<WfSlotUpdate> ups;
             std::vector<int> ord;
             bool have_work;
+            uint32_t want_queue = short_queue;
             {
                 std::unique_lock<std::mutex> lk(mu);
                 if (stop) break;
@@ -181,13 +186,14 @@ struct Server {
                 for (int s : order)
                     if (!reqs[slot_owner[s]].cancel) ord.push_back(s);
                 have_work = !order.empty();
+                want_queue = pending.empty() ? short_queue : wf_config(E).capacity;
                 if (!have_work && ups.empty()) {
                     cv.wait_for(lk, std::chrono::milliseconds(2));
                     continue;
                 }
             }
-            int rc = WR_OK;
-            if (!ups.empty() || ord != last_order) rc = wf_update_jobs(ctx, E, ups, ord, stream);
+            int rc = wf_set_live_cap(ctx, E, want_queue, stream);
+            if (rc == WR_OK && (!ups.empty() || ord != last_order)) rc = wf_update_jobs(ctx, E, ups, ord, stream);
             last_order = ord;
             if (rc == WR_OK && have_work) rc = wf_launch(ctx, E, stream);
             if (rc == WR_OK) rc = wf_read_counters(ctx, E, cnt, stream);
@@ -272,11 +278,10 @@ int wr_serve_start(wr_ctx* ctx, const wr_serve_desc* desc) {
         const uint32_t pif = desc && desc->paths_in_flight ? desc->paths_in_flight : WR_SERVE_DEFAULT_PATHS;
         if (pif < 1024 || pif > (1u << 25) || (desc && desc->reserved))
             return set_error(ctx, WR_ERR_INVALID_ARGUMENT, "paths_in_flight must be 1024 .. 2^25, reserved 0");
-        // the serving queue: no longer than the renderer's
-        WfConfig cfg = wf_tuned_config(ctx);
-        cfg.capacity = std::min(cfg.capacity, pif);
-        int rc = wf_engine_get(ctx, cfg, &S->E);
+        int rc = wf_engine_get(ctx, wf_tuned_config(ctx), &S->E);
         if (rc != WR_OK) return rc;
+        S->short_queue = std::min(pif, wf_config(S->E).capacity);
+        if ((rc = wf_set_live_cap(ctx, S->E, S->short_queue, S->stream)) != WR_OK) return rc;
         if ((rc = wf_set_equal_share(ctx, S->E, !(desc && (desc->flags & WR_SERVE_FIFO)))) != WR_OK) return rc;
         // start from an empty job table and empty queues
         std::vector<WfSlotUpdate> clear;

@@ -455,7 +455,9 @@ __global__ void __launch_bounds__(128) k_wf_drain(const RenderScene* __restrict_
 // a small request admitted behind a large one starts at once), capped by what
 // it has left; slots nobody's share used go to the jobs in admission order.
 // With `equal_share` off, every slot goes in admission order (first come,
-// first served).  The plan reserves each job's index range [first, first +
+// first served).  The queue is filled up to *live_cap paths (at most its
+// capacity): a word in device memory, so that the serving loop can shorten
+// the queue without recapturing the bounce loop.  The plan reserves each job's index range [first, first +
 // quota) by advancing its claim counter; the generate kernel then maps queue
 // position t to a job and a path index without atomics.  Which paths a job
 // renders does not depend on the plan, only when.
@@ -476,13 +478,15 @@ __device__ __forceinline__ unsigned long long block_excl_scan(unsigned long long
 
 __global__ void __launch_bounds__(WF_MAX_JOBS) k_wf_plan(const WfJob* __restrict__ jobs, const int* __restrict__ order,
                                                           WfJobCounters* __restrict__ counters, WfSide Y,
-                                                          uint32_t capacity, int equal_share, WfPlan P) {
+                                                          uint32_t capacity, const uint32_t* __restrict__ live_cap,
+                                                          int equal_share, WfPlan P) {
     __shared__ unsigned long long buf[WF_MAX_JOBS];
     __shared__ unsigned long long s_total_q;
     const int n = order[0];
     const int k = threadIdx.x;
     const uint32_t survivors = Y.counts[0];
-    const unsigned long long free_slots = capacity > survivors ? capacity - survivors : 0u;
+    const uint32_t cap = min(capacity, *live_cap);
+    const unsigned long long free_slots = cap > survivors ? cap - survivors : 0u;
     int j = -1;
     unsigned long long rem = 0, claimed = 0;
     if (k < n) {
@@ -594,6 +598,8 @@ struct WfEngine {
     WfSide side[2];
     WfPlan plan{};
     int equal_share = 1;  // the plan's policy (captured into the graph)
+    DeviceBuffer live_cap;     // uint32: paths the plan fills the queue up to
+    uint32_t live_cap_host = 0;
     WfShadow shadow{};
     WfSort sort{};
     int grid_sort = 0;
@@ -687,6 +693,9 @@ int wf_engine_get(wr_ctx* ctx, const WfConfig& cfg, WfEngine** out) {
     WR_CUDA(ctx, cudaMemset(E->counters.p, 0, sizeof(WfJobCounters) * WF_MAX_JOBS));
     WR_CUDA(ctx, E->work.reserve(sizeof(unsigned long long)));
     WR_CUDA(ctx, E->err_word.reserve(sizeof(unsigned int)));
+    WR_CUDA(ctx, E->live_cap.reserve(sizeof(uint32_t)));
+    E->live_cap_host = cfg.capacity;
+    WR_CUDA(ctx, cudaMemcpy(E->live_cap.p, &E->live_cap_host, sizeof(uint32_t), cudaMemcpyHostToDevice));
     WR_CUDA(ctx, cudaMemset(E->err_word.p, 0, sizeof(unsigned int)));
     // the job counters, then one extra record for the queue counts of side 0
     WR_CUDA(ctx, cudaMallocHost(&E->host_counters, sizeof(WfJobCounters) * (WF_MAX_JOBS + 1)));
@@ -836,7 +845,8 @@ static void enqueue_iteration(WfEngine* E, int x, cudaStream_t s, cudaEvent_t* e
     k_wf_shadow<<<E->grid_shadow, E->cfg.extend_block, E->smem_shadow, s>>>(scenes, jobs, E->shadow, E->side[y],
                                                                            E->stack_cap, E->err_word.as<unsigned int>());
     if (ev) cudaEventRecord(ev[3], s);
-    k_wf_plan<<<1, WF_MAX_JOBS, 0, s>>>(jobs, E->order.as<int>(), cnt, E->side[y], E->cfg.capacity, E->equal_share,
+    k_wf_plan<<<1, WF_MAX_JOBS, 0, s>>>(jobs, E->order.as<int>(), cnt, E->side[y], E->cfg.capacity,
+                                        E->live_cap.as<uint32_t>(), E->equal_share,
                                         E->plan);
     k_wf_generate<<<E->grid_gen, E->cfg.shade_block, 0, s>>>(jobs, E->plan, E->side[y]);
     if (ev) cudaEventRecord(ev[4], s);
@@ -850,6 +860,7 @@ int profile_wavefront(wr_ctx* ctx, RenderData& rd, const RenderParams& P, uint32
     int rc = wf_engine_get(ctx, wf_tuned_config(ctx), &E);
     if (rc != WR_OK) return rc;
     cudaStream_t s = ctx->stream;
+    if ((rc = wf_set_live_cap(ctx, E, wf_config(E).capacity, s)) != WR_OK) return rc;
     const RenderScene& S = RenderDataView::scene(&rd);
     WfSlotUpdate u;
     u.slot = 0;
@@ -1009,6 +1020,17 @@ int wf_set_equal_share(wr_ctx* ctx, WfEngine* E, bool on) {
     return WR_OK;
 }
 
+int wf_set_live_cap(wr_ctx* ctx, WfEngine* E, uint32_t paths, cudaStream_t s) {
+    paths = std::max<uint32_t>(1, std::min(paths, E->cfg.capacity));
+    if (paths == E->live_cap_host) return WR_OK;
+    E->live_cap_host = paths;
+    // from pageable memory: the call has read `paths` when it returns
+    WR_CUDA(ctx, cudaMemcpyAsync(E->live_cap.p, &paths, sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    return WR_OK;
+}
+
+uint32_t wf_live_cap(const WfEngine* E) { return E->live_cap_host; }
+
 int wf_reset_queues(wr_ctx* ctx, WfEngine* E, cudaStream_t s) {
     for (int k = 0; k < 2; k++) WR_CUDA(ctx, cudaMemsetAsync(E->side[k].counts, 0, 2 * sizeof(unsigned int), s));
     return WR_OK;
@@ -1039,6 +1061,7 @@ int render_wavefront(wr_ctx* ctx, RenderData& rd, const RenderParams& P, uint32_
     WfEngine* E = nullptr;
     int rc = wf_engine_get(ctx, wf_tuned_config(ctx), &E);
     if (rc != WR_OK) return rc;
+    if ((rc = wf_set_live_cap(ctx, E, wf_config(E).capacity, s)) != WR_OK) return rc;  // the whole queue
     const RenderScene& S = RenderDataView::scene(&rd);
     WfSlotUpdate u;
     u.slot = 0;

@@ -156,6 +156,10 @@ int wf_reset_queues(wr_ctx* ctx, WfEngine* E, cudaStream_t s);
 // free queue slots shared equally among the jobs with paths left (default)
 // or handed out in admission order
 int wf_set_equal_share(wr_ctx* ctx, WfEngine* E, bool on);
+// the queue is filled up to `paths` (clamped to 1 .. capacity; capacity when
+// the engine is made); takes effect from the next bounce loop on stream s
+int wf_set_live_cap(wr_ctx* ctx, WfEngine* E, uint32_t paths, cudaStream_t s);
+uint32_t wf_live_cap(const WfEngine* E);
 const WfConfig& wf_config(const WfEngine* E);
 int wf_set_config(wr_ctx* ctx, const WfConfig& cfg);
 WfConfig wf_tuned_config(wr_ctx* ctx);
