@@ -10,7 +10,11 @@ every material, through the C ABI:
   and the heterogeneous grid (render_pt_*.npz);
 * per-pixel pairing with the oracle on the same random streams (same draws
   per path) on the mixed-material, media and anisotropic scenes, the rule
-  the Cornell box is held to in test_render_gpu.py.
+  the Cornell box is held to in test_render_gpu.py;
+* the same pairing at configurations 2 and 3 as configured (the 1024^2
+  mixed-material scene of 512,006 triangles, depth 16; the 512^2 Cornell
+  box with both media, depth 24) on a band of rows the oracle renders in
+  seconds, through the wavefront renderer the benchmark times.
 """
 import os
 
@@ -130,3 +134,27 @@ def test_per_pixel_paired_with_oracle(ctx, name, depth, flags, mean_tol):
     assert np.median(d) < 0.05, np.median(d)
     assert np.mean(d > 3) < 0.01, np.mean(d > 3)
     assert abs(gmean / omean - 1) < mean_tol, (gmean, omean)
+
+
+@pytest.mark.parametrize("name,depth,flags,spp,rows", [
+    ("mixed_1024", 16, 0, 16, (448, 576)),
+    ("media_512", 24, wr_oracle.DELTA, 32, (224, 288)),
+])
+def test_configuration_scenes_paired_with_oracle(ctx, name, depth, flags, spp, rows):
+    """Configurations 2 and 3 at their own resolution, scene and depth: the
+    wavefront renderer's per-pixel estimates on a band of rows against the
+    oracle's on the same streams, by the rule of the paired test above."""
+    s = S.mixed_spheres(1024, 1024, seed=7) if name == "mixed_1024" else S.cornell_media(512, 512)
+    sid = ctx.upload(s)
+    gsum, gsq = ctx.render_stats(sid, spp, depth, seed=91, mode="wavefront")
+    ctx.release(sid)
+    w = s.camera.width
+    p0, p1 = rows[0] * w, rows[1] * w
+    osum, osq, _ = wr_oracle.SceneOracle(s).render(spp, depth, seed=91, flags=flags, p0=p0, p1=p1, want_sumsq=True)
+    gm = gsum[rows[0]:rows[1]].reshape(-1, 3) / spp
+    om = osum / spp
+    sem = np.sqrt(np.maximum(osq / spp - om * om, 0) / spp) + 1e-6
+    d = np.abs(gm - om) / sem
+    assert np.median(d) < 0.05, np.median(d)
+    assert np.mean(d > 3) < 0.01, np.mean(d > 3)
+    assert abs(gm.mean() / om.mean() - 1) < 0.01, (gm.mean(), om.mean())
