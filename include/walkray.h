@@ -188,7 +188,9 @@ typedef struct wr_trace_filter {
 } wr_trace_filter;
 
 /* Closest hit of n rays (origin xyz, direction xyz; n x 6 floats).  Host
- * buffers: the call copies rays to the device and hits back.
+ * buffers: the call copies rays to the device and hits back, from 2^20 rays
+ * on in 2 or 4 chunks whose copies overlap the other chunks' traversal
+ * (page-locked buffers let the copies run asynchronously).
  * Replaces KDTree::intersect (kdtree.cpp:349-353) and Scene::intersect
  * (scene.cpp:102-113). */
 int wr_trace_closest(wr_ctx* ctx, wr_scene_id scene, const float* rays, uint64_t n,

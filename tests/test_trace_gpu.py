@@ -187,8 +187,9 @@ def test_device_entry_point_matches_host_entry_point(ctx):
 
 
 def test_large_filtered_host_batch_matches_device_entry_point(ctx):
-    """4.5 M filtered rays through the host-buffer entry point: the same hits
-    as the device-buffer entry point."""
+    """4.5 M filtered rays through the host-buffer entry point (four chunks
+    through its copy pipeline): the same hits as the device-buffer entry
+    point."""
     torch = pytest.importorskip("torch")
     s = make_golden.golden_scenes()["mixed_l2"]
     n = 4_500_000

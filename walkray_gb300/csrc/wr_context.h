@@ -74,6 +74,10 @@ struct wr_ctx {
     wr::DeviceBuffer rays, hits, inside, contact;
     wr::DeviceBuffer scratch_words;  // counters / error flags
     wr::DeviceBuffer film;           // wr_render's image, kept between calls (no allocation per call)
+    // wr_trace_closest's copy pipeline: host-to-device and device-to-host
+    // streams beside `stream` (which runs the kernels), and its events
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;
+    cudaEvent_t pipe_ev[9] = {};
     bool trace_prune = true;  // wr_trace_closest skips boxes beyond the closest hit (WR_CTX_EXACT_TRAVERSAL: never)
     int last_trace_blocks = 0;
     uint64_t kernel_launches = 0;  // kernels this library has launched on the context
