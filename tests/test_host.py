@@ -1,10 +1,12 @@
 """Host-side logic of the library without a GPU: the C ABI loads and exports
-every declared entry point, the host tree equals the reference tree, and the
-boundary rejects malformed input."""
+every declared entry point, the Python binding's structures have the
+header's sizes and field offsets, the host tree equals the reference tree,
+and the boundary rejects malformed input."""
 import ctypes as C
 import hashlib
 import json
 import os
+import subprocess
 
 import numpy as np
 import pytest
@@ -24,6 +26,35 @@ def test_library_exports_declared_symbols(built):
     assert not missing, missing
     v = C.c_uint32()
     assert lib.wr_get_abi_version(C.byref(v)) == 0 and v.value == 2
+
+
+ABI_STRUCTS = ["wr_object_desc", "wr_camera_desc", "wr_grid_desc", "wr_scene_desc", "wr_scene_file_settings",
+               "wr_hit", "wr_scene_info", "wr_ctx_desc", "wr_trace_filter", "wr_render_desc",
+               "wr_wavefront_config", "wr_serve_desc", "wr_request_desc", "wr_req_status", "wr_render_profile"]
+
+
+def test_binding_structs_match_header(tmp_path):
+    """Every structure the ctypes binding passes across the C ABI has the
+    size and field offsets that include/walkray.h gives it (a C program
+    compiled against the header prints them)."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "walkray.h"', "int main(void) {"]
+    for name in ABI_STRUCTS:
+        lines.append(f'printf("{name} %zu\\n", sizeof({name}));')
+        for f, _ in getattr(L, name)._fields_:
+            lines.append(f'printf("{name}.{f} %zu\\n", offsetof({name}, {f}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(root, "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(line.split() for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                       text=True).stdout.splitlines())
+    for name in ABI_STRUCTS:
+        T = getattr(L, name)
+        assert int(got[name]) == C.sizeof(T), (name, got[name], C.sizeof(T))
+        for f, _ in T._fields_:
+            assert int(got[f"{name}.{f}"]) == getattr(T, f).offset, (name, f)
 
 
 @pytest.mark.parametrize("name", ["cornell", "ico4", "mixed_l2", "media_small"])
