@@ -106,7 +106,8 @@ __device__ __forceinline__ uint32_t warp_append(unsigned int* counter, bool want
 __global__ void k_wf_reset(WfSide Y, unsigned long long* work, unsigned int* shadow_count, WfSort B) {
     Y.counts[0] = 0;
     Y.counts[1] = 0;
-    *work = 0;
+    work[0] = 0;  // the extend stage's ray counter
+    work[1] = 0;  // the shadow stage's
     *shadow_count = 0;
     for (int k = 0; k < WF_SORT_KEYS; k++) B.counts[k] = 0;
 }
@@ -160,22 +161,22 @@ __device__ __forceinline__ void film_add(const WfJob& J, uint32_t pixel, f3 resu
     }
 }
 
-// shadow stage: visibility of every NEE connection and light connection
-// (WF_SHADOW_*): visible contributions to the film or to their path
+// shadow stage, second half: with the closest hit of every NEE connection
+// and light connection (WF_SHADOW_*) from k_wf_shadow_trace, the visible
+// contributions go to the film or to their path
 __global__ void __launch_bounds__(128) k_wf_shadow(const RenderScene* __restrict__ scenes,
-                                                     const WfJob* __restrict__ jobs, WfShadow Q, WfSide Y,
-                                                     int stack_cap, unsigned int* __restrict__ err) {
-    extern __shared__ uint32_t s_stack[];
-    uint32_t* stack = s_stack + threadIdx.x;
+                                                     const WfJob* __restrict__ jobs, WfShadow Q,
+                                                     const int2* __restrict__ hits, WfSide Y) {
     const uint32_t n = *Q.count;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 o = Q.o[i], d = Q.d[i], c = Q.c[i];
         const int4 ids = Q.ids[i];
         const WfJob& J = jobs[ids.z];
         const RenderScene& S = scenes[J.scene];
-        RayQ q = make_rayq(mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), S.tree.scene_mag);
-        q.pf = prune_factor(J.flags);
-        const Hit h = trace_closest<true, true>(S.tree, q, ids.x, ids.y, stack, blockDim.x, stack_cap, err);
+        const int2 hv = hits[i];
+        Hit h;
+        h.slot = hv.x;
+        h.t = __int_as_float(hv.y);
         const int kind = __float_as_int(c.w);
         const f3 contrib = mk(c.x, c.y, c.z);
         if (kind == WF_SHADOW_NEE) {
@@ -267,6 +268,58 @@ __global__ void WR_EXTEND_BOUNDS(MINB) k_wf_extend(const RenderScene* __restrict
 
 using ExtendKernel = void (*)(const RenderScene*, const WfJob*, WfSide, int2*, unsigned long long*, int, TraceTune,
                               unsigned int*, unsigned long long*);
+
+// shadow stage, first half: the closest hit of every connection in the
+// shadow queue, through the same warp-persistent loop as extend (filtered by
+// the connection's inside / contact objects, as trace_closest<true, true>)
+struct ShadowSrc {
+    const RenderScene* __restrict__ scenes;
+    const WfJob* __restrict__ jobs;
+    WfShadow Q;
+    int2* __restrict__ hits;
+
+    __device__ __forceinline__ void load(uint64_t id, TraceLane& L, uint32_t* stack, int stride) {
+        const float4 o = Q.o[id], d = Q.d[id];
+        const int4 ids = Q.ids[id];
+        const WfJob& J = jobs[ids.z];
+        const DevTree& T = scenes[J.scene].tree;
+        L.pairs = T.pairs;
+        L.tris = T.tris;
+        L.q = make_rayq(mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), T.scene_mag);
+        L.q.pf = prune_factor(J.flags);
+        L.inside = ids.x;
+        L.contact = ids.y;
+        L.filt = true;
+        const Box root{T.root_lo[0], T.root_lo[1], T.root_lo[2], T.root_hi[0], T.root_hi[1], T.root_hi[2]};
+        lane_start(L, root, T.root_w0, T.root_w1, stack, stride);
+    }
+    __device__ __forceinline__ void store(uint64_t id, const TraceLane& L) {
+        hits[id] = make_int2(L.h.slot, __float_as_int(L.h.t));
+    }
+};
+
+template <int MINB>
+__global__ void WR_EXTEND_BOUNDS(MINB)
+    k_wf_shadow_trace(const RenderScene* __restrict__ scenes, const WfJob* __restrict__ jobs, WfShadow Q,
+                      int2* __restrict__ hits, unsigned long long* __restrict__ work, int stack_cap, TraceTune tune,
+                      unsigned int* __restrict__ err) {
+    extern __shared__ uint32_t s_stack[];
+    const uint64_t n = *Q.count;
+    ShadowSrc src{scenes, jobs, Q, hits};
+    warp_trace<true, false>(src, n, work, tune, s_stack + threadIdx.x, blockDim.x, stack_cap, err);
+}
+
+using ShadowTraceKernel = void (*)(const RenderScene*, const WfJob*, WfShadow, int2*, unsigned long long*, int,
+                                   TraceTune, unsigned int*);
+
+// the shadow traversal for a configuration: the extend stage's register cap
+static ShadowTraceKernel shadow_trace_kernel(int ctas_per_sm) {
+    if (ctas_per_sm == 0) ctas_per_sm = 6;
+    if (ctas_per_sm >= 8) return k_wf_shadow_trace<8>;
+    if (ctas_per_sm >= 7) return k_wf_shadow_trace<7>;
+    if (ctas_per_sm >= 6) return k_wf_shadow_trace<6>;
+    return k_wf_shadow_trace<0>;
+}
 
 // the extend kernel for a configuration: register cap from ctas_per_sm
 // (0 = the 6-CTA variant, fastest on the mixed-material scene)
@@ -604,7 +657,6 @@ struct WfEngine {
     WfSort sort{};
     int grid_sort = 0;
     int grid_shadow = 0;
-    size_t smem_shadow = 0;
     std::vector<const RenderData*> scene_of;  // host mirror of the scene table
     std::vector<RenderScene> scene_tab;
     std::vector<WfJob> job_tab;               // host mirror of the job slots
@@ -691,7 +743,7 @@ int wf_engine_get(wr_ctx* ctx, const WfConfig& cfg, WfEngine** out) {
     E->plan.n = reinterpret_cast<int*>(E->plan.off + WF_MAX_JOBS + 1);
     WR_CUDA(ctx, E->counters.reserve(sizeof(WfJobCounters) * WF_MAX_JOBS));
     WR_CUDA(ctx, cudaMemset(E->counters.p, 0, sizeof(WfJobCounters) * WF_MAX_JOBS));
-    WR_CUDA(ctx, E->work.reserve(sizeof(unsigned long long)));
+    WR_CUDA(ctx, E->work.reserve(2 * sizeof(unsigned long long)));
     WR_CUDA(ctx, E->err_word.reserve(sizeof(unsigned int)));
     WR_CUDA(ctx, E->live_cap.reserve(sizeof(uint32_t)));
     E->live_cap_host = cfg.capacity;
@@ -795,12 +847,10 @@ int wf_update_jobs(wr_ctx* ctx, WfEngine* E, const std::vector<WfSlotUpdate>& up
                              &per_sm, extend_kernel(E->cfg.ctas_per_sm, false), E->cfg.extend_block, E->smem_extend));
             if (E->cfg.ctas_per_sm > 0) per_sm = std::min(per_sm, E->cfg.ctas_per_sm);
             E->grid_extend = ctx->num_sms * std::max(1, per_sm);
-            E->smem_shadow = E->smem_extend;
-            if (E->smem_shadow > 48 * 1024)
-                WR_CUDA(ctx, cudaFuncSetAttribute(k_wf_shadow, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  (int)E->smem_shadow));
-            WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_shadow, E->cfg.extend_block,
-                                                                       E->smem_shadow));
+            if (E->smem_extend > 48 * 1024)
+                WR_CUDA(ctx, cudaFuncSetAttribute(shadow_trace_kernel(E->cfg.ctas_per_sm),
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)E->smem_extend));
+            WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_shadow, 128, 0));
             E->grid_shadow = ctx->num_sms * std::max(1, per_sm);
         }
     }
@@ -842,8 +892,11 @@ static void enqueue_iteration(WfEngine* E, int x, cudaStream_t s, cudaEvent_t* e
     (E->mis_any ? k_wf_shade<true> : k_wf_shade<false>)<<<E->grid_shade, E->cfg.shade_block, 0, s>>>(scenes, jobs, cnt, E->side[x], E->hits.as<int2>(),
                                                             E->side[y], E->shadow, E->sort, E->cfg.capacity);
     if (ev) cudaEventRecord(ev[2], s);
-    k_wf_shadow<<<E->grid_shadow, E->cfg.extend_block, E->smem_shadow, s>>>(scenes, jobs, E->shadow, E->side[y],
-                                                                           E->stack_cap, E->err_word.as<unsigned int>());
+    // the connections' closest hits go into E->hits, which shade has read
+    shadow_trace_kernel(E->cfg.ctas_per_sm)<<<E->grid_extend, E->cfg.extend_block, E->smem_extend, s>>>(
+        scenes, jobs, E->shadow, E->hits.as<int2>(), E->work.as<unsigned long long>() + 1, E->stack_cap, E->cfg.trace,
+        E->err_word.as<unsigned int>());
+    k_wf_shadow<<<E->grid_shadow, 128, 0, s>>>(scenes, jobs, E->shadow, E->hits.as<int2>(), E->side[y]);
     if (ev) cudaEventRecord(ev[3], s);
     k_wf_plan<<<1, WF_MAX_JOBS, 0, s>>>(jobs, E->order.as<int>(), cnt, E->side[y], E->cfg.capacity,
                                         E->live_cap.as<uint32_t>(), E->equal_share,
@@ -884,7 +937,7 @@ int profile_wavefront(wr_ctx* ctx, RenderData& rd, const RenderParams& P, uint32
     uint32_t queued = 0;  // rays waiting in side x
     for (uint64_t it = 0;; it++) {
         enqueue_iteration(E, x, s, ev, st.as<unsigned long long>());
-        ctx->kernel_launches += 7;
+        ctx->kernel_launches += 8;
         x = 1 - x;
         WR_CUDA(ctx, cudaEventSynchronize(ev[4]));
         float a = 0, b = 0, cc = 0, d = 0;
@@ -970,7 +1023,8 @@ int wf_launch(wr_ctx* ctx, WfEngine* E, cudaStream_t s) {
         E->graph_stack = E->stack_cap;
     }
     WR_CUDA(ctx, cudaGraphLaunch(E->graph, s));
-    ctx->kernel_launches += 7ull * 2 * E->cfg.iters_per_graph;  // reset, extend, sort, shade, shadow, plan, generate
+    // reset, extend, sort, shade, shadow trace, shadow, plan, generate
+    ctx->kernel_launches += 8ull * 2 * E->cfg.iters_per_graph;
     return WR_OK;
 }
 

@@ -3,16 +3,23 @@
 //
 //   extend    persistent warps trace every queued ray (closest hit, the same
 //             bit-exact traversal as k_trace_closest)
+//   sort      buckets the queue by the material each ray hit
 //   shade     one bounce of the reference loop per path (scatter, throughput,
-//             termination); survivors are compacted into the other state
-//             buffer with warp-aggregated appends, finished paths go to their
-//             job's film
-//   generate  refills free queue slots with camera paths of the jobs in
-//             table order (continuous batching)
+//             termination) in bucket order; survivors are compacted into the
+//             other state buffer with warp-aggregated appends, finished
+//             paths go to their job's film, NEE and light connections to
+//             the shadow queue
+//   shadow    the connections' closest hits through the same persistent
+//             warp loop (k_wf_shadow_trace), then their visible
+//             contributions to the film or the path (k_wf_shadow)
+//   plan      shares the free queue slots among the jobs
+//   generate  refills free queue slots with camera paths of the jobs as
+//             planned (continuous batching)
 //
-// The [reset, extend, shade, generate] x 2 sequence (one per ping-pong side)
-// is captured once into a CUDA graph and replayed until every job is done;
-// kernel sizes never depend on host-side counts.
+// The [reset, extend, sort, shade, shadow trace, shadow, plan, generate] x 2
+// sequence (one per ping-pong side) is captured once into a CUDA graph and
+// replayed until every job is done; kernel sizes never depend on host-side
+// counts.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -80,7 +87,8 @@ struct WfSort {
     uint32_t* idx;         // bucket k at idx + k * capacity
 };
 
-// shadow rays of next-event estimation, written by shade, traced by k_wf_shadow
+// shadow rays of next-event estimation, written by shade, traced by
+// k_wf_shadow_trace and resolved by k_wf_shadow
 struct WfShadow {
     float4* o;    // origin, distance to the light sample
     float4* d;    // direction, light object (int bits; WR_RENDER_NEE_MIS)
