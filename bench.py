@@ -67,6 +67,7 @@ KD_TRI_TESTS = 2.9383
 # test 8 B topology + 24 B AABB + per triangle test 3 x 16 B vertices + 4 B id
 RAY_IO_BYTES, BOX_BYTES, TRI_BYTES = 40, 32, 52
 KD_BYTES_PER_RAY = RAY_IO_BYTES + KD_BOX_TESTS * BOX_BYTES + KD_TRI_TESTS * TRI_BYTES
+KD_WORKLOAD = "kd: level-8 displaced icosphere (1,310,720 tris), 2^24 rays (origins in 2x bounds, uniform directions)"
 
 PT_SIZE, PT_DEPTH, PT_SEED = 1024, 16, 7
 PT_SPP = 256  # samples per pixel per step: one render call of the whole configuration
@@ -290,9 +291,7 @@ def run_pt(args, world, rank, local):
         "metric": METRIC_PT, "value": round(value, 2), "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
-        "config": {"workload": "pt: 25 displaced level-5 icospheres (512,006 tris) on a ground plane, 40% diffuse / "
-                               f"40% Phong / 20% refractive, two area lights, {PT_SIZE}x{PT_SIZE}, max depth 16, "
-                               f"{PT_SPP} spp per step (one render call), the reference's estimator",
+        "config": {"workload": pt_workload(),
                    "renderer": "wavefront (generate/extend/shade/shadow queues, CUDA-graph bounce loop)",
                    "l2": "flushed (512 MiB write) before every step", "parallelism": f"replicas x{world}"},
         "e2e": {"value": round(e2e, 2), "unit": "Mpaths/s", "h2d_bytes_per_step": 256 + 4 * 257,
@@ -368,6 +367,12 @@ def run_pt(args, world, rank, local):
     return line
 
 
+def pt_workload():
+    return ("pt: 25 displaced level-5 icospheres (512,006 tris) on a ground plane, 40% diffuse / 40% Phong / "
+            f"20% refractive, two area lights, {PT_SIZE}x{PT_SIZE}, max depth 16, {PT_SPP} spp per step (one render "
+            "call), the reference's estimator")
+
+
 def reference_pt(args):
     scene = pt_scene()
     threads = os.cpu_count() or 1
@@ -376,11 +381,11 @@ def reference_pt(args):
         cpu_baseline_pt(scene, 2, threads)
     vals = [cpu_baseline_pt(scene, rows, threads) for _ in range(args.steps)]
     v = statistics.median(x["value"] for x in vals)
-    return {"metric": METRIC_PT, "value": round(v, 4), "unit": "Mpaths/s", "impl": "reference", "n_gpus": 0,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
-            "config": {"workload": "pt: 1024^2 mixed-material scene, max depth 16, 1 spp",
-                       "paths_per_step": rows * PT_SIZE},
+    return {"metric": METRIC_PT, "value": round(v, 4), "unit": "Mpaths/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+            "config": {"workload": pt_workload(), "parallelism": "host cores of rank 0",
+                       "sample_per_step": f"{rows} centre rows x {PT_SIZE} pixels x 1 spp ({rows * PT_SIZE} paths)"},
             "cpu_baseline": dict(vals[0], value=round(v, 4)),
             "e2e": {"value": round(v, 4), "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
@@ -460,8 +465,7 @@ def run_bpt(args, world, rank, local):
         "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (MIS products f64, as the reference)",
         "data": "synthetic (seeded scene generator)",
-        "config": {"workload": f"bpt: Cornell box {BPT_SIZE}x{BPT_SIZE}, max depth {BPT_DEPTH}, {BPT_SPP} spp per step "
-                               "(one render call), BidirectionalPathTracer semantics",
+        "config": {"workload": bpt_workload(),
                    "l2": "flushed (512 MiB write) before every step", "parallelism": f"replicas x{world}"},
         "e2e": {"value": round(e2e, 3), "unit": "Msamples/s", "h2d_bytes_per_step": 256 + 4 * 257,
                 "d2h_bytes_per_step": npix * 12},
@@ -493,17 +497,22 @@ def run_bpt(args, world, rank, local):
     return line
 
 
+def bpt_workload():
+    return (f"bpt: Cornell box {BPT_SIZE}x{BPT_SIZE}, max depth {BPT_DEPTH}, {BPT_SPP} spp per step (one render call), "
+            "BidirectionalPathTracer semantics")
+
+
 def reference_bpt(args):
     scene = bpt_scene()
     threads = os.cpu_count() or 1
     spp = args.cpu_rows or 1
     vals = [cpu_baseline_bpt(scene, spp, threads) for _ in range(args.steps)]
     v = statistics.median(x["value"] for x in vals)
-    return {"metric": METRIC_BPT, "value": round(v, 4), "unit": "Msamples/s", "impl": "reference", "n_gpus": 0,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
-            "config": {"workload": f"bpt: Cornell box {BPT_SIZE}x{BPT_SIZE}, max depth {BPT_DEPTH}",
-                       "samples_per_step": BPT_SIZE * BPT_SIZE * spp},
+    return {"metric": METRIC_BPT, "value": round(v, 4), "unit": "Msamples/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+            "config": {"workload": bpt_workload(), "parallelism": "host cores of rank 0",
+                       "sample_per_step": f"{spp} spp of the {BPT_SIZE}x{BPT_SIZE} image"},
             "cpu_baseline": dict(vals[0], value=round(v, 4)),
             "e2e": {"value": round(v, 4), "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
@@ -847,8 +856,7 @@ def run_kd(args, world, rank, local):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(ms_max / args.steps, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": "kd: level-8 displaced icosphere (1,310,720 tris), 2^24 rays (origins in 2x bounds, "
-                               "uniform directions)", "rays_per_step": n, "l2": "flushed (512 MiB write) before every step",
+        "config": {"workload": KD_WORKLOAD, "rays_per_step": n, "l2": "flushed (512 MiB write) before every step",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": round(e2e, 2), "unit": "Mrays/s", "h2d_bytes_per_step": n * 24, "d2h_bytes_per_step": n * 16},
         "roofline": {"bound": "hbm", "kernel": "k_trace_closest", "achieved": round(achieved, 1), "peak": peak,
@@ -873,11 +881,11 @@ def reference_kd(args):
     v = statistics.median(x["value"] for x in vals)
     cb = dict(vals[0], value=round(v, 3))
     return {"metric": "Mrays/s (closest hit, bit-exact vs reference)", "value": round(v, 3), "unit": "Mrays/s",
-            "impl": "reference", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+            "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded)",
-            "config": {"workload": "kd: level-8 displaced icosphere (1,310,720 tris), 2^24 rays",
-                       "rays_per_step": sample},
+            "config": {"workload": KD_WORKLOAD, "parallelism": "host cores of rank 0",
+                       "sample_per_step": f"{sample} of the 2^24 rays"},
             "cpu_baseline": cb, "e2e": {"value": round(v, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0,
                                         "d2h_bytes_per_step": 0}}
 
