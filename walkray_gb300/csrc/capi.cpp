@@ -257,6 +257,61 @@ int wr_trace_closest_device(wr_ctx* ctx, wr_scene_id id, const float* d_rays, ui
     return WR_OK;
 }
 
+// wr_trace_closest's copies and launches: rays in on `sin`, chunks traced on
+// the context's stream, hits (and, last, the error word into *herr) out on
+// `sout`; the caller synchronises all three
+static cudaError_t enqueue_trace(wr_ctx* ctx, SceneGPU* sc, const float* rays, uint64_t n,
+                                 const wr_trace_filter* filter, wr_hit* hits, int K, cudaStream_t sin,
+                                 cudaStream_t sout, unsigned int* herr) {
+    cudaStream_t s = ctx->stream;
+    unsigned long long* counter = ctx->scratch_words.as<unsigned long long>();
+    unsigned int* err = reinterpret_cast<unsigned int*>(counter + 1);
+    const TraceTune tt = trace_tune_of(ctx);
+    cudaError_t e = cudaMemsetAsync(err, 0, sizeof(unsigned int), s);
+#define WR_TRY(call)                     \
+    do {                                 \
+        if (e == cudaSuccess) e = (call); \
+    } while (0)
+    if (K > 1) {  // the copies wait for earlier work on the context's stream (it may still use the buffers)
+        WR_TRY(cudaEventRecord(ctx->pipe_ev[8], s));
+        WR_TRY(cudaStreamWaitEvent(sin, ctx->pipe_ev[8], 0));
+        WR_TRY(cudaStreamWaitEvent(sout, ctx->pipe_ev[8], 0));
+    }
+    const uint64_t chunk = (n + K - 1) / K;
+    for (int k = 0; k < K && e == cudaSuccess; k++) {
+        const uint64_t a = k * chunk, m = std::min<uint64_t>(n, a + chunk) - a;
+        if (m == 0) break;
+        WR_TRY(cudaMemcpyAsync(ctx->rays.as<float>() + 6 * a, rays + 6 * a, m * 6 * sizeof(float),
+                               cudaMemcpyHostToDevice, sin));
+        if (filter) {
+            WR_TRY(cudaMemcpyAsync(ctx->inside.as<int32_t>() + a, filter->inside_obj + a, m * 4,
+                                   cudaMemcpyHostToDevice, sin));
+            WR_TRY(cudaMemcpyAsync(ctx->contact.as<int32_t>() + a, filter->contact_obj + a, m * 4,
+                                   cudaMemcpyHostToDevice, sin));
+        }
+        if (K > 1) {
+            WR_TRY(cudaEventRecord(ctx->pipe_ev[2 * k], sin));
+            WR_TRY(cudaStreamWaitEvent(s, ctx->pipe_ev[2 * k], 0));
+        }
+        WR_TRY(launch_trace_closest(sc->tree, ctx->rays.as<float>() + 6 * a, m,
+                                    filter ? ctx->inside.as<int32_t>() + a : nullptr,
+                                    filter ? ctx->contact.as<int32_t>() + a : nullptr, ctx->hits.as<wr_hit>() + a,
+                                    counter, err, ctx->num_sms, ctx->trace_prune, s, &ctx->last_trace_blocks, &tt,
+                                    ctx->wf_ctas_per_sm));
+        if (e == cudaSuccess) ctx->kernel_launches++;
+        if (K > 1) {
+            WR_TRY(cudaEventRecord(ctx->pipe_ev[2 * k + 1], s));
+            WR_TRY(cudaStreamWaitEvent(sout, ctx->pipe_ev[2 * k + 1], 0));
+        }
+        WR_TRY(cudaMemcpyAsync(hits + a, ctx->hits.as<wr_hit>() + a, m * sizeof(wr_hit), cudaMemcpyDeviceToHost,
+                               sout));
+    }
+    // the error word after the last kernel (sout waited for it)
+    WR_TRY(cudaMemcpyAsync(herr, err, sizeof *herr, cudaMemcpyDeviceToHost, sout));
+#undef WR_TRY
+    return e;
+}
+
 int wr_trace_closest(wr_ctx* ctx, wr_scene_id id, const float* rays, uint64_t n, const wr_trace_filter* filter,
                      wr_hit* hits) {
     if (!ctx) return WR_ERR_INVALID_ARGUMENT;
@@ -275,61 +330,28 @@ int wr_trace_closest(wr_ctx* ctx, wr_scene_id id, const float* rays, uint64_t n,
         WR_CUDA(ctx, ctx->inside.reserve(n * sizeof(int32_t)));
         WR_CUDA(ctx, ctx->contact.reserve(n * sizeof(int32_t)));
     }
-    cudaStream_t s = ctx->stream;
-    unsigned long long* counter = ctx->scratch_words.as<unsigned long long>();
-    unsigned int* err = reinterpret_cast<unsigned int*>(counter + 1);
-    WR_CUDA(ctx, cudaMemsetAsync(err, 0, sizeof(unsigned int), s));
-    const TraceTune tt = trace_tune_of(ctx);
     // K chunks in a pipeline: chunk k's rays go in on copy_in while chunk k-1
     // is traced on `stream` and chunk k-2's hits come out on copy_out (2^24
     // rays: 6.7 -> 5.3 ms with 4 chunks on GB300; with 8 the chunks' launch
     // tails cost more than the overlap saves)
     const int K = n >= (1ull << 22) ? 4 : (n >= (1ull << 20) ? 2 : 1);
-    if (K > 1 && !ctx->copy_in) {
-        WR_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking));
+    if (K > 1 && !ctx->copy_out) {  // made once per context; copy_out last, so that it marks them all made
+        if (!ctx->copy_in) WR_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking));
+        for (cudaEvent_t& e : ctx->pipe_ev)
+            if (!e) WR_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         WR_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking));
-        for (cudaEvent_t& e : ctx->pipe_ev) WR_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
+    cudaStream_t s = ctx->stream;
     cudaStream_t sin = K > 1 ? ctx->copy_in : s, sout = K > 1 ? ctx->copy_out : s;
-    if (K > 1) {  // the copies wait for earlier work on the context's stream (it may still read the buffers)
-        WR_CUDA(ctx, cudaEventRecord(ctx->pipe_ev[8], s));
-        WR_CUDA(ctx, cudaStreamWaitEvent(sin, ctx->pipe_ev[8], 0));
-        WR_CUDA(ctx, cudaStreamWaitEvent(sout, ctx->pipe_ev[8], 0));
-    }
-    const uint64_t chunk = (n + K - 1) / K;
-    for (int k = 0; k < K; k++) {
-        const uint64_t a = k * chunk, m = std::min<uint64_t>(n, a + chunk) - a;
-        if (m == 0) break;
-        WR_CUDA(ctx, cudaMemcpyAsync(ctx->rays.as<float>() + 6 * a, rays + 6 * a, m * 6 * sizeof(float),
-                                     cudaMemcpyHostToDevice, sin));
-        if (filtered) {
-            WR_CUDA(ctx, cudaMemcpyAsync(ctx->inside.as<int32_t>() + a, filter->inside_obj + a, m * 4,
-                                         cudaMemcpyHostToDevice, sin));
-            WR_CUDA(ctx, cudaMemcpyAsync(ctx->contact.as<int32_t>() + a, filter->contact_obj + a, m * 4,
-                                         cudaMemcpyHostToDevice, sin));
-        }
-        if (K > 1) {
-            WR_CUDA(ctx, cudaEventRecord(ctx->pipe_ev[2 * k], sin));
-            WR_CUDA(ctx, cudaStreamWaitEvent(s, ctx->pipe_ev[2 * k], 0));
-        }
-        WR_CUDA(ctx, launch_trace_closest(sc->tree, ctx->rays.as<float>() + 6 * a, m,
-                                          filtered ? ctx->inside.as<int32_t>() + a : nullptr,
-                                          filtered ? ctx->contact.as<int32_t>() + a : nullptr,
-                                          ctx->hits.as<wr_hit>() + a, counter, err, ctx->num_sms, ctx->trace_prune, s,
-                                          &ctx->last_trace_blocks, &tt, ctx->wf_ctas_per_sm));
-        ctx->kernel_launches++;
-        if (K > 1) {
-            WR_CUDA(ctx, cudaEventRecord(ctx->pipe_ev[2 * k + 1], s));
-            WR_CUDA(ctx, cudaStreamWaitEvent(sout, ctx->pipe_ev[2 * k + 1], 0));
-        }
-        WR_CUDA(ctx, cudaMemcpyAsync(hits + a, ctx->hits.as<wr_hit>() + a, m * sizeof(wr_hit),
-                                     cudaMemcpyDeviceToHost, sout));
-    }
-    // the error word after the last kernel (sout waited for it)
     unsigned int herr = 0;
-    WR_CUDA(ctx, cudaMemcpyAsync(&herr, err, sizeof herr, cudaMemcpyDeviceToHost, sout));
-    WR_CUDA(ctx, cudaStreamSynchronize(sout));
-    if (K > 1) WR_CUDA(ctx, cudaStreamSynchronize(s));
+    const cudaError_t e = enqueue_trace(ctx, sc, rays, n, filtered ? filter : nullptr, hits, K, sin, sout, &herr);
+    // even after a failed call, nothing may still read the caller's rays or
+    // write its hits once this returns
+    const cudaError_t e_in = cudaStreamSynchronize(sin), e_k = cudaStreamSynchronize(s);
+    const cudaError_t e_out = cudaStreamSynchronize(sout);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "wr_trace_closest");
+    for (cudaError_t f : {e_in, e_k, e_out})
+        if (f != cudaSuccess) return cuda_error(ctx, f, "wr_trace_closest");
     if (herr) return set_error(ctx, WR_ERR_INTERNAL, "traversal stack overflow");
     return WR_OK;
     WR_GUARD_END
