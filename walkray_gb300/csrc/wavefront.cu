@@ -1,5 +1,8 @@
 // wavefront.cu — kernels and driver of the wavefront renderer (see
 // wavefront.h for the stage structure).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <cstring>
 #include <map>
@@ -81,6 +84,25 @@ __device__ __forceinline__ void wf_store(const WfSide& Y, uint32_t j, const WfPa
     r[WF_COL] = make_float4(p.color.x, p.color.y, p.color.z, p.cur.cnorm.y);
     r[WF_STK] = as_f4(make_int4(p.st.v0, p.st.v1, p.st.v2, p.st.v3));
     r[WF_PREV] = make_float4(p.prev_d.x, p.prev_d.y, p.prev_d.z, p.mis_pdf);
+}
+
+// The same record written into row `row` of a shared-memory tile of 128-byte
+// rows in the 128-byte swizzle of the tensor-memory-access unit (16-byte
+// chunk c of row r at chunk c ^ (r & 7)): eight consecutive rows' stores of
+// one field then fall on eight different bank groups, and the bulk tensor
+// store writes the rows to global memory unswizzled.
+__device__ __forceinline__ void wf_store_tile(float4* tile, uint32_t row, const WfPath& p) {
+    float4* r = tile + (size_t)WF_REC * row;
+    const uint32_t x = row & 7u;
+    r[WF_O ^ x] = make_float4(p.cur.o.x, p.cur.o.y, p.cur.o.z, p.cur.oP);
+    r[WF_D ^ x] = make_float4(p.cur.d.x, p.cur.d.y, p.cur.d.z, p.cur.dP);
+    r[WF_IDS ^ x] = as_f4(make_int4(p.cur.inside, p.cur.contact, p.job, (int)p.pixel));
+    r[WF_MISC ^ x] = as_f4(make_int4((int)p.sample, (int)p.dim, (int)(p.depth | ((uint32_t)p.st.n << 16)),
+                                     __float_as_int(p.cur.cnorm.z)));
+    r[WF_RAD ^ x] = make_float4(p.cur.rad.x, p.cur.rad.y, p.cur.rad.z, p.cur.cnorm.x);
+    r[WF_COL ^ x] = make_float4(p.color.x, p.color.y, p.color.z, p.cur.cnorm.y);
+    r[WF_STK ^ x] = as_f4(make_int4(p.st.v0, p.st.v1, p.st.v2, p.st.v3));
+    r[WF_PREV ^ x] = make_float4(p.prev_d.x, p.prev_d.y, p.prev_d.z, p.mis_pdf);
 }
 
 __device__ __forceinline__ void wf_store_acc(const WfSide& Y, uint32_t j, const WfPath& p) {
@@ -598,7 +620,18 @@ __device__ __forceinline__ uint32_t tile_pixel(uint32_t k, uint32_t W, uint32_t 
 // them out: queue position survivors + t belongs to the job whose planned
 // range holds t; the list lives in device memory so the captured graph does
 // not change when jobs come and go
-__global__ void __launch_bounds__(128) k_wf_generate(const WfJob* __restrict__ jobs, WfPlan P, WfSide Y) {
+// Each block builds WF_GEN_ROWS consecutive records at a time in a
+// shared-memory tile and one thread writes the tile with a bulk tensor store
+// (cp.async.bulk.tensor through `tmap`, the side's records as a 2-D tensor of
+// 32 floats x capacity rows): full 128-byte lines instead of eight 16-byte
+// pieces per record from every thread.  The tile's rows past the last new
+// path hold stale data and land past the queue's end, which nothing reads;
+// the tensor's bounds clip rows past the capacity.
+constexpr uint32_t WF_GEN_ROWS = 128;  // = the generate kernel's block size
+
+__global__ void __launch_bounds__(WF_GEN_ROWS) k_wf_generate(const WfJob* __restrict__ jobs, WfPlan P, WfSide Y,
+                                                             const __grid_constant__ CUtensorMap tmap) {
+    __shared__ __align__(1024) float4 s_tile[WF_GEN_ROWS * WF_REC];  // 16 KiB, 128-byte swizzle
     __shared__ uint32_t s_off[WF_MAX_JOBS + 1];
     __shared__ int s_slot[WF_MAX_JOBS];
     __shared__ unsigned long long s_first[WF_MAX_JOBS];
@@ -613,33 +646,52 @@ __global__ void __launch_bounds__(128) k_wf_generate(const WfJob* __restrict__ j
     __syncthreads();
     const uint32_t total = s_off[n];
     const uint32_t survivors = Y.counts[0];
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
-        int lo = 0, hi = n - 1;  // the last k with s_off[k] <= t (its range is not empty)
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (s_off[mid] <= t) lo = mid;
-            else hi = mid - 1;
+    const uint32_t tile_addr = (uint32_t)__cvta_generic_to_shared(s_tile);
+    for (uint32_t base = blockIdx.x * WF_GEN_ROWS; base < total; base += gridDim.x * WF_GEN_ROWS) {  // block-uniform
+        const uint32_t t = base + threadIdx.x;
+        if (t < total) {
+            int lo = 0, hi = n - 1;  // the last k with s_off[k] <= t (its range is not empty)
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (s_off[mid] <= t) lo = mid;
+                else hi = mid - 1;
+            }
+            const int jid = s_slot[lo];
+            const unsigned long long idx = s_first[lo] + (t - s_off[lo]);
+            const WfJob& J = jobs[jid];
+            WfPath p;
+            p.job = jid;
+            p.pixel = tile_pixel((uint32_t)(idx % J.npix), J.cam.width, J.cam.height, J.tile);
+            p.sample = J.s0 + (uint32_t)(idx / J.npix);
+            PathRng g;
+            g.init(J.seed, p.pixel, p.sample);
+            p.cur = camera_ray(J.cam, p.pixel, g);
+            p.dim = g.dim;
+            p.color = mk(1, 1, 1);
+            p.prev_d = mk(0, 0, 0);
+            p.depth = 0;
+            p.st.reset(p.cur.inside);
+            p.mis_pdf = 0.f;
+            p.acc = mk(0, 0, 0);
+            wf_store_tile(s_tile, threadIdx.x, p);
+            if (J.flags & WR_RENDER_NEE_MIS) wf_store_acc(Y, survivors + t, p);
         }
-        const int jid = s_slot[lo];
-        const unsigned long long idx = s_first[lo] + (t - s_off[lo]);
-        const WfJob& J = jobs[jid];
-        WfPath p;
-        p.job = jid;
-        p.pixel = tile_pixel((uint32_t)(idx % J.npix), J.cam.width, J.cam.height, J.tile);
-        p.sample = J.s0 + (uint32_t)(idx / J.npix);
-        PathRng g;
-        g.init(J.seed, p.pixel, p.sample);
-        p.cur = camera_ray(J.cam, p.pixel, g);
-        p.dim = g.dim;
-        p.color = mk(1, 1, 1);
-        p.prev_d = mk(0, 0, 0);
-        p.depth = 0;
-        p.st.reset(p.cur.inside);
-        p.mis_pdf = 0.f;
-        p.acc = mk(0, 0, 0);
-        wf_store(Y, survivors + t, p);
-        if (J.flags & WR_RENDER_NEE_MIS) wf_store_acc(Y, survivors + t, p);
+        // the tile's generic-proxy writes before the tensor unit reads it
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            // row survivors + base, column 0: a 16-byte-aligned start (x = 0)
+            asm volatile(
+                "cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];\n\t"
+                "cp.async.bulk.commit_group;\n\t"
+                "cp.async.bulk.wait_group.read 0;"
+                :
+                : "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(0), "r"((int)(survivors + base)), "r"(tile_addr)
+                : "memory");
+        }
+        __syncthreads();  // the tile may be written again
     }
+    if (threadIdx.x == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
 // ---------------------------------------------------------------------------
@@ -649,6 +701,7 @@ struct WfEngine {
     WfConfig cfg;
     DeviceBuffer side_mem[2], hits, scenes, jobs, order, counters, work, err_word, shadow_mem, sort_mem, plan_mem;
     WfSide side[2];
+    CUtensorMap rec_map[2];  // each side's records as a 2-D tensor (k_wf_generate's bulk stores)
     WfPlan plan{};
     int equal_share = 1;  // the plan's policy (captured into the graph)
     DeviceBuffer live_cap;     // uint32: paths the plan fills the queue up to
@@ -675,6 +728,29 @@ struct WfEngine {
 };
 
 const WfConfig& wf_config(const WfEngine* E) { return E->cfg; }
+
+// side k's records as a tensor of 32 floats x capacity rows (128-byte rows),
+// written in WF_GEN_ROWS x 32 boxes from 128-byte-swizzled shared memory
+static int map_side(wr_ctx* ctx, WfEngine* E, int k) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        cudaDriverEntryPointQueryResult q{};
+        void* fn = nullptr;
+        WR_CUDA(ctx, cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || !fn)
+            return set_error(ctx, WR_ERR_UNSUPPORTED, "the driver has no cuTensorMapEncodeTiled");
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    const cuuint64_t dims[2] = {4 * WF_REC, E->cfg.capacity};
+    const cuuint64_t strides[1] = {sizeof(float4) * WF_REC};
+    const cuuint32_t box[2] = {4 * WF_REC, WF_GEN_ROWS};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = encode(&E->rec_map[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, E->side[k].rec, dims, strides, box,
+                              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                              CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(ctx, WR_ERR_INTERNAL, "cuTensorMapEncodeTiled failed for the path records");
+    return WR_OK;
+}
 
 static int alloc_side(wr_ctx* ctx, WfEngine* E, int k) {
     const size_t Q = E->cfg.capacity;
@@ -710,6 +786,7 @@ int wf_engine_get(wr_ctx* ctx, const WfConfig& cfg, WfEngine** out) {
     E->cfg = cfg;
     for (int k = 0; k < 2; k++) {
         int rc = alloc_side(ctx, E.get(), k);
+        if (rc == WR_OK) rc = map_side(ctx, E.get(), k);
         if (rc != WR_OK) return rc;
     }
     WR_CUDA(ctx, E->hits.reserve(sizeof(int2) * (size_t)cfg.capacity));
@@ -758,7 +835,7 @@ int wf_engine_get(wr_ctx* ctx, const WfConfig& cfg, WfEngine** out) {
     WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_shade<false>, cfg.shade_block, 0));
     if (cfg.ctas_per_sm > 0) per_sm = std::min(per_sm, cfg.ctas_per_sm);
     E->grid_shade = ctx->num_sms * std::max(1, per_sm);
-    WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_generate, cfg.shade_block, 0));
+    WR_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_generate, WF_GEN_ROWS, 0));
     E->grid_gen = ctx->num_sms * std::max(1, per_sm);
     *out = E.get();
     ctx->wavefront = E;
@@ -901,7 +978,7 @@ static void enqueue_iteration(WfEngine* E, int x, cudaStream_t s, cudaEvent_t* e
     k_wf_plan<<<1, WF_MAX_JOBS, 0, s>>>(jobs, E->order.as<int>(), cnt, E->side[y], E->cfg.capacity,
                                         E->live_cap.as<uint32_t>(), E->equal_share,
                                         E->plan);
-    k_wf_generate<<<E->grid_gen, E->cfg.shade_block, 0, s>>>(jobs, E->plan, E->side[y]);
+    k_wf_generate<<<E->grid_gen, WF_GEN_ROWS, 0, s>>>(jobs, E->plan, E->side[y], E->rec_map[y]);
     if (ev) cudaEventRecord(ev[4], s);
 }
 
