@@ -720,6 +720,8 @@ struct WfEngine {
     cudaGraphExec_t graph = nullptr;
     int graph_stack = -1;
     bool mis_any = false;  // a job in the table has WR_RENDER_NEE_MIS: the shade stage with that code
+    bool conn_any = true;  // a job in the table connects to lights (NEE or MIS): the shadow stage is in the loop
+    int launches_per_iteration() const { return conn_any ? 8 : 6; }
     WfJobCounters* host_counters = nullptr;  // pinned
     ~WfEngine() {
         if (graph) cudaGraphExecDestroy(graph);
@@ -932,11 +934,16 @@ int wf_update_jobs(wr_ctx* ctx, WfEngine* E, const std::vector<WfSlotUpdate>& up
         }
     }
     // the shade stage compiled with the light-connection code only while a job needs it
-    bool mis_any = false;
-    for (int slot : order)
-        if (E->job_tab[slot].active && (E->job_tab[slot].flags & WR_RENDER_NEE_MIS)) mis_any = true;
-    if (mis_any != E->mis_any) {
+    // and the shadow stage only while a job can queue a connection
+    bool mis_any = false, conn_any = false;
+    for (int slot : order) {
+        if (!E->job_tab[slot].active) continue;
+        if (E->job_tab[slot].flags & WR_RENDER_NEE_MIS) mis_any = true;
+        if (E->job_tab[slot].flags & (WR_RENDER_NEE | WR_RENDER_NEE_MIS)) conn_any = true;
+    }
+    if (mis_any != E->mis_any || conn_any != E->conn_any) {
         E->mis_any = mis_any;
+        E->conn_any = conn_any;
         if (E->graph) {
             WR_CUDA(ctx, cudaStreamSynchronize(s));
             cudaGraphExecDestroy(E->graph);
@@ -969,11 +976,12 @@ static void enqueue_iteration(WfEngine* E, int x, cudaStream_t s, cudaEvent_t* e
     (E->mis_any ? k_wf_shade<true> : k_wf_shade<false>)<<<E->grid_shade, E->cfg.shade_block, 0, s>>>(scenes, jobs, cnt, E->side[x], E->hits.as<int2>(),
                                                             E->side[y], E->shadow, E->sort, E->cfg.capacity);
     if (ev) cudaEventRecord(ev[2], s);
-    // the connections' closest hits go into E->hits, which shade has read
-    shadow_trace_kernel(E->cfg.ctas_per_sm)<<<E->grid_extend, E->cfg.extend_block, E->smem_extend, s>>>(
-        scenes, jobs, E->shadow, E->hits.as<int2>(), E->work.as<unsigned long long>() + 1, E->stack_cap, E->cfg.trace,
-        E->err_word.as<unsigned int>());
-    k_wf_shadow<<<E->grid_shadow, 128, 0, s>>>(scenes, jobs, E->shadow, E->hits.as<int2>(), E->side[y]);
+    if (E->conn_any) {  // the connections' closest hits go into E->hits, which shade has read
+        shadow_trace_kernel(E->cfg.ctas_per_sm)<<<E->grid_extend, E->cfg.extend_block, E->smem_extend, s>>>(
+            scenes, jobs, E->shadow, E->hits.as<int2>(), E->work.as<unsigned long long>() + 1, E->stack_cap,
+            E->cfg.trace, E->err_word.as<unsigned int>());
+        k_wf_shadow<<<E->grid_shadow, 128, 0, s>>>(scenes, jobs, E->shadow, E->hits.as<int2>(), E->side[y]);
+    }
     if (ev) cudaEventRecord(ev[3], s);
     k_wf_plan<<<1, WF_MAX_JOBS, 0, s>>>(jobs, E->order.as<int>(), cnt, E->side[y], E->cfg.capacity,
                                         E->live_cap.as<uint32_t>(), E->equal_share,
@@ -1014,7 +1022,7 @@ int profile_wavefront(wr_ctx* ctx, RenderData& rd, const RenderParams& P, uint32
     uint32_t queued = 0;  // rays waiting in side x
     for (uint64_t it = 0;; it++) {
         enqueue_iteration(E, x, s, ev, st.as<unsigned long long>());
-        ctx->kernel_launches += 8;
+        ctx->kernel_launches += E->launches_per_iteration();
         x = 1 - x;
         WR_CUDA(ctx, cudaEventSynchronize(ev[4]));
         float a = 0, b = 0, cc = 0, d = 0;
@@ -1100,8 +1108,8 @@ int wf_launch(wr_ctx* ctx, WfEngine* E, cudaStream_t s) {
         E->graph_stack = E->stack_cap;
     }
     WR_CUDA(ctx, cudaGraphLaunch(E->graph, s));
-    // reset, extend, sort, shade, shadow trace, shadow, plan, generate
-    ctx->kernel_launches += 8ull * 2 * E->cfg.iters_per_graph;
+    // reset, extend, sort, shade, [shadow trace, shadow,] plan, generate
+    ctx->kernel_launches += (uint64_t)E->launches_per_iteration() * 2 * E->cfg.iters_per_graph;
     return WR_OK;
 }
 

@@ -17,7 +17,8 @@
 //             planned (continuous batching)
 //
 // The [reset, extend, sort, shade, shadow trace, shadow, plan, generate] x 2
-// sequence (one per ping-pong side) is captured once into a CUDA graph and
+// sequence (one per ping-pong side; the two shadow kernels only while a job
+// in the table connects to lights) is captured once into a CUDA graph and
 // replayed until every job is done; kernel sizes never depend on host-side
 // counts.
 #pragma once
