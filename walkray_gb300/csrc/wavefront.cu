@@ -733,16 +733,18 @@ const WfConfig& wf_config(const WfEngine* E) { return E->cfg; }
 
 // side k's records as a tensor of 32 floats x capacity rows (128-byte rows),
 // written in WF_GEN_ROWS x 32 boxes from 128-byte-swizzled shared memory
+static PFN_cuTensorMapEncodeTiled_v12000 lookup_encode_tiled() {
+    cudaDriverEntryPointQueryResult q{};
+    void* fn = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+        return nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+}
+
 static int map_side(wr_ctx* ctx, WfEngine* E, int k) {
-    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-    if (!encode) {
-        cudaDriverEntryPointQueryResult q{};
-        void* fn = nullptr;
-        WR_CUDA(ctx, cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
-        if (q != cudaDriverEntryPointSuccess || !fn)
-            return set_error(ctx, WR_ERR_UNSUPPORTED, "the driver has no cuTensorMapEncodeTiled");
-        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-    }
+    static const PFN_cuTensorMapEncodeTiled_v12000 encode = lookup_encode_tiled();  // once, thread-safe
+    if (!encode) return set_error(ctx, WR_ERR_UNSUPPORTED, "the driver has no cuTensorMapEncodeTiled");
     const cuuint64_t dims[2] = {4 * WF_REC, E->cfg.capacity};
     const cuuint64_t strides[1] = {sizeof(float4) * WF_REC};
     const cuuint32_t box[2] = {4 * WF_REC, WF_GEN_ROWS};
