@@ -935,13 +935,10 @@ def main():
     build.build_lib()
     run = {"pt": run_pt, "kd": run_kd, "serve": run_serve, "relmse": run_relmse, "bpt": run_bpt}[args.workload]
     extras = args.workload == "pt" and world == 1 and not args.no_extras
-    # the kd microbenchmark and a short serving stream in the same run; kd
-    # first: right after the pt leg, host<->device copies run slower for a few
-    # seconds on GB300 (kd e2e 3188 Mrays/s before the pt leg, 2543 right
-    # after it, 3201 after one more kd leg; the device-timed figures do not move)
-    kd = run_kd(args, world, rank, local) if extras else None
     line = run(args, world, rank, local)
     if extras:
+        # the kd microbenchmark and a short serving stream in the same run
+        kd = run_kd(args, world, rank, local)
         line["kd"] = {k: kd[k] for k in ("metric", "value", "unit", "ms_per_step", "e2e", "roofline", "config",
                                          "gpu_launches", "clocks") if k in kd}
         if "cpu_baseline" in kd:
