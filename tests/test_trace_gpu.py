@@ -186,6 +186,27 @@ def test_device_entry_point_matches_host_entry_point(ctx):
     ctx.release(sid)
 
 
+@pytest.mark.parametrize("n", [1_000_000, 1_500_000, 4_194_305])
+def test_host_batch_chunks_match_device_entry_point(ctx, n):
+    """Host batches below, in and above the two-chunk range of the copy
+    pipeline (2^20 .. 2^22 rays; 4 chunks from 2^22, here with a ragged last
+    chunk): the same hits as the device-buffer entry point."""
+    torch = pytest.importorskip("torch")
+    s = make_golden.golden_scenes()["ico4"]
+    rays = S.kd_rays(s, n, seed=31)
+    sid = ctx.upload(s)
+    want = ctx.trace_closest(sid, rays)
+    d_rays = torch.from_numpy(rays).cuda()
+    d_hits = torch.empty((n, 4), dtype=torch.int32, device="cuda")
+    ctx.trace_closest_device(sid, d_rays.data_ptr(), n, d_hits.data_ptr(),
+                             stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    got = d_hits.cpu().numpy().view(np.uint32)
+    assert np.array_equal(got[:, 0], want["tri"])
+    assert np.array_equal(got[:, 1], want["t"].view(np.uint32))
+    ctx.release(sid)
+
+
 def test_large_filtered_host_batch_matches_device_entry_point(ctx):
     """4.5 M filtered rays through the host-buffer entry point (four chunks
     through its copy pipeline): the same hits as the device-buffer entry
